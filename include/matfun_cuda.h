@@ -1,0 +1,56 @@
+/* matfun_cuda.h -- C ABI of libmatfun_cuda (GB300 / sm_103a build): batched 3x3 matrix functions exp, log, sqrt and
+ * A^alpha with first and second derivatives, on the GPU.
+ *
+ * Drop-in for the reference's CUDA library: the same three entry points, argument meaning, layouts and return codes
+ * as cuda/include/matfun/matfun_cuda.h:16-22 of BodeTobias/matfun (layouts: c/include/matfun/matfun.h:1-41).
+ *
+ * Conventions (unchanged from the reference):
+ *   - all arrays are DEVICE pointers owned by the caller, row-major, one matrix after the other;
+ *   - the work is queued on `stream` (a cudaStream_t, NULL = default stream) and the call returns without waiting;
+ *   - J and H may be NULL (H needs J); F is required;
+ *   - returns 0; -1 for invalid arguments (unknown kind, n < 0, H without J, alpha <= 0 for SMF_POW, and in this
+ *     build also a NULL input or F pointer with n > 0); -2 for a CUDA launch error or a grid the reference could not
+ *     launch (n > 32 (2^31 - 1) for smf, n > 64 (2^31 - 1) for gmf) -- then nothing is launched and no CUDA error
+ *     stays pending;
+ *   - n == 0 returns 0 without a launch;
+ *   - a matrix outside the domain (gmf: a real eigenvalue <= 0 for log / sqrt / pow) or a non-symmetric matrix in
+ *     smf_cuda_eval_matrix (|A_ij - A_ji| > 1e-8 max|A_kl|) gives NaN results for that matrix only.
+ *
+ * Layouts:
+ *   smf_cuda_eval         v (n, 6) Voigt (A11, A22, A33, A12, A13, A23) -> F (n, 6), J (n, 6, 6), H (n, 6, 6, 6)
+ *   smf_cuda_eval_matrix  A (n, 3, 3) symmetric -> F (n, 3, 3), J (n, 3,3,3,3), H (n, 3,3,3,3,3,3), the derivatives of
+ *                         A -> f((A + A^T) / 2)
+ *   gmf_cuda_eval         A (n, 3, 3) general -> F, J, H as above, the full derivatives, principal branch
+ */
+#ifndef MATFUN_GB300_CUDA_H
+#define MATFUN_GB300_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* kind codes: c/include/matfun/matfun.h:28 */
+#ifndef MATFUN_H
+enum smf_kind { SMF_EXP = 0, SMF_LOG = 1, SMF_POW = 2, SMF_SQRT = 3 };
+#endif
+
+/* replaces smf_cuda_eval, cuda/include/matfun/matfun_cuda.h:17 (implementation cuda/src/matfun_cuda.cu:199-202) */
+int smf_cuda_eval(int kind, double alpha, int64_t n, const double *v, double *F, double *J, double *H, void *stream);
+
+/* replaces smf_cuda_eval_matrix, cuda/include/matfun/matfun_cuda.h:19-20 (cuda/src/matfun_cuda.cu:204-207) */
+int smf_cuda_eval_matrix(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H,
+                         void *stream);
+
+/* replaces gmf_cuda_eval, cuda/include/matfun/matfun_cuda.h:22 (cuda/src/matfun_cuda.cu:194-197) */
+int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H, void *stream);
+
+/* version string of this library (no counterpart in the reference's CUDA header; cf. smf_version, matfun.h:51) */
+const char *matfun_cuda_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MATFUN_GB300_CUDA_H */

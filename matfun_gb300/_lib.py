@@ -1,0 +1,41 @@
+"""ctypes binding of libmatfun_cuda.so (the C ABI of include/matfun_cuda.h).
+
+The library is built in-tree (matfun_gb300/build.py); MATFUN_CUDA_LIB overrides the path, as for the reference's
+JAX plugin (python/src/matfun/jax.py:100-103).  There is no CPU fallback: loading fails loudly when the library is
+missing.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+
+KINDS = {"exp": 0, "log": 1, "pow": 2, "sqrt": 3}
+
+# exported symbol -> (restype, argtypes)
+_EVAL = [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [ctypes.c_void_p] * 5
+SIGNATURES = {
+    "smf_cuda_eval": (ctypes.c_int, _EVAL),
+    "smf_cuda_eval_matrix": (ctypes.c_int, _EVAL),
+    "gmf_cuda_eval": (ctypes.c_int, _EVAL),
+    "matfun_cuda_version": (ctypes.c_char_p, []),
+}
+
+
+def library_path():
+    return os.environ.get("MATFUN_CUDA_LIB") or os.path.join(HERE, "libmatfun_cuda.so")
+
+
+def load():
+    """the loaded library (raises OSError if it is missing: build it with matfun_gb300.build)"""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise OSError(f"libmatfun_cuda not found at {path}; run `python -m matfun_gb300.build`")
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype, fn.argtypes = res, args
+        _lib = lib
+    return _lib

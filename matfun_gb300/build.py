@@ -1,0 +1,109 @@
+"""Builds libmatfun_cuda.so (sm_103a) in-tree from matfun_gb300/csrc, and the CPU oracle library used by the tests.
+
+    python -m matfun_gb300.build            (or __graft_entry__.build())
+
+The kernel translation units (one per family and kind) are compiled in parallel with nvcc and linked into
+matfun_gb300/libmatfun_cuda.so.  Objects go to matfun_gb300/_build/ and are reused while no source changed.
+"""
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libmatfun_cuda.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
+
+
+def _nvcc():
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libmatfun_cuda")
+
+
+def _elf_native(path):
+    """True if path is an ELF file for this machine (objects built on another host architecture are rebuilt)"""
+    import platform
+    want = {"x86_64": 62, "aarch64": 183, "arm64": 183}.get(platform.machine())
+    try:
+        with open(path, "rb") as f:
+            h = f.read(20)
+    except OSError:
+        return False
+    if len(h) < 20 or h[:4] != b"\x7fELF":
+        return False
+    return want is None or int.from_bytes(h[18:20], "little") == want
+
+
+def _fresh(out, inputs_time):
+    return os.path.exists(out) and _elf_native(out) and os.path.getmtime(out) >= inputs_time
+
+
+def _newest_header():
+    hs = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
+    hs += glob.glob(os.path.join(ROOT, "include", "*.h"))
+    return max((os.path.getmtime(h) for h in hs), default=0.0)
+
+
+def _compile(src, hdr_time, verbose):
+    obj = os.path.join(OBJ, os.path.basename(src)[:-3] + ".o")
+    if _fresh(obj, max(os.path.getmtime(src), hdr_time)):
+        return obj, ""
+    cmd = [_nvcc()] + NVFLAGS + ["-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    return obj, (r.stdout + r.stderr) if verbose else ""
+
+
+def build_cuda(verbose=False, jobs=None):
+    os.makedirs(OBJ, exist_ok=True)
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    hdr = _newest_header()
+    jobs = jobs or max(1, min(len(srcs), os.cpu_count() or 4))
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        res = list(ex.map(lambda s: _compile(s, hdr, verbose), srcs))
+    objs = [o for o, _ in res]
+    for _, log in res:
+        if log:
+            print(log)
+    if not _fresh(LIB, max(os.path.getmtime(o) for o in objs)):
+        tmp = LIB + ".tmp"
+        cmd = [_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def build_oracle():
+    """the CPU restatement (oracle/oracle.c) as oracle/liboracle.so: test infrastructure, never the product path"""
+    src = os.path.join(ROOT, "oracle", "oracle.c")
+    lib = os.path.join(ROOT, "oracle", "liboracle.so")
+    if _fresh(lib, os.path.getmtime(src)):
+        return lib
+    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-fno-math-errno", "-fno-trapping-math",
+           "-o", lib + ".tmp", src, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(lib + ".tmp", lib)
+    return lib
+
+
+def build_reference_oracle(ref="/root/reference"):
+    """the reference's own CPU library (oracle/_ref/libmatfun_ref.so), only where its sources are present"""
+    if not os.path.isdir(os.path.join(ref, "c", "src")):
+        return None
+    subprocess.run(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={ref}"], cwd=ROOT, check=True)
+    return os.path.join(ROOT, "oracle", "_ref", "libmatfun_ref.so")
+
+
+if __name__ == "__main__":
+    print(build_cuda(verbose=True))
+    print(build_oracle())

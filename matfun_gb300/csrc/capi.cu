@@ -1,0 +1,66 @@
+// capi.cu -- the C ABI of include/matfun_cuda.h: argument checks, normalisation of kind / alpha, grid limits and
+// return codes as the reference's launchers (cuda/src/matfun_cuda.cu:119-141 launch, :169-190 glaunch), then the
+// launch of the per-kind kernels (smf_<kind>.cu, gmf_<kind>.cu).
+#include <climits>
+#include <cstdint>
+
+#include "../../include/matfun_cuda.h"
+#include "mf_launch.h"
+
+namespace {
+
+constexpr int64_t SMF_MAX_N = (int64_t)INT_MAX * 32;  // the reference's grid limit: 2^31 - 1 blocks of 32
+constexpr int64_t GMF_MAX_N = (int64_t)INT_MAX * 64;  // 2^31 - 1 blocks of 64
+
+bool bad_args(int kind, double alpha, int64_t n, const double *x, const double *F, const double *J, const double *H) {
+  if (kind < SMF_EXP || kind > SMF_SQRT || n < 0 || (H && !J) || (kind == SMF_POW && !(alpha > 0))) return true;
+  return n > 0 && (!x || !F);
+}
+
+int smf_call(int kind, double alpha, int64_t n, const double *x, bool mat, double *F, double *J, double *H,
+             void *stream) {
+  if (bad_args(kind, alpha, n, x, F, J, H)) return -1;
+  if (kind != SMF_POW) alpha = kind == SMF_SQRT ? 0.5 : 0.0;
+  if (n == 0) return 0;
+  if (n > SMF_MAX_N) return -2;
+  const cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  switch (kind) {
+    case SMF_EXP: e = mf::smf_launch_exp(alpha, n, x, mat, F, J, H, st); break;
+    case SMF_LOG: e = mf::smf_launch_log(alpha, n, x, mat, F, J, H, st); break;
+    case SMF_SQRT: e = mf::smf_launch_sqrt(alpha, n, x, mat, F, J, H, st); break;
+    default: e = mf::smf_launch_pow(alpha, n, x, mat, F, J, H, st); break;
+  }
+  return e == cudaSuccess ? 0 : -2;
+}
+
+}  // namespace
+
+extern "C" int smf_cuda_eval(int kind, double alpha, int64_t n, const double *v, double *F, double *J, double *H,
+                             void *stream) {
+  return smf_call(kind, alpha, n, v, false, F, J, H, stream);
+}
+
+extern "C" int smf_cuda_eval_matrix(int kind, double alpha, int64_t n, const double *A, double *F, double *J,
+                                    double *H, void *stream) {
+  return smf_call(kind, alpha, n, A, true, F, J, H, stream);
+}
+
+extern "C" int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H,
+                             void *stream) {
+  if (bad_args(kind, alpha, n, A, F, J, H)) return -1;
+  if (kind == SMF_SQRT) kind = SMF_POW, alpha = 0.5;
+  if (kind != SMF_POW) alpha = 0.0;
+  if (n == 0) return 0;
+  if (n > GMF_MAX_N) return -2;
+  const cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  switch (kind) {
+    case SMF_EXP: e = mf::gmf_launch_exp(alpha, n, A, F, J, H, st); break;
+    case SMF_LOG: e = mf::gmf_launch_log(alpha, n, A, F, J, H, st); break;
+    default: e = mf::gmf_launch_pow(alpha, n, A, F, J, H, st); break;
+  }
+  return e == cudaSuccess ? 0 : -2;
+}
+
+extern "C" const char *matfun_cuda_version(void) { return "matfun-gb300 0.1.0 (sm_103a)"; }

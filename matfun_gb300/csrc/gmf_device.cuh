@@ -1,0 +1,587 @@
+// gmf_device.cuh -- per-matrix device math of the general family (FP64, one thread per matrix).
+// Algorithm of c/include/matfun/gmf_kernel.hpp:251-692 (theory: confluent Newton-Hermite form over the eigenvalues):
+//   * eigenvalues of the deviator in closed form, refined against A itself where the closed form loses accuracy
+//     (Newton on det(A - mu I), a pair from det A and the principal minors, the branch-cut pair from the 2x2 block
+//     on the complement of the left eigenvector)
+//   * node order, groups (triple / closest pair / none), the 19 confluent divided differences by the streamed group
+//     series and the residues of single nodes
+//   * the real basis r_0 = I, r_1, r_2 and T = I + iN, giving F and the real-reduced divided differences
+//     D2' = Re(T^T D T) (symmetric, 6 distinct) and D3' (T on all three indices; symmetric, 10 distinct).
+// Same branch thresholds and the same evaluation order of the series as the reference.  The kernels then contract
+// D2' and D3' with r into J and H through symmetric tensors (gmf_kernels.cu).
+// Written with sel() and non-short-circuit &, | (see mf_common.cuh) instead of long ?: / && chains.
+#pragma once
+#include "mf_common.cuh"
+
+namespace mf {
+
+constexpr double G_RHO = 0.7, G_R_EXP = 4.0, G_RHO_POLE = 0.6;  // gmf_kernel.hpp:30
+constexpr int G_KMAX = 200;                                      // gmf_kernel.hpp:31
+
+// launch constants of the gmf kernels (host-computed once per call)
+struct GmfCoef {
+  double al;              // exponent (pow; sqrt arrives as pow 0.5), 0 otherwise
+  double rho_f;           // group radius ratio: 0.7, or min(0.7, 3 / al) for pow
+  double bh[3], bl[3];    // al - k split exactly (k = 0, 1, 2)
+  double bt[G_KMAX];      // series coefficients b_j of f(c (1 + u)) (gmf_kernel.hpp:48-53)
+  double bin[G_KMAX];     // C(k + n, n), n = 3 (order + 1) - 1, by the recurrence of gmf_kernel.hpp:84
+};
+
+// the 19 divided differences f[x0^a x1^b x2^c], a >= b >= c, a >= 1, in lexicographic order of (a, b, c); each is
+// its parent with one node added (node 0 if a - 1 >= b, else node 1 if b - 1 >= c, else node 2)
+MF_D constexpr int gpos(int a, int b, int c) { return (a == 1 ? 0 : (a == 2 ? 3 : 9)) + b * (b + 1) / 2 + c; }
+MF_D constexpr int gms(int t, int i) {  // multiplicity of node i in entry t
+  return i == 0 ? (t < 3 ? 1 : (t < 9 ? 2 : 3))
+                : (i == 1 ? (t < 3 ? (t >= 1) : (t < 9 ? (t >= 6 ? 2 : (t >= 4)) : (t >= 15 ? 3 : (t >= 12 ? 2 : (t >= 10)))))
+                          : (t < 3 ? (t == 2) : (t < 9 ? (t == 5 || t == 7 ? 1 : (t == 8 ? 2 : 0))
+                                                      : (t == 11 || t == 13 || t == 16 ? 1 : (t == 14 || t == 17 ? 2 : (t == 18 ? 3 : 0))))));
+}
+MF_D constexpr int gnode(int t) {
+  return t == 0 ? 0 : (gms(t, 0) - 1 >= gms(t, 1) ? 0 : (gms(t, 1) - 1 >= gms(t, 2) ? 1 : 2));
+}
+MF_D constexpr int gpar(int t) {
+  return t == 0 ? -1
+                : (gnode(t) == 0 ? gpos(gms(t, 0) - 1, gms(t, 1), gms(t, 2))
+                                 : (gnode(t) == 1 ? gpos(gms(t, 0), gms(t, 1) - 1, gms(t, 2))
+                                                  : gpos(gms(t, 0), gms(t, 1), gms(t, 2) - 1)));
+}
+MF_D constexpr int gpos2(int j, int k) { return gpos(2, (j >= 1) + (k >= 1), (j >= 2) + (k >= 2)); }
+MF_D constexpr int gpos3(int j, int k, int l) {
+  return gpos(3, (j >= 1) + (k >= 1) + (l >= 1), (j >= 2) + (k >= 2) + (l >= 2));
+}
+
+MF_D double det3(const double *M) {
+  return M[0] * (M[4] * M[8] - M[5] * M[7]) - M[1] * (M[3] * M[8] - M[5] * M[6]) + M[2] * (M[3] * M[7] - M[4] * M[6]);
+}
+
+// det by elimination with partial pivoting (gmf_kernel.hpp:138-159)
+MF_D double det_lu(const double *M) {
+  double a0 = fabs(M[0]), a1 = fabs(M[3]), a2 = fabs(M[6]);
+  bool p1 = (a1 > a0) & (a1 >= a2), p2 = (a2 > a0) & (a2 > a1);
+  double P[3], R1[3], R2[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    P[c] = sel(p1, M[3 + c], sel(p2, M[6 + c], M[c]));
+    R1[c] = sel(p1 | p2, M[c], M[3 + c]);
+    R2[c] = sel(p2, M[3 + c], M[6 + c]);
+  }
+  double sgn = sel(p1, -1.0, 1.0);
+  double piv = sel(P[0] != 0, P[0], 1.0);
+  double l1 = R1[0] / piv, l2 = R2[0] / piv;
+  double b = R1[1] - l1 * P[1], c = R1[2] - l1 * P[2], d = R2[1] - l2 * P[1], e = R2[2] - l2 * P[2];
+  bool sw = fabs(d) > fabs(b);
+  double bb = sel(sw, d, b), cc = sel(sw, e, c), dd = sel(sw, b, d), ee = sel(sw, c, e);
+  sgn = sel(sw, -sgn, sgn);
+  double det = sgn * P[0] * bb * (ee - dd / sel(bb != 0, bb, 1.0) * cc);
+  return sel((P[0] != 0) & (bb != 0), det, 0.0);
+}
+
+MF_D double minors2(const double *M) {
+  return M[0] * M[4] - M[1] * M[3] + M[0] * M[8] - M[2] * M[6] + M[4] * M[8] - M[5] * M[7];
+}
+
+// eigenvalues of the deviator S (gmf_kernel.hpp:166-208)
+MF_D void roots3(const double *S, cx *x) {
+  constexpr double TWO_PI_3 = 2.0943951023931957;
+  double tau = (S[0] + S[4] + S[8]) / 3.0;
+  double Sp[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) Sp[k] = k % 4 == 0 ? S[k] - tau : S[k];
+  double s = fabs(Sp[0]);
+#pragma unroll
+  for (int k = 1; k < 9; k++) s = tmax(s, fabs(Sp[k]));
+  double t = pow2safe(s), it = 1.0 / t;
+#pragma unroll
+  for (int k = 0; k < 9; k++) Sp[k] = Sp[k] * it;
+  double P = 0.5 * (Sp[0] * Sp[0] + Sp[4] * Sp[4] + Sp[8] * Sp[8]) + Sp[1] * Sp[3] + Sp[2] * Sp[6] + Sp[5] * Sp[7];
+  double Q = det3(Sp);
+  double u = pow2safe(tmax(sqrt(fabs(P)), cbrt(fabs(Q)))), iu = 1.0 / u;
+  P = P * iu * iu;
+  Q = Q * iu * iu * iu;
+  t = t * u;
+  bool trig = (P > 0) & (4.0 * P * P * P >= 27.0 * Q * Q);
+  double s1;
+  if (trig) {
+    double p3 = P / 3.0;
+    double r = 0.5 * Q / (p3 * sqrt(p3));
+    r = sel(r > 1.0, 1.0, sel(r < -1.0, -1.0, r));
+    double ph = acos(r) / 3.0;
+    s1 = 2.0 * sqrt(p3) * cos(sel(r >= 0, ph, ph + TWO_PI_3));
+  } else {
+    double D = 0.25 * Q * Q - P * P * P / 27.0;
+    double uc = cbrt(0.5 * Q + copysgn(sqrt(sel(D > 0, D, 0.0)), Q));
+    s1 = uc + sel(uc != 0, P / (3.0 * sel(uc != 0, uc, 1.0)), 0.0);
+  }
+  double d = P - 0.75 * s1 * s1;
+  bool real = d >= 0;
+  double sq = sqrt(fabs(d));
+  double sa = -0.5 * s1 - copysgn(sq, s1);
+  double prod = sel(s1 != 0, Q / sel(s1 != 0, s1, 1.0), -P);
+  double sb = sel(sa != 0, prod / sel(sa != 0, sa, 1.0), 0.0);
+  double im = sel(real, 0.0, sq) * t;
+  x[0] = cmk(s1 * t + tau, 0.0 * t);
+  x[1] = cmk(sel(real, sa, -0.5 * s1) * t + tau, im);
+  x[2] = cmk(sel(real, sb, -0.5 * s1) * t + tau, -im);
+}
+
+// 3 Newton steps on det(A - mu_j I), derivative from the other nodes (gmf_kernel.hpp:210-226)
+template <int J>
+MF_D void newton(const double *As, cx *mu) {
+#pragma unroll
+  for (int it = 0; it < 3; it++) {
+    cx den = cmk(1.0, 0.0);
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      if (k != J) den = cmul(den, csub(mu[k], mu[J]));
+    bool ok = (den.re != 0) | (den.im != 0);
+    double B[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) B[k] = k % 4 == 0 ? As[k] - mu[J].re : As[k];
+    double step = det_lu(B) * cinv_s(den).re;
+    mu[J].re = sel(ok, mu[J].re + step, mu[J].re);
+  }
+}
+
+// f of a node (k: output order; pow times sig^(al - k)) (gmf_kernel.hpp:228-248)
+template <int KIND>
+MF_D cx coef0(const GmfCoef &C, double sig, double m, cx x, cx mu, int k) {
+  if (KIND == EXP) {
+    double e = exp(x.re);
+    return cmk(e * cos(x.im), e * sin(x.im));
+  }
+  double th = atan2(mu.im, mu.re);
+  if (KIND == LOG) {
+    bool near = (m > 0) & (cabs_s(x) <= 0.5 * m);
+    double ms = sel(m > 0, m, 1.0), zr = x.re / ms, zi = x.im / ms;
+    double l1r = 0.5 * log1p(zr * (2.0 + zr) + zi * zi), l1i = atan2(zi, 1.0 + zr);
+    double lr = near ? log(sig * ms) + l1r : log(sig * cabs_s(mu));
+    return cmk(lr, sel(near, l1i, th));
+  }
+  double mag = pow_split(sig * cabs_s(mu), C.bh[k], C.bl[k]);
+  double ph = (C.al - k) * th;
+  cx out = cmk(mag * cos(ph), mag * sin(ph));
+  for (int i = 0; i < k; i++) out = cmul(out, mu);
+  return out;
+}
+
+// number of series terms from the term bound 1e-17 (gmf_kernel.hpp:73-97); the binomial factors come from a table
+// computed on the host with the reference's recurrence, so the bound is bit-identical
+MF_D int nterms(const GmfCoef &C, int n, double r, double q) {
+  int M = 1;
+  if (r > 0) {
+    double best = 0.0, rk = 1.0;
+    for (int k = 0; n + k < G_KMAX; k++) {
+      double t = fabs(C.bt[n + k]) * C.bin[k] * rk;
+      best = tmax(t, best);
+      M = k;
+      if (((k > 2) & (t <= 1e-17 * best)) | !(rk > 0)) break;
+      rk *= r;
+    }
+  }
+  if (q > 0) {
+    double qk = 1.0;
+    for (int k = 0; n + k < G_KMAX; k++) {
+      if ((k > M) & ((k + 1.0) * (k + 2.0) / 2.0 * qk <= 1e-17)) break;
+      M = k > M ? k : M;
+      qk *= q;
+    }
+  }
+  return n + M + 1 < G_KMAX ? n + M + 1 : G_KMAX;
+}
+
+// the per-matrix record the kernels contract into F, J, H
+struct GmfRec {
+  double F[9];
+  double r1[9], r2[9];   // real basis (r_0 = I)
+  double D2[6];          // Re(T^T D T) at (00, 11, 22, 01, 02, 12)
+  double D3[10];         // D3' at the sorted triples (000, 001, 011, 111, 002, 012, 112, 022, 122, 222) = sym3 order
+  double sc1, sc2;       // output factors of J and H (NaN for a matrix outside the domain)
+};
+
+template <int KIND, int ORDER>
+MF_D void gmf_record(const double *a, const GmfCoef &C, GmfRec &R) {
+  constexpr int ND = ORDER == 0 ? 3 : (ORDER == 1 ? 9 : 19);
+  // ---- scaling (exp: none), shift m, deviator S
+  double amax = fabs(a[0]);
+#pragma unroll
+  for (int k = 1; k < 9; k++) amax = tmax(amax, fabs(a[k]));
+  double sig = KIND == EXP ? 1.0 : pow2safe(amax), isig = 1.0 / sig;
+  double As[9], S[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) As[k] = a[k] * isig;
+  double m = (As[0] + As[4] + As[8]) / 3.0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) S[k] = k % 4 == 0 ? As[k] - m : As[k];
+  cx x[3], mu[3];
+  roots3(S, x);
+#pragma unroll
+  for (int i = 0; i < 3; i++) mu[i] = cmk(m + x[i].re, x[i].im);
+
+  // ---- pair refinement (gmf_kernel.hpp:277-304)
+  double smax = fabs(S[0]);
+#pragma unroll
+  for (int k = 1; k < 9; k++) smax = tmax(smax, fabs(S[k]));
+  double mid = 0.5 * (mu[1].re + mu[2].re), Rp = 0.5 * cabs_s(csub(mu[1], mu[2]));
+  bool small = fabs(mid) + Rp <= 0.25 * fabs(mu[0].re);
+  bool aniso = (fabs(m) <= smax) & (Rp <= 0.25 * fabs(mid - mu[0].re));
+  bool pc = (mu[0].re != 0) & (small | aniso);
+  double pcen = 0.0, ps = 0.0;
+  bool preal = true;
+  if (pc) {
+    newton<0>(As, mu);
+    double m0 = mu[0].re;
+    bool big = fabs(m0) >= fabs(mid) + Rp;
+    double pid = det_lu(As) / m0, c2 = minors2(As);
+    double sgt = As[0] + As[4] + As[8] - m0;
+    double sg = sel(big, (c2 - pid) / m0, sgt), pi = sel(big, pid, c2 - m0 * sgt);
+    double disc = 0.25 * sg * sg - pi;
+    pcen = 0.5 * sg;
+    ps = sqrt(fabs(disc));
+    preal = disc >= 0;
+    double r1 = pcen + copysgn(ps, pcen);
+    double r2 = sel(r1 != 0, pi / sel(r1 != 0, r1, 1.0), pcen - copysgn(ps, pcen));
+    mu[1] = csel(preal, cmk(r1, 0.0), cmk(pcen, ps));
+    mu[2] = csel(preal, cmk(r2, 0.0), cmk(pcen, -ps));
+  }
+  // ---- branch-cut pair (log, pow) (gmf_kernel.hpp:305-367)
+  bool cut = (KIND != EXP) & (mu[1].re + mu[2].re < 0);
+  if (cut) {
+    if (!pc) newton<0>(As, mu);
+    double l0 = mu[0].re;
+    double Mc[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) Mc[k] = k % 4 == 0 ? As[k] - l0 : As[k];
+    double c01[3] = {Mc[3] * Mc[7] - Mc[6] * Mc[4], Mc[6] * Mc[1] - Mc[0] * Mc[7], Mc[0] * Mc[4] - Mc[3] * Mc[1]};
+    double c02[3] = {Mc[3] * Mc[8] - Mc[6] * Mc[5], Mc[6] * Mc[2] - Mc[0] * Mc[8], Mc[0] * Mc[5] - Mc[3] * Mc[2]};
+    double c12[3] = {Mc[4] * Mc[8] - Mc[7] * Mc[5], Mc[7] * Mc[2] - Mc[1] * Mc[8], Mc[1] * Mc[5] - Mc[4] * Mc[2]};
+    double n01 = c01[0] * c01[0] + c01[1] * c01[1] + c01[2] * c01[2];
+    double n02 = c02[0] * c02[0] + c02[1] * c02[1] + c02[2] * c02[2];
+    double n12 = c12[0] * c12[0] + c12[1] * c12[1] + c12[2] * c12[2];
+    bool s1 = n02 > n01;
+    double u[3], nn = sel(s1, n02, n01);
+#pragma unroll
+    for (int k = 0; k < 3; k++) u[k] = sel(s1, c02[k], c01[k]);
+    bool s2 = n12 > nn;
+#pragma unroll
+    for (int k = 0; k < 3; k++) u[k] = sel(s2, c12[k], u[k]);
+    nn = sel(s2, n12, nn);
+    bool okd = nn > 0;
+    double iu = 1.0 / sqrt(sel(okd, nn, 1.0));
+#pragma unroll
+    for (int k = 0; k < 3; k++) u[k] = u[k] * iu;
+    double au0 = fabs(u[0]), au1 = fabs(u[1]), au2 = fabs(u[2]);
+    bool k1 = au1 < au0, k2 = au2 < sel(k1, au1, au0);
+    double ex = sel(k1 | k2, 0.0, 1.0), ey = sel(k1 & !k2, 1.0, 0.0), ez = sel(k2, 1.0, 0.0);
+    double eu = ex * u[0] + ey * u[1] + ez * u[2];
+    double q1[3] = {ex - eu * u[0], ey - eu * u[1], ez - eu * u[2]};
+    double iq = 1.0 / sqrt(q1[0] * q1[0] + q1[1] * q1[1] + q1[2] * q1[2]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) q1[k] = q1[k] * iq;
+    double q2[3] = {u[1] * q1[2] - u[2] * q1[1], u[2] * q1[0] - u[0] * q1[2], u[0] * q1[1] - u[1] * q1[0]};
+    double Sq1[3], Sq2[3];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      Sq1[r] = S[3 * r] * q1[0] + S[3 * r + 1] * q1[1] + S[3 * r + 2] * q1[2];
+      Sq2[r] = S[3 * r] * q2[0] + S[3 * r + 1] * q2[1] + S[3 * r + 2] * q2[2];
+    }
+    double b11 = q1[0] * Sq1[0] + q1[1] * Sq1[1] + q1[2] * Sq1[2];
+    double b12 = q1[0] * Sq2[0] + q1[1] * Sq2[1] + q1[2] * Sq2[2];
+    double b21 = q2[0] * Sq1[0] + q2[1] * Sq1[1] + q2[2] * Sq1[2];
+    double b22 = q2[0] * Sq2[0] + q2[1] * Sq2[1] + q2[2] * Sq2[2];
+    double dd = 0.5 * (b11 - b22), beta2 = -(dd * dd + b12 * b21), cc = m + 0.5 * (b11 + b22);
+    double bb = sqrt(fabs(beta2));
+    bool creal = beta2 <= 0;
+    mu[1] = csel(okd, csel(creal, cmk(cc + bb, 0.0), cmk(cc, bb)), mu[1]);
+    mu[2] = csel(okd, csel(creal, cmk(cc - bb, 0.0), cmk(cc, -bb)), mu[2]);
+    pcen = sel(okd, cc, pcen);
+    ps = sel(okd, bb, ps);
+    preal = (okd & creal) | (!okd & preal);
+    pc = pc | okd;
+  }
+  bool ab[3] = {pc, pc, pc};
+  double og[3] = {0.0, 1.0, 2.0};
+#pragma unroll
+  for (int i = 0; i < 3; i++) x[i] = csel(pc, cmk(mu[i].re - m, mu[i].im), x[i]);
+
+  // ---- node order (gmf_kernel.hpp:373-410)
+  {
+    auto key = [&](cx v) { return KIND == EXP ? v.re : -cabs_s(v); };
+    bool cplxp = x[1].im != 0;
+    if (cplxp) {
+      bool first = (key(mu[0]) <= key(mu[1])) | cut;
+      if (!first) {  // rotate to (pair, real node)
+        cx tx = x[0], tm = mu[0];
+        bool ta = ab[0];
+        double to = og[0];
+        x[0] = x[1]; mu[0] = mu[1]; ab[0] = ab[1]; og[0] = og[1];
+        x[1] = x[2]; mu[1] = mu[2]; ab[1] = ab[2]; og[1] = og[2];
+        x[2] = tx; mu[2] = tm; ab[2] = ta; og[2] = to;
+      }
+    } else {
+#pragma unroll
+      for (int s = 0; s < 3; s++) {
+        const int i = s == 1 ? 1 : 0, j = i + 1;
+        bool sw = key(mu[i]) > key(mu[j]);
+        cx tx = x[i], tm = mu[i];
+        bool ta = ab[i];
+        double to = og[i];
+        x[i] = csel(sw, x[j], x[i]); x[j] = csel(sw, tx, x[j]);
+        mu[i] = csel(sw, mu[j], mu[i]); mu[j] = csel(sw, tm, mu[j]);
+        ab[i] = (sw & ab[j]) | (!sw & ab[i]); ab[j] = (sw & ta) | (!sw & ab[j]);
+        og[i] = sel(sw, og[j], og[i]); og[j] = sel(sw, to, og[j]);
+      }
+    }
+  }
+
+  // ---- groups (gmf_kernel.hpp:412-437)
+  auto okf = [&](double c, double R) -> bool {
+    if (KIND == EXP) return R <= G_R_EXP;
+    return (m + c > 0) & (R <= C.rho_f * (m + c));
+  };
+  double cs3 = (x[0].re + x[1].re + x[2].re) / 3.0;
+  double R3 = tmax(tmax(cabs_s(cmk(x[0].re - cs3, x[0].im)), cabs_s(cmk(x[1].re - cs3, x[1].im))),
+                   cabs_s(cmk(x[2].re - cs3, x[2].im)));
+  bool triple = okf(cs3, R3);
+  bool psel[3] = {false, false, false};
+  double bestR = __longlong_as_double(0x7FF0000000000000ll);
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+    const int i = p == 2 ? 1 : 0, j = p == 0 ? 1 : 2, k = 3 - i - j;
+    bool elig = ((x[i].im == 0) & (x[j].im == 0)) | ((x[i].re == x[j].re) & (x[i].im == -x[j].im));
+    double c = 0.5 * (x[i].re + x[j].re), R = 0.5 * cabs_s(csub(x[i], x[j]));
+    bool okp = elig & okf(c, R) & (R <= G_RHO_POLE * cabs_s(cmk(c - x[k].re, -x[k].im))) & !triple;
+    bool better = okp & (R < bestR);
+    bestR = sel(better, R, bestR);
+#pragma unroll
+    for (int q = 0; q < p; q++) psel[q] = psel[q] & !better;
+    psel[p] = better;
+  }
+  bool inG[3] = {bool(triple | psel[0] | psel[1]), bool(triple | psel[0] | psel[2]), bool(triple | psel[1] | psel[2])};
+  bool pk[3] = {psel[2], psel[1], psel[0]};
+
+  // ---- group centre and offsets (gmf_kernel.hpp:439-460)
+  double gsum = sel(inG[0], 1.0, 0.0) + sel(inG[1], 1.0, 0.0) + sel(inG[2], 1.0, 0.0);
+  double cxg = (sel(inG[0], x[0].re, 0.0) + sel(inG[1], x[1].re, 0.0) + sel(inG[2], x[2].re, 0.0)) /
+               sel(gsum > 0, gsum, 1.0);
+  double cmu = m + cxg;
+  bool is12[3] = {og[0] > 0.5, og[1] > 0.5, og[2] > 0.5};
+  bool ovr = pc & (gsum == 2.0) &
+             ((inG[0] & inG[1] & is12[0] & is12[1]) | (inG[0] & inG[2] & is12[0] & is12[2]) |
+              (inG[1] & inG[2] & is12[1] & is12[2]));
+  cxg = sel(ovr, pcen - m, cxg);
+  cmu = sel(ovr, pcen, cmu);
+  cx dpair = cmk(sel(preal, ps, 0.0), sel(preal, 0.0, ps));
+  cx off[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    bool neg = (mu[i].re - pcen < 0) | (mu[i].im < 0);
+    cx di = csel(neg, cmk(-dpair.re, -dpair.im), dpair);
+    bool ovi = ovr & inG[i];
+    mu[i] = csel(ovi, cmk(pcen + di.re, di.im), mu[i]);
+    x[i] = csel(ovi, cmk(mu[i].re - m, mu[i].im), x[i]);
+    off[i] = csel(inG[i], csel(ovi, di, cmk(x[i].re - cxg, x[i].im)), cmk(0.0, 0.0));
+  }
+
+  // ---- single real nodes far from m: Newton (gmf_kernel.hpp:462-476)
+#define MF_FAR_NEWTON(I)                                                                           \
+  {                                                                                                \
+    bool mask = !inG[I] & !ab[I] & (x[I].im == 0) & (fabs(x[I].re) > 0.5 * fabs(m));              \
+    if (mask) {                                                                                    \
+      newton<I>(As, mu);                                                                           \
+      ab[I] = true;                                                                                \
+      x[I] = cmk(mu[I].re - m, mu[I].im);                                                          \
+    }                                                                                              \
+  }
+  MF_FAR_NEWTON(0)
+  MF_FAR_NEWTON(1)
+  MF_FAR_NEWTON(2)
+#undef MF_FAR_NEWTON
+  bool absc = (inG[0] & ab[0]) | (inG[1] & ab[1]) | (inG[2] & ab[2]);
+  double apole = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) apole = sel(pk[k], sel(absc | ab[k], cmu - mu[k].re, cxg - x[k].re), apole);
+  double xshift = KIND == EXP ? tmax(tmax(x[0].re, x[1].re), x[2].re) : 0.0;
+  bool bad = KIND == EXP ? false
+                         : (((x[0].im == 0) & (mu[0].re <= 0)) | ((x[1].im == 0) & (mu[1].re <= 0)) |
+                            ((x[2].im == 0) & (mu[2].re <= 0)));
+
+  // ---- group series (gmf_kernel.hpp:478-533)
+  bool hasg = inG[0] | inG[1] | inG[2];
+  double L = KIND == EXP ? 1.0 : sel(hasg & (cmu > 0), cmu, 1.0), iL = 1.0 / L;
+  cx u[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) u[i] = cscl(off[i], iL);
+  double ap = sel(fabs(apole) > 0, apole * iL, 1.0), iap = 1.0 / ap;
+  double rr = tmax(cabs_s(u[0]), tmax(cabs_s(u[1]), cabs_s(u[2])));
+  double rq = sel((pk[0] | pk[1] | pk[2]) & (rr * fabs(iap) <= 1.0), rr * fabs(iap), 0.0);
+  rr = sel(hasg & (rr <= G_R_EXP + 0.5), rr, 0.0);
+  double b0 = 1.0;
+  if (KIND == LOG) b0 = coef0<LOG>(C, sig, m, cmk(cxg, 0.0), cmk(cmu, 0.0), 0).re;
+  cx D[ND];
+#pragma unroll
+  for (int c = 0; c < ND; c++) D[c] = cmk(0.0, 0.0);
+  if (hasg) {
+    const int K = nterms(C, 3 * (ORDER + 1) - 1, rr, rq);
+    cx Ep[ND], Ec[ND];
+#pragma unroll
+    for (int c = 0; c < ND; c++) Ep[c] = csel(inG[gnode(c)], cmk(0.0, 0.0), gpar(c) < 0 ? cmk(1.0, 0.0) : Ep[gpar(c) < 0 ? 0 : gpar(c)]);
+    double q1 = 0.0, q2 = 0.0, q3 = 0.0;
+    for (int j = 0; j < K; j++) {
+      double bj = j == 0 ? b0 : C.bt[j];
+      double g1 = (bj - q1) * iap, g2 = (g1 - q2) * iap, g3 = (g2 - q3) * iap;
+      q1 = g1; q2 = g2; q3 = g3;
+      double qv[4] = {bj, g1, g2, g3};
+#pragma unroll
+      for (int c = 0; c < ND; c++) {
+        const int par = gpar(c), i = gnode(c);
+        cx epp = par < 0 ? cmk(sel(j == 0, 1.0, 0.0), 0.0) : Ep[par < 0 ? 0 : par];
+        cx epc = par < 0 ? cmk(0.0, 0.0) : Ec[par < 0 ? 0 : par];
+        Ec[c] = csel(inG[i], cadd(epp, cmul(u[i], Ep[c])), epc);
+        double g = sel(pk[0], qv[gms(c, 0)], sel(pk[1], qv[gms(c, 1)], sel(pk[2], qv[gms(c, 2)], qv[0])));
+        D[c] = cadd(D[c], cscl(Ec[c], g));
+      }
+#pragma unroll
+      for (int c = 0; c < ND; c++) Ep[c] = Ec[c];
+    }
+#pragma unroll
+    for (int c = 0; c < ND; c++) {
+      const int nn = gms(c, 0) + gms(c, 1) + gms(c, 2) - 1, k = gms(c, 0) - 1;
+      double fac;
+      if (KIND == EXP) {
+        fac = exp(cxg - xshift);
+      } else {
+        double iLn = 1.0;
+#pragma unroll
+        for (int r = 0; r < nn - (KIND == POW ? k : 0); r++) iLn = iLn * iL;
+        fac = KIND == LOG ? iLn : pow_split(sig * L, C.bh[k], C.bl[k]) * iLn;
+      }
+      D[c] = cscl(D[c], fac);
+    }
+  }
+  // ---- residues of the single nodes (gmf_kernel.hpp:534-576)
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    if (inG[i]) continue;
+    cx xs = KIND == EXP ? cmk(x[i].re - xshift, x[i].im) : x[i];
+    cx f0[3];
+    f0[0] = coef0<KIND>(C, sig, m, xs, mu[i], 0);
+    if (KIND == POW && ORDER >= 1) f0[1] = coef0<KIND>(C, sig, m, xs, mu[i], 1);
+    if (KIND == POW && ORDER >= 2) f0[2] = coef0<KIND>(C, sig, m, xs, mu[i], 2);
+    cx imu = cinv_s(mu[i]);
+    cx w[3];
+#pragma unroll
+    for (int z = 0; z < 3; z++)
+      if (z != i) w[z] = cinv_s(csel(ab[i] | ab[z], csub(mu[i], mu[z]), csub(x[i], x[z])));
+#pragma unroll
+    for (int c = 0; c < ND; c++) {
+      const int mi = gms(c, i);
+      if (mi == 0) continue;
+      const int k = gms(c, 0) - 1;
+      cx fb = KIND == POW ? f0[k] : f0[0], ser[3];
+      if (KIND == EXP) {
+        ser[0] = fb; ser[1] = fb; ser[2] = cscl(fb, 0.5);
+      } else if (KIND == LOG) {
+        ser[0] = fb; ser[1] = imu; ser[2] = cscl(cmul(imu, imu), -0.5);
+      } else {
+        ser[0] = fb;
+        ser[1] = cscl(cmul(fb, imu), C.al);
+        ser[2] = cscl(cmul(ser[1], imu), (C.al - 1.0) / 2.0);
+      }
+#pragma unroll
+      for (int z = 0; z < 3; z++) {
+        const int mz = gms(c, z);
+        if (z == i || mz == 0) continue;
+        cx wp = cmk(1.0, 0.0);
+#pragma unroll
+        for (int r = 0; r < mz; r++) wp = cmul(wp, w[z]);
+        cx p1 = cscl(cmul(wp, w[z]), (double)-mz);
+        cx p2 = cscl(cmul(cmul(wp, w[z]), w[z]), mz * (mz + 1) / 2.0);
+        cx n0 = cmul(ser[0], wp), n1 = cadd(cmul(ser[1], wp), cmul(ser[0], p1));
+        cx n2 = cadd(cadd(cmul(ser[2], wp), cmul(ser[1], p1)), cmul(ser[0], p2));
+        ser[0] = n0; ser[1] = n1; ser[2] = n2;
+      }
+      D[c] = cadd(D[c], ser[mi - 1]);
+    }
+  }
+
+  // ---- real basis and T = I + iN (gmf_kernel.hpp:578-599)
+  double b0i = x[0].im, b1i = x[1].im;
+  double B1[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const bool dg = k % 4 == 0;
+    R.r1[k] = dg ? sel(ab[0], As[k] - mu[0].re, S[k] - x[0].re) : S[k];
+    B1[k] = dg ? sel(ab[1], As[k] - mu[1].re, S[k] - x[1].re) : S[k];
+  }
+#pragma unroll
+  for (int i2 = 0; i2 < 3; i2++)
+#pragma unroll
+    for (int j2 = 0; j2 < 3; j2++)
+      R.r2[3 * i2 + j2] = R.r1[3 * i2] * B1[j2] + R.r1[3 * i2 + 1] * B1[3 + j2] + R.r1[3 * i2 + 2] * B1[6 + j2] -
+                          (i2 == j2 ? b0i * b1i : 0.0);
+  double a01 = sel(ab[0] | ab[1], mu[0].re - mu[1].re, x[0].re - x[1].re);
+  double N10 = -b0i, N20 = -b0i * a01, N21 = -(b0i + b1i);
+  double nanf = sel(bad, __longlong_as_double(0x7FF8000000000000ll), 1.0);
+  {  // F = sum_m Re(T^T D)_m r_m
+    double Dr0 = D[0].re - (N10 * D[1].im + N20 * D[2].im), Dr1 = D[1].re - N21 * D[2].im, Dr2 = D[2].re;
+    double e = KIND == EXP ? exp(m + xshift) : 1.0;
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      R.F[k] = ((k % 4 == 0 ? Dr0 : 0.0) + Dr1 * R.r1[k] + Dr2 * R.r2[k]) * e * nanf;
+  }
+  if (ORDER < 1) return;
+  R.sc1 = (KIND == EXP ? exp(m + xshift) : (KIND == LOG ? isig : 1.0)) * nanf;
+  {  // D2' = Re(T^T D T): T on index 0 (complex), then the real part after T on index 1
+    double Dr[9], Di[9];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) { Dr[3 * j + k] = D[gpos2(j, k)].re; Di[3 * j + k] = D[gpos2(j, k)].im; }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      double vr0 = Dr[k], vr1 = Dr[3 + k], vr2 = Dr[6 + k], vi0 = Di[k], vi1 = Di[3 + k], vi2 = Di[6 + k];
+      Dr[k] = vr0 - (N10 * vi1 + N20 * vi2); Di[k] = vi0 + (N10 * vr1 + N20 * vr2);
+      Dr[3 + k] = vr1 - N21 * vi2;           Di[3 + k] = vi1 + N21 * vr2;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      Dr[3 * j] = Dr[3 * j] - (N10 * Di[3 * j + 1] + N20 * Di[3 * j + 2]);
+      Dr[3 * j + 1] = Dr[3 * j + 1] - N21 * Di[3 * j + 2];
+    }
+    R.D2[0] = Dr[0]; R.D2[1] = Dr[4]; R.D2[2] = Dr[8]; R.D2[3] = Dr[1]; R.D2[4] = Dr[2]; R.D2[5] = Dr[5];
+  }
+  if (ORDER < 2) return;
+  R.sc2 = (KIND == EXP ? exp(m + xshift) : (KIND == LOG ? isig * isig : 1.0)) * nanf;
+  {  // D3': T on each of the three indices, real part
+    double Dr[27], Di[27];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int l = 0; l < 3; l++) {
+          Dr[9 * j + 3 * k + l] = D[gpos3(j, k, l)].re;
+          Di[9 * j + 3 * k + l] = D[gpos3(j, k, l)].im;
+        }
+#pragma unroll
+    for (int axis = 0; axis < 3; axis++) {
+      const int s = axis == 0 ? 9 : (axis == 1 ? 3 : 1);
+#pragma unroll
+      for (int base = 0; base < 27; base++) {
+        if ((base / s) % 3 != 0) continue;
+        double vr0 = Dr[base], vr1 = Dr[base + s], vr2 = Dr[base + 2 * s];
+        double vi0 = Di[base], vi1 = Di[base + s], vi2 = Di[base + 2 * s];
+        Dr[base] = vr0 - (N10 * vi1 + N20 * vi2); Di[base] = vi0 + (N10 * vr1 + N20 * vr2);
+        Dr[base + s] = vr1 - N21 * vi2;           Di[base + s] = vi1 + N21 * vr2;
+      }
+    }
+#pragma unroll
+    for (int z = 0; z < 3; z++)
+#pragma unroll
+      for (int y = 0; y <= z; y++)
+#pragma unroll
+        for (int xx = 0; xx <= y; xx++) R.D3[sym3(xx, y, z)] = Dr[9 * xx + 3 * y + z];
+  }
+}
+
+}  // namespace mf

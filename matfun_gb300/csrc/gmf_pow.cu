@@ -1,0 +1,9 @@
+// gmf_pow.cu -- the pow instantiations of the gmf kernels (gmf_kernels.cuh), one translation unit per kind.
+#include "gmf_kernels.cuh"
+
+namespace mf {
+cudaError_t gmf_launch_pow(double al, int64_t n, const double *A, double *F, double *J, double *H,
+                            cudaStream_t st) {
+  return gmf_launch_t<POW>(al, n, A, F, J, H, st);
+}
+}  // namespace mf

@@ -1,0 +1,23 @@
+// mf_launch.h -- internal launch interface between the C ABI layer (capi.cu) and the kernel translation units
+// (one per family and kind).  Arguments are validated and normalised by the caller: n > 0, the grid within limits,
+// sqrt of the general family arrives as pow with al = 0.5, al = 0.5 for smf sqrt and 0 for exp / log.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mf {
+#define MF_SMF_DECL(k)                                                                                          \
+  cudaError_t smf_launch_##k(double al, int64_t n, const double *x, bool mat, double *F, double *J, double *H, \
+                             cudaStream_t st);
+MF_SMF_DECL(exp)
+MF_SMF_DECL(log)
+MF_SMF_DECL(sqrt)
+MF_SMF_DECL(pow)
+#undef MF_SMF_DECL
+#define MF_GMF_DECL(k) \
+  cudaError_t gmf_launch_##k(double al, int64_t n, const double *A, double *F, double *J, double *H, cudaStream_t st);
+MF_GMF_DECL(exp)
+MF_GMF_DECL(log)
+MF_GMF_DECL(pow)
+#undef MF_GMF_DECL
+}  // namespace mf

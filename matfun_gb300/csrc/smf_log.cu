@@ -1,0 +1,9 @@
+// smf_log.cu -- the log instantiations of the smf kernels (smf_kernels.cuh), one translation unit per kind.
+#include "smf_kernels.cuh"
+
+namespace mf {
+cudaError_t smf_launch_log(double al, int64_t n, const double *x, bool mat, double *F, double *J, double *H,
+                            cudaStream_t st) {
+  return smf_launch_t<LOG>(al, n, x, mat, F, J, H, st);
+}
+}  // namespace mf

@@ -1,0 +1,9 @@
+// smf_pow.cu -- the pow instantiations of the smf kernels (smf_kernels.cuh), one translation unit per kind.
+#include "smf_kernels.cuh"
+
+namespace mf {
+cudaError_t smf_launch_pow(double al, int64_t n, const double *x, bool mat, double *F, double *J, double *H,
+                            cudaStream_t st) {
+  return smf_launch_t<POW>(al, n, x, mat, F, J, H, st);
+}
+}  // namespace mf

@@ -1,0 +1,46 @@
+"""comparison helpers shared by the tests"""
+import re
+
+import numpy as np
+
+
+def maxrel(a, b):
+    """max |a - b| / max |b| over entries, skipping positions where both are NaN (a NaN on one side only: inf),
+    as the reference's CUDA test (cuda/tests/test_cuda_api.cu:15-23)"""
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    both = np.isnan(a) & np.isnan(b)
+    d = np.abs(a - b)
+    d[both] = 0.0
+    d = np.where(np.isnan(d), np.inf, d)
+    s = np.max(np.abs(np.where(np.isnan(b), 0.0, b)), initial=0.0)
+    return float(np.max(d, initial=0.0) / max(s, 1e-300))
+
+
+def maxrel_rows(a, b):
+    """per-row version of maxrel for (n, k) arrays"""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    both = np.isnan(a) & np.isnan(b)
+    d = np.abs(a - b)
+    d[both] = 0.0
+    d = np.where(np.isnan(d), np.inf, d)
+    s = np.max(np.abs(np.where(np.isnan(b), 0.0, b)), axis=1)
+    return np.max(d, axis=1) / np.maximum(s, 1e-300)
+
+
+def header_functions(path):
+    """names of the functions an include/*.h declares"""
+    src = open(path).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*([a-z_][a-z_0-9]*)\s*\(", src, flags=re.M)
+
+
+def voigt_to_matrix(v):
+    """(n, 6) Voigt vectors -> (n, 3, 3) symmetric matrices"""
+    A = np.empty(v.shape[:-1] + (3, 3))
+    A[..., 0, 0], A[..., 1, 1], A[..., 2, 2] = v[..., 0], v[..., 1], v[..., 2]
+    A[..., 0, 1] = A[..., 1, 0] = v[..., 3]
+    A[..., 0, 2] = A[..., 2, 0] = v[..., 4]
+    A[..., 1, 2] = A[..., 2, 1] = v[..., 5]
+    return A
