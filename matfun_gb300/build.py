@@ -97,11 +97,27 @@ def build_oracle():
 
 
 def build_reference_oracle(ref="/root/reference"):
-    """the reference's own CPU library (oracle/_ref/libmatfun_ref.so), only where its sources are present"""
+    """the reference's own CPU library (oracle/_ref/libmatfun_ref.so) and its CUDA kernels as an sm_103a cubin
+    (oracle/_ref/matfun_cuda_ref.cubin), only where the reference sources are present"""
     if not os.path.isdir(os.path.join(ref, "c", "src")):
         return None
-    subprocess.run(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={ref}"], cwd=ROOT, check=True)
+    subprocess.run(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={ref}", "all"], cwd=ROOT,
+                   check=True)
     return os.path.join(ROOT, "oracle", "_ref", "libmatfun_ref.so")
+
+
+def build_ref_gpu_timer():
+    """oracle/ref_gpu_timer.so: launcher of the reference's cubin (test and benchmark infrastructure)"""
+    src = os.path.join(ROOT, "oracle", "ref_gpu_timer.cu")
+    lib = os.path.join(ROOT, "oracle", "ref_gpu_timer.so")
+    if _fresh(lib, os.path.getmtime(src)):
+        return lib
+    cmd = [_nvcc(), "-shared", "-Xcompiler", "-fPIC", "-O2", "-o", lib + ".tmp", src, "-lcuda"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"ref_gpu_timer build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(lib + ".tmp", lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -24,7 +24,7 @@ struct GmfCoef {
   double rho_f;           // group radius ratio: 0.7, or min(0.7, 3 / al) for pow
   double bh[3], bl[3];    // al - k split exactly (k = 0, 1, 2)
   double bt[G_KMAX];      // series coefficients b_j of f(c (1 + u)) (gmf_kernel.hpp:48-53)
-  double bin[G_KMAX];     // C(k + n, n), n = 3 (order + 1) - 1, by the recurrence of gmf_kernel.hpp:84
+  float lterm[G_KMAX];    // log2(|b_(n+k)| C(k + n, n)), n = 3 (order + 1) - 1: the term bound of gmf_kernel.hpp:73-97
 };
 
 // the 19 divided differences f[x0^a x1^b x2^c], a >= b >= c, a >= 1, in lexicographic order of (a, b, c); each is
@@ -164,29 +164,75 @@ MF_D cx coef0(const GmfCoef &C, double sig, double m, cx x, cx mu, int k) {
   return out;
 }
 
-// number of series terms from the term bound 1e-17 (gmf_kernel.hpp:73-97); the binomial factors come from a table
-// computed on the host with the reference's recurrence, so the bound is bit-identical
+// number of series terms (gmf_kernel.hpp:73-97): the group series needs terms until |b_(n+k)| C(k+n, n) r^k drops
+// below 1e-17 of the largest, the pole series until C(k+2, 2) q^k <= 1e-17.  Evaluated on log2 values in FP32 (the
+// FP64 pipe is the bottleneck of this kernel) with a threshold 2^-0.05 below 1e-17, so that the count is never
+// smaller than the FP64 bound's; one term more changes a result by less than 1e-17 relative.
 MF_D int nterms(const GmfCoef &C, int n, double r, double q) {
+  constexpr float L17 = -56.5237f - 0.05f;  // log2(1e-17) less a margin
   int M = 1;
   if (r > 0) {
-    double best = 0.0, rk = 1.0;
+    const float lr = log2f((float)r);
+    float best = -INFINITY;
     for (int k = 0; n + k < G_KMAX; k++) {
-      double t = fabs(C.bt[n + k]) * C.bin[k] * rk;
-      best = tmax(t, best);
+      const float lk = (float)k * lr;
+      const float t = C.lterm[k] + lk;
+      best = fmaxf(best, t);
       M = k;
-      if (((k > 2) & (t <= 1e-17 * best)) | !(rk > 0)) break;
-      rk *= r;
+      if (((k > 2) & (t <= best + L17)) | (lk < -1074.0f)) break;
     }
   }
   if (q > 0) {
-    double qk = 1.0;
+    const float lq = log2f((float)q);
     for (int k = 0; n + k < G_KMAX; k++) {
-      if ((k > M) & ((k + 1.0) * (k + 2.0) / 2.0 * qk <= 1e-17)) break;
+      if ((k > M) & (log2f((k + 1.0f) * (k + 2.0f) * 0.5f) + (float)k * lq <= L17)) break;
       M = k > M ? k : M;
-      qk *= q;
     }
   }
   return n + M + 1 < G_KMAX ? n + M + 1 : G_KMAX;
+}
+
+// the group-series constant of log, f(c) at the real group centre (the real part of coef0<LOG>, without the
+// arguments of the complex logarithm, which it does not need)
+MF_D double log_b0(double sig, double m, double cxg, double cmu) {
+  bool near = (m > 0) & (fabs(cxg) <= 0.5 * m);
+  double ms = sel(m > 0, m, 1.0), zr = cxg / ms;
+  return near ? log(sig * ms) + 0.5 * log1p(zr * (2.0 + zr)) : log(sig * fabs(cmu));
+}
+
+// the streamed group series (gmf_kernel.hpp:493-519) of the ND divided differences; REAL: every in-group offset
+// and hence every term is real (half the FP64 instructions of the complex recursion)
+template <int ND, bool REAL>
+MF_D void group_series(int K, double b0, const GmfCoef &C, const bool *inG, const bool *pk, const cx *u, double iap,
+                       cx *D) {
+  cx Ep[ND], Ec[ND];
+#pragma unroll
+  for (int c = 0; c < ND; c++)
+    Ep[c] = csel(inG[gnode(c)], cmk(0.0, 0.0), gpar(c) < 0 ? cmk(1.0, 0.0) : Ep[gpar(c) < 0 ? 0 : gpar(c)]);
+  double q1 = 0.0, q2 = 0.0, q3 = 0.0;
+  for (int j = 0; j < K; j++) {
+    double bj = j == 0 ? b0 : C.bt[j];
+    double g1 = (bj - q1) * iap, g2 = (g1 - q2) * iap, g3 = (g2 - q3) * iap;
+    q1 = g1; q2 = g2; q3 = g3;
+    double qv[4] = {bj, g1, g2, g3};
+#pragma unroll
+    for (int c = 0; c < ND; c++) {
+      const int par = gpar(c), i = gnode(c);
+      cx epp = par < 0 ? cmk(sel(j == 0, 1.0, 0.0), 0.0) : Ep[par < 0 ? 0 : par];
+      cx epc = par < 0 ? cmk(0.0, 0.0) : Ec[par < 0 ? 0 : par];
+      double g = sel(pk[0], qv[gms(c, 0)], sel(pk[1], qv[gms(c, 1)], sel(pk[2], qv[gms(c, 2)], qv[0])));
+      if (REAL) {
+        Ec[c].re = sel(inG[i], epp.re + u[i].re * Ep[c].re, epc.re);
+        Ec[c].im = 0.0;
+        D[c].re = D[c].re + Ec[c].re * g;
+      } else {
+        Ec[c] = csel(inG[i], cadd(epp, cmul(u[i], Ep[c])), epc);
+        D[c] = cadd(D[c], cscl(Ec[c], g));
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < ND; c++) Ep[c] = Ec[c];
+  }
 }
 
 // the per-matrix record the kernels contract into F, J, H
@@ -416,33 +462,15 @@ MF_D void gmf_record(const double *a, const GmfCoef &C, GmfRec &R) {
   double rq = sel((pk[0] | pk[1] | pk[2]) & (rr * fabs(iap) <= 1.0), rr * fabs(iap), 0.0);
   rr = sel(hasg & (rr <= G_R_EXP + 0.5), rr, 0.0);
   double b0 = 1.0;
-  if (KIND == LOG) b0 = coef0<LOG>(C, sig, m, cmk(cxg, 0.0), cmk(cmu, 0.0), 0).re;
+  if (KIND == LOG) b0 = log_b0(sig, m, cxg, cmu);
   cx D[ND];
 #pragma unroll
   for (int c = 0; c < ND; c++) D[c] = cmk(0.0, 0.0);
   if (hasg) {
     const int K = nterms(C, 3 * (ORDER + 1) - 1, rr, rq);
-    cx Ep[ND], Ec[ND];
-#pragma unroll
-    for (int c = 0; c < ND; c++) Ep[c] = csel(inG[gnode(c)], cmk(0.0, 0.0), gpar(c) < 0 ? cmk(1.0, 0.0) : Ep[gpar(c) < 0 ? 0 : gpar(c)]);
-    double q1 = 0.0, q2 = 0.0, q3 = 0.0;
-    for (int j = 0; j < K; j++) {
-      double bj = j == 0 ? b0 : C.bt[j];
-      double g1 = (bj - q1) * iap, g2 = (g1 - q2) * iap, g3 = (g2 - q3) * iap;
-      q1 = g1; q2 = g2; q3 = g3;
-      double qv[4] = {bj, g1, g2, g3};
-#pragma unroll
-      for (int c = 0; c < ND; c++) {
-        const int par = gpar(c), i = gnode(c);
-        cx epp = par < 0 ? cmk(sel(j == 0, 1.0, 0.0), 0.0) : Ep[par < 0 ? 0 : par];
-        cx epc = par < 0 ? cmk(0.0, 0.0) : Ec[par < 0 ? 0 : par];
-        Ec[c] = csel(inG[i], cadd(epp, cmul(u[i], Ep[c])), epc);
-        double g = sel(pk[0], qv[gms(c, 0)], sel(pk[1], qv[gms(c, 1)], sel(pk[2], qv[gms(c, 2)], qv[0])));
-        D[c] = cadd(D[c], cscl(Ec[c], g));
-      }
-#pragma unroll
-      for (int c = 0; c < ND; c++) Ep[c] = Ec[c];
-    }
+    const bool real = (u[0].im == 0) & (u[1].im == 0) & (u[2].im == 0);
+    if (__all_sync(__activemask(), real)) group_series<ND, true>(K, b0, C, inG, pk, u, iap, D);
+    else group_series<ND, false>(K, b0, C, inG, pk, u, iap, D);
 #pragma unroll
     for (int c = 0; c < ND; c++) {
       const int nn = gms(c, 0) + gms(c, 1) + gms(c, 2) - 1, k = gms(c, 0) - 1;

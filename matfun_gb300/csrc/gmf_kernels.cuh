@@ -1,16 +1,22 @@
-// gmf_kernels.cu -- general family (gmf_cuda_eval): F, J, H of f(A) for general real 3x3 matrices, FP64, matrix
+// gmf_kernels.cuh -- general family (gmf_cuda_eval): F, J, H of f(A) for general real 3x3 matrices, FP64, matrix
 // layout.  Replaces gmf_eval_kernel of the reference (cuda/src/matfun_cuda.cu:144-190).
 //
-// One CTA = 64 matrices.  Phase A: one thread per matrix computes the record of gmf_device.cuh (F, the real basis
-// r_1, r_2 and the symmetric reduced divided differences D2', D3').  Phase B contracts them per thread into
-//   T4[P1, P2]     = sum_mn  D2'_mn  r_m[P1] r_n[P2]            (symmetric: 45 distinct of 81)
-//   T6[P1, P2, P3] = sum_mnp D3'_mnp r_m[P1] r_n[P2] r_p[P3]    (symmetric: 165 distinct of 729)
-// (P = 3a + c a matrix entry, r_0 = I) into shared memory, and the CTA writes
+// One CTA = 64 matrices (two warps).
+// Phase A: one thread per matrix computes the record of gmf_device.cuh -- F, the real basis r_1, r_2 (r_0 = I) and
+//   the symmetric reduced divided differences D2' (6), D3' (10) -- into shared memory (36 doubles per matrix).
+// Phase B: each warp walks its 32 matrices; for one matrix the 32 lanes build, through shared memory,
+//   Y2[y][m]      = sum_n D2'_mn r_n[y]                       (27)
+//   T4[x, y]      = sum_m r_m[x] Y2[y][m]                      (symmetric: 45 distinct of 81)
+//   Z[z][m, n]    = sum_p D3'_mnp r_p[z]                       (54)
+//   Y[y, z][m]    = sum_n Z[z][m, n] r_n[y]                    (135)
+//   T6[x, y, z]   = sum_m r_m[x] Y[y, z][m]                    (symmetric: 165 distinct of 729)
+// (x, y, z = 3a + c index matrix entries) and writes, 32 consecutive doubles per store,
 //   J_abcd   = sc1 T4[ac, db]
-//   H_abcdef = sc2 (T6[ac, de, fb] + T6[ae, fc, db])
-// with fully coalesced stores.  The reference forms Y (27), Z (81) and Yh (243) per matrix and evaluates all 729 H
-// entries with 6 multiply-adds each from every thread (gmf_kernel.hpp:636-691); the symmetric form needs about a
-// third of the FP64 instructions, which on GB300 (FP64 at 1/74 of the FP32 rate) is what bounds this kernel.
+//   H_abcdef = sc2 (T6[ac, de, fb] + T6[ae, fc, db]).
+// The reference forms Y (27), Z (81) and Yh (243) per matrix and evaluates each of the 729 H entries with 6
+// multiply-adds in every thread (gmf_kernel.hpp:636-691); the symmetric form needs about a third of the FP64
+// instructions, which bound this kernel on GB300 (FP64 at 1/74 of the FP32 rate).  Spreading one matrix over the
+// warp keeps the shared memory per CTA small (31 KB), so the occupancy is set by the registers of phase A.
 #pragma once
 #include "gmf_device.cuh"
 #include "mf_launch.h"
@@ -18,182 +24,177 @@
 namespace mf {
 
 constexpr int GMF_TPB = 64;
+constexpr int GMF_REC = 36;  // r1 (9), r2 (9), D2' (6), D3' (10), sc1, sc2
 
-// r_m[P] with r_0 = I (known per P at compile time after unrolling)
-#define MF_R0(P) ((P) % 4 == 0 ? 1.0 : 0.0)
+// shared memory layout of one CTA (doubles unless noted)
+struct GmfSmem {
+  double x[GMF_TPB * 9];          // input, then F
+  double rec[GMF_TPB * GMF_REC];  // records
+  double work[2][54 + 135 + 165]; // per warp: Z, Y, T6 (J: Y2 in Z, T4 in Y)
+  unsigned short hmap[729];       // H entry -> (T6 index of the first term) | (second) << 8
+  unsigned short t6map[165];      // T6 item -> x | y << 4 | z << 8
+  unsigned short ymap[135];       // Y item  -> y | z << 4 | m << 8
+};
+
+// a T6 index pair of an H entry w = 243 a + 81 b + 27 c + 9 d + 3 e + f
+MF_D unsigned short hmap_entry(int w) {
+  const int a = w / 243, b = (w / 81) % 3, c = (w / 27) % 3, d = (w / 9) % 3, e = (w / 3) % 3, f = w % 3;
+  int x1 = 3 * a + c, y1 = 3 * d + e, z1 = 3 * f + b;
+  int x2 = 3 * a + e, y2 = 3 * f + c, z2 = 3 * d + b;
+  sort3(x1, y1, z1);
+  sort3(x2, y2, z2);
+  return (unsigned short)(sym3(x1, y1, z1) | (sym3(x2, y2, z2) << 8));
+}
 
 template <int KIND, int ORDER>
 __global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const double *__restrict__ A, double *__restrict__ F,
                                                       double *__restrict__ J, double *__restrict__ H,
                                                       const GmfCoef C) {
-  extern __shared__ double smem[];
-  double *sX = smem;                        // 64 x 9: input, then F
-  double *sS = smem + GMF_TPB * 9;          // 64 x 2: output scale of J / H (1 when folded into T4 / T6)
-  double *sT = smem + GMF_TPB * 11;         // 64 x 45 (T4) or 64 x 165 (T6)
-  const int tid = threadIdx.x;
+  __shared__ GmfSmem S;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t base = (int64_t)blockIdx.x * GMF_TPB;
   const int cnt = (int)min((int64_t)GMF_TPB, n - base);
 
-  for (int e = tid; e < cnt * 9; e += GMF_TPB) sX[e] = A[base * 9 + e];
+  for (int e = tid; e < cnt * 9; e += GMF_TPB) S.x[e] = A[base * 9 + e];
+  if (ORDER >= 2) {  // index tables of phase B
+    for (int w = tid; w < 729; w += GMF_TPB) S.hmap[w] = hmap_entry(w);
+    for (int t = tid; t < 165; t += GMF_TPB) {
+      int z = 0;
+      while (sym3(0, 0, z + 1) <= t) z++;
+      int y = 0;
+      while (sym3(0, y + 1, z) <= t && y + 1 <= z) y++;
+      S.t6map[t] = (unsigned short)((t - sym3(0, y, z)) | (y << 4) | (z << 8));
+    }
+    for (int t = tid; t < 135; t += GMF_TPB) {
+      const int pr = t / 3, m = t % 3;
+      int z = 0;
+      while (sym2(0, z + 1) <= pr) z++;
+      S.ymap[t] = (unsigned short)((pr - sym2(0, z)) | (z << 4) | (m << 8));
+    }
+  }
   __syncthreads();
-  GmfRec R;
-  const bool active = tid < cnt;
-  if (active) {
+
+  // ---- phase A: one thread per matrix
+  if (tid < cnt) {
     double a[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) a[k] = sX[tid * 9 + k];
+    for (int k = 0; k < 9; k++) a[k] = S.x[tid * 9 + k];
+    GmfRec R;
     gmf_record<KIND, ORDER>(a, C, R);
-  }
-  __syncthreads();
-  if (active) {
 #pragma unroll
-    for (int k = 0; k < 9; k++) sX[tid * 9 + k] = R.F[k];
+    for (int k = 0; k < 9; k++) S.x[tid * 9 + k] = R.F[k];
+    if (ORDER >= 1) {
+      double *rc = S.rec + tid * GMF_REC;
+#pragma unroll
+      for (int k = 0; k < 9; k++) { rc[k] = R.r1[k]; rc[9 + k] = R.r2[k]; }
+#pragma unroll
+      for (int k = 0; k < 6; k++) rc[18 + k] = R.D2[k];
+      if (ORDER >= 2) {
+#pragma unroll
+        for (int k = 0; k < 10; k++) rc[24 + k] = R.D3[k];
+        rc[35] = R.sc2;
+      }
+      rc[34] = R.sc1;
+    }
   }
   __syncthreads();
-  for (int e = tid; e < cnt * 9; e += GMF_TPB) F[base * 9 + e] = sX[e];
+  for (int e = tid; e < cnt * 9; e += GMF_TPB) F[base * 9 + e] = S.x[e];
   if (ORDER < 1) return;
 
-  // ---- J: T4 per thread, then the coalesced gather
-  if (active) {
-    const bool fold = isfinite(R.sc1) & (R.sc1 != 0.0);
-    const double s = sel(fold, R.sc1, 1.0);
-    sS[tid * 2] = sel(fold, 1.0, R.sc1);
-    const double D00 = R.D2[0] * s, D11 = R.D2[1] * s, D22 = R.D2[2] * s, D01 = R.D2[3] * s, D02 = R.D2[4] * s,
-                 D12 = R.D2[5] * s;
-    double *t4 = sT + tid * 45;
-#pragma unroll
-    for (int y = 0; y < 9; y++) {
-      // Y2[m] = sum_n D2'_mn r_n[y]
-      const double y0 = (y % 4 == 0 ? D00 : 0.0) + D01 * R.r1[y] + D02 * R.r2[y];
-      const double y1 = (y % 4 == 0 ? D01 : 0.0) + D11 * R.r1[y] + D12 * R.r2[y];
-      const double y2 = (y % 4 == 0 ? D02 : 0.0) + D12 * R.r1[y] + D22 * R.r2[y];
-#pragma unroll
-      for (int xx = 0; xx <= y; xx++) t4[sym2(xx, y)] = (xx % 4 == 0 ? y0 : 0.0) + R.r1[xx] * y1 + R.r2[xx] * y2;
-    }
-  }
-  __syncthreads();
-  {
-    constexpr int KJ = (81 + GMF_TPB - 1) / GMF_TPB;
-    int jidx[KJ];
-#pragma unroll
-    for (int k = 0; k < KJ; k++) {
-      const int w = min(tid + GMF_TPB * k, 80);
-      const int a = w / 27, b = (w / 9) % 3, c = (w / 3) % 3, d = w % 3;
-      const int p1 = 3 * a + c, p2 = 3 * d + b;
-      jidx[k] = sym2(min(p1, p2), max(p1, p2));
-    }
-    for (int mi = 0; mi < cnt; mi++) {
+  // ---- phase B: the warp's 32 matrices one after the other
+  double *wk = S.work[warp];
+  const int m0 = warp * 32, m1 = min(cnt, m0 + 32);
+  for (int mi = m0; mi < m1; mi++) {
+    const double *rc = S.rec + mi * GMF_REC;
+    const double *r1 = rc, *r2 = rc + 9;
+    // J: fold sc1 into D2' when finite and nonzero (else multiply each entry, keeping the reference's NaN / Inf)
+    {
+      const double sc1 = rc[34];
+      const bool fold = isfinite(sc1) & (sc1 != 0.0);
+      const double s = sel(fold, sc1, 1.0);
+      if (lane < 27) {  // Y2[y][m] = sum_n D2'_mn r_n[y]
+        const int y = lane / 3, m = lane % 3;
+        const int i0 = m == 0 ? 0 : (m == 1 ? 3 : 4), i1 = m == 0 ? 3 : (m == 1 ? 1 : 5), i2 = m == 0 ? 4 : (m == 1 ? 5 : 2);
+        const double d0 = rc[18 + i0] * s, d1 = rc[18 + i1] * s, d2 = rc[18 + i2] * s;
+        wk[lane] = (y % 4 == 0 ? d0 : 0.0) + d1 * r1[y] + d2 * r2[y];
+      }
+      __syncwarp();
+      for (int t = lane; t < 45; t += 32) {  // T4[x, y] = sum_m r_m[x] Y2[y][m], x <= y
+        int y = 0;
+        while (sym2(0, y + 1) <= t) y++;
+        const int x = t - sym2(0, y);
+        const double *yv = wk + 3 * y;
+        wk[54 + t] = (x % 4 == 0 ? yv[0] : 0.0) + r1[x] * yv[1] + r2[x] * yv[2];
+      }
+      __syncwarp();
       double *o = J + (base + mi) * 81;
-      const double *t = sT + mi * 45;
-      const double sc = sS[mi * 2];
-      const bool plain = sc == 1.0;
-#pragma unroll
-      for (int k = 0; k < KJ; k++) {
-        if (tid + GMF_TPB * k < 81) {
-          const double v = t[jidx[k]];
-          o[tid + GMF_TPB * k] = plain ? v : v * sc;
-        }
+      for (int w = lane; w < 81; w += 32) {
+        const int a = w / 27, b = (w / 9) % 3, c = (w / 3) % 3, d = w % 3;
+        const int p1 = 3 * a + c, p2 = 3 * d + b;
+        const double v = wk[54 + sym2(min(p1, p2), max(p1, p2))];
+        o[w] = fold ? v : v * sc1;
       }
+      __syncwarp();
     }
-  }
-  if (ORDER < 2) return;
-  __syncthreads();
-
-  // ---- H: T6 per thread, then the coalesced gather
-  if (active) {
-    const bool fold = isfinite(R.sc2) & (R.sc2 != 0.0);
-    const double s = sel(fold, R.sc2, 1.0);
-    sS[tid * 2 + 1] = sel(fold, 1.0, R.sc2);
-    double d3[10];
-#pragma unroll
-    for (int k = 0; k < 10; k++) d3[k] = R.D3[k] * s;
-    double *t6 = sT + tid * 165;
-#pragma unroll
-    for (int z = 0; z < 9; z++) {
-      // Zz[m][n] = sum_p D3'_mnp r_p[z]   (m <= n)
-      double Zz[3][3];
-      // sorted index of the triple (m, n, p) for p = 0, 1, 2 (m <= n)
-#pragma unroll
-      for (int mm = 0; mm < 3; mm++)
-#pragma unroll
-        for (int nn = mm; nn < 3; nn++) {
-          const int i0 = sym3(0, mm, nn);
-          const int i1 = nn <= 1 ? sym3(mm, nn, 1) : (mm <= 1 ? sym3(mm, 1, nn) : sym3(1, mm, nn));
-          const int i2 = sym3(mm, nn, 2);
-          Zz[mm][nn] = (z % 4 == 0 ? d3[i0] : 0.0) + d3[i1] * R.r1[z] + d3[i2] * R.r2[z];
-          Zz[nn][mm] = Zz[mm][nn];
-        }
-#pragma unroll
-      for (int y = 0; y <= z; y++) {
-        const double Y0 = (y % 4 == 0 ? Zz[0][0] : 0.0) + Zz[0][1] * R.r1[y] + Zz[0][2] * R.r2[y];
-        const double Y1 = (y % 4 == 0 ? Zz[1][0] : 0.0) + Zz[1][1] * R.r1[y] + Zz[1][2] * R.r2[y];
-        const double Y2 = (y % 4 == 0 ? Zz[2][0] : 0.0) + Zz[2][1] * R.r1[y] + Zz[2][2] * R.r2[y];
-#pragma unroll
-        for (int xx = 0; xx <= y; xx++)
-          t6[sym3(xx, y, z)] = (xx % 4 == 0 ? Y0 : 0.0) + R.r1[xx] * Y1 + R.r2[xx] * Y2;
+    if (ORDER < 2) continue;
+    {
+      const double sc2 = rc[35];
+      const bool fold = isfinite(sc2) & (sc2 != 0.0);
+      const double s = sel(fold, sc2, 1.0);
+      const double *d3 = rc + 24;
+      double *Zs = wk, *Ys = wk + 54, *T6 = wk + 54 + 135;
+      for (int t = lane; t < 54; t += 32) {  // Z[z][mn] = sum_p D3'_mnp r_p[z]  (mn: 00 01 02 11 12 22)
+        const int z = t / 6, mn = t % 6;
+        const int mm = mn < 3 ? 0 : (mn < 5 ? 1 : 2), nn = mn < 3 ? mn : (mn < 5 ? mn - 2 : 2);
+        const int i0 = sym3(0, mm, nn);
+        const int i1 = nn <= 1 ? sym3(mm, nn, 1) : (mm <= 1 ? sym3(mm, 1, nn) : sym3(1, mm, nn));
+        const int i2 = sym3(mm, nn, 2);
+        Zs[t] = (z % 4 == 0 ? d3[i0] * s : 0.0) + (d3[i1] * s) * r1[z] + (d3[i2] * s) * r2[z];
       }
-    }
-  }
-  __syncthreads();
-  {
-    constexpr int KH = (729 + GMF_TPB - 1) / GMF_TPB;
-    int h1[KH], h2[KH];
-#pragma unroll
-    for (int k = 0; k < KH; k++) {
-      const int w = min(tid + GMF_TPB * k, 728);
-      const int a = w / 243, b = (w / 81) % 3, c = (w / 27) % 3, d = (w / 9) % 3, e = (w / 3) % 3, f = w % 3;
-      int x1 = 3 * a + c, y1 = 3 * d + e, z1 = 3 * f + b;
-      int x2 = 3 * a + e, y2 = 3 * f + c, z2 = 3 * d + b;
-      sort3(x1, y1, z1);
-      sort3(x2, y2, z2);
-      h1[k] = sym3(x1, y1, z1);
-      h2[k] = sym3(x2, y2, z2);
-    }
-    for (int mi = 0; mi < cnt; mi++) {
+      __syncwarp();
+      for (int t = lane; t < 135; t += 32) {  // Y[y, z][m] = sum_n Z[z][m, n] r_n[y]
+        const unsigned short e = S.ymap[t];
+        const int y = e & 15, z = (e >> 4) & 15, m = e >> 8;
+        const double *zz = Zs + 6 * z;
+        const int k0 = m == 0 ? 0 : (m == 1 ? 1 : 2), k1 = m == 0 ? 1 : (m == 1 ? 3 : 4), k2 = m == 0 ? 2 : (m == 1 ? 4 : 5);
+        Ys[t] = (y % 4 == 0 ? zz[k0] : 0.0) + zz[k1] * r1[y] + zz[k2] * r2[y];
+      }
+      __syncwarp();
+      for (int t = lane; t < 165; t += 32) {  // T6[x, y, z] = sum_m r_m[x] Y[y, z][m]
+        const unsigned short e = S.t6map[t];
+        const int x = e & 15, y = (e >> 4) & 15, z = e >> 8;
+        const double *yv = Ys + 3 * sym2(y, z);
+        T6[t] = (x % 4 == 0 ? yv[0] : 0.0) + r1[x] * yv[1] + r2[x] * yv[2];
+      }
+      __syncwarp();
       double *o = H + (base + mi) * 729;
-      const double *t = sT + mi * 165;
-      const double sc = sS[mi * 2 + 1];
-      const bool plain = sc == 1.0;
-#pragma unroll
-      for (int k = 0; k < KH; k++) {
-        if (tid + GMF_TPB * k < 729) {
-          const double v = t[h1[k]] + t[h2[k]];
-          o[tid + GMF_TPB * k] = plain ? v : v * sc;
-        }
+      for (int w = lane; w < 729; w += 32) {
+        const unsigned short e = S.hmap[w];
+        const double v = T6[e & 255] + T6[e >> 8];
+        o[w] = fold ? v : v * sc2;
       }
+      __syncwarp();
     }
   }
-}
-#undef MF_R0
-
-inline size_t gmf_smem(int order) {
-  return sizeof(double) * GMF_TPB * (11 + (order == 2 ? 165 : (order == 1 ? 45 : 0)));
 }
 
 template <int KIND, int ORDER>
 cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const double *A, double *F, double *J,
-                                  double *H, const GmfCoef &C) {
-  static bool attr_done = false;  // per instantiation; setting the attribute twice is harmless
-  const size_t smem = gmf_smem(ORDER);
-  if (!attr_done) {
-    const cudaError_t e = cudaFuncSetAttribute(gmf_kernel<KIND, ORDER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_done = true;
-  }
-  gmf_kernel<KIND, ORDER><<<blocks, GMF_TPB, smem, st>>>(n, A, F, J, H, C);
+                           double *H, const GmfCoef &C) {
+  gmf_kernel<KIND, ORDER><<<blocks, GMF_TPB, 0, st>>>(n, A, F, J, H, C);
   return cudaGetLastError();
 }
 
 template <int KIND>
 cudaError_t gmf_launch_kind(int order, cudaStream_t st, unsigned blocks, int64_t n, const double *A, double *F,
-                                   double *J, double *H, const GmfCoef &C) {
+                            double *J, double *H, const GmfCoef &C) {
   if (order == 2) return gmf_launch_one<KIND, 2>(st, blocks, n, A, F, J, H, C);
   if (order == 1) return gmf_launch_one<KIND, 1>(st, blocks, n, A, F, J, H, C);
   return gmf_launch_one<KIND, 0>(st, blocks, n, A, F, J, H, C);
 }
 
-// host: launch constants (gmf_kernel.hpp:48-53 series coefficients, :84 binomial recurrence)
+// host: launch constants (series coefficients gmf_kernel.hpp:48-53; the binomial factors of the term bound by the
+// recurrence of gmf_kernel.hpp:84, as log2 values)
 inline void gmf_coef(int kind, double al, int order, GmfCoef &C) {
   C.al = al;
   C.rho_f = (kind == POW && 3.0 / al < G_RHO) ? 3.0 / al : G_RHO;
@@ -208,7 +209,8 @@ inline void gmf_coef(int kind, double al, int order, GmfCoef &C) {
   const int nn = 3 * (order + 1) - 1;
   double c = 1.0;
   for (int k = 0; k < G_KMAX; k++) {
-    C.bin[k] = c;
+    const double t = nn + k < G_KMAX ? std::fabs(C.bt[nn + k]) * c : 0.0;
+    C.lterm[k] = t > 0 ? (float)std::log2(t) : -INFINITY;
     c = c * (k + nn + 1) / (k + 1);
   }
 }

@@ -4,6 +4,7 @@
 // FP64 instructions where an exact integer or select form exists: powers of two are made by masking exponent bits,
 // maxima of non-negative values are taken on their bit patterns, and selects are plain register moves.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 

@@ -33,7 +33,8 @@ def test_gmf_log_full_size(c1):
     assert bool((torch.isnan(H).flatten(1).all(1) == bad).all())
     assert int(bad[n // 2:].sum()) == 0 and int(bad.sum()) < n // 50
     # H_abcdef = H_abefcd exactly (the two index pairs of the second derivative)
-    assert bool((H == H.permute(0, 1, 2, 5, 6, 3, 4)).all())
+    Hp = H.permute(0, 1, 2, 5, 6, 3, 4)
+    assert bool(((H == Hp) | (torch.isnan(H) & torch.isnan(Hp))).all())
     # a sample against the oracle, one from each group of the workload
     idx = np.concatenate([np.arange(g * n // 4, g * n // 4 + 512) for g in range(4)])
     Fo, Jo, Ho = ol.gmf("log", c1[idx], order=2)
