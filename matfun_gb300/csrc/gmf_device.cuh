@@ -235,6 +235,18 @@ MF_D void group_series(int K, double b0, const GmfCoef &C, const bool *inG, cons
   }
 }
 
+// the state after the spectral analysis (eigenvalues, refinement, node order, groups, offsets, series length):
+// everything the divided differences and the basis need.  Between the two halves the kernel sorts the matrices of a
+// CTA by class and series length, so that the lanes of a warp do the same amount of the same work.
+struct GmfState {
+  double As[9];                     // A scaled by 1 / sig
+  double sig, m, cxg, cmu, xshift, iap, L, iL;
+  cx x[3], mu[3], u[3];
+  int K;                            // series terms; 0 without a group
+  int flags;                        // ab (bits 0-2), inG (3-5), pk (6-8), bad (9), real offsets (10)
+};
+constexpr int GMF_STATE_D = 9 + 8 + 18;  // doubles of a packed state (K and flags in two ints apart)
+
 // the per-matrix record the kernels contract into F, J, H
 struct GmfRec {
   double F[9];
@@ -245,8 +257,7 @@ struct GmfRec {
 };
 
 template <int KIND, int ORDER>
-MF_D void gmf_record(const double *a, const GmfCoef &C, GmfRec &R) {
-  constexpr int ND = ORDER == 0 ? 3 : (ORDER == 1 ? 9 : 19);
+MF_D void gmf_classify(const double *a, const GmfCoef &C, GmfState &St) {
   // ---- scaling (exp: none), shift m, deviator S
   double amax = fabs(a[0]);
 #pragma unroll
@@ -461,16 +472,46 @@ MF_D void gmf_record(const double *a, const GmfCoef &C, GmfRec &R) {
   double rr = tmax(cabs_s(u[0]), tmax(cabs_s(u[1]), cabs_s(u[2])));
   double rq = sel((pk[0] | pk[1] | pk[2]) & (rr * fabs(iap) <= 1.0), rr * fabs(iap), 0.0);
   rr = sel(hasg & (rr <= G_R_EXP + 0.5), rr, 0.0);
+  St.K = hasg ? nterms(C, 3 * (ORDER + 1) - 1, rr, rq) : 0;
+  bool real = (u[0].im == 0) & (u[1].im == 0) & (u[2].im == 0);
+#pragma unroll
+  for (int k = 0; k < 9; k++) St.As[k] = As[k];
+  St.sig = sig; St.m = m; St.cxg = cxg; St.cmu = cmu; St.xshift = xshift; St.iap = iap; St.L = L; St.iL = iL;
+#pragma unroll
+  for (int i = 0; i < 3; i++) { St.x[i] = x[i]; St.mu[i] = mu[i]; St.u[i] = u[i]; }
+  St.flags = (ab[0] ? 1 : 0) | (ab[1] ? 2 : 0) | (ab[2] ? 4 : 0) | (inG[0] ? 8 : 0) | (inG[1] ? 16 : 0) |
+             (inG[2] ? 32 : 0) | (pk[0] ? 64 : 0) | (pk[1] ? 128 : 0) | (pk[2] ? 256 : 0) | (bad ? 512 : 0) |
+             (real ? 1024 : 0);
+}
+
+// the second half: divided differences (series, residues), real basis, F and the reduced D2', D3'
+template <int KIND, int ORDER>
+MF_D void gmf_finish(const GmfState &St, const GmfCoef &C, GmfRec &R) {
+  constexpr int ND = ORDER == 0 ? 3 : (ORDER == 1 ? 9 : 19);
+  double As[9], S[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) As[k] = St.As[k];
+  const double sig = St.sig, isig = 1.0 / sig, m = St.m, cxg = St.cxg, cmu = St.cmu, xshift = St.xshift;
+  const double iap = St.iap, L = St.L, iL = St.iL;
+#pragma unroll
+  for (int k = 0; k < 9; k++) S[k] = k % 4 == 0 ? As[k] - m : As[k];
+  cx x[3], mu[3], u[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) { x[i] = St.x[i]; mu[i] = St.mu[i]; u[i] = St.u[i]; }
+  const int fl = St.flags;
+  bool ab[3] = {(fl & 1) != 0, (fl & 2) != 0, (fl & 4) != 0};
+  bool inG[3] = {(fl & 8) != 0, (fl & 16) != 0, (fl & 32) != 0};
+  bool pk[3] = {(fl & 64) != 0, (fl & 128) != 0, (fl & 256) != 0};
+  const bool bad = (fl & 512) != 0, hasg = St.K > 0;
   double b0 = 1.0;
   if (KIND == LOG) b0 = log_b0(sig, m, cxg, cmu);
   cx D[ND];
 #pragma unroll
   for (int c = 0; c < ND; c++) D[c] = cmk(0.0, 0.0);
   if (hasg) {
-    const int K = nterms(C, 3 * (ORDER + 1) - 1, rr, rq);
-    const bool real = (u[0].im == 0) & (u[1].im == 0) & (u[2].im == 0);
-    if (__all_sync(__activemask(), real)) group_series<ND, true>(K, b0, C, inG, pk, u, iap, D);
-    else group_series<ND, false>(K, b0, C, inG, pk, u, iap, D);
+    const bool real = (fl & 1024) != 0;
+    if (__all_sync(__activemask(), real)) group_series<ND, true>(St.K, b0, C, inG, pk, u, iap, D);
+    else group_series<ND, false>(St.K, b0, C, inG, pk, u, iap, D);
 #pragma unroll
     for (int c = 0; c < ND; c++) {
       const int nn = gms(c, 0) + gms(c, 1) + gms(c, 2) - 1, k = gms(c, 0) - 1;
@@ -496,15 +537,21 @@ MF_D void gmf_record(const double *a, const GmfCoef &C, GmfRec &R) {
     if (KIND == POW && ORDER >= 1) f0[1] = coef0<KIND>(C, sig, m, xs, mu[i], 1);
     if (KIND == POW && ORDER >= 2) f0[2] = coef0<KIND>(C, sig, m, xs, mu[i], 2);
     cx imu = cinv_s(mu[i]);
-    cx w[3];
+    // powers w_z^e (e = 1..5) of 1 / (mu_i - mu_z) for the two other nodes z: the Taylor coefficients of
+    // 1 / (t - mu_z)^mz at mu_i are (w^mz, -mz w^(mz+1), mz (mz+1)/2 w^(mz+2))
+    const int za = i == 0 ? 1 : 0, zb = i == 2 ? 1 : 2;
+    cx wa[6], wb[6];
+    wa[0] = cmk(1.0, 0.0);
+    wb[0] = cmk(1.0, 0.0);
+    wa[1] = cinv_s(csel(ab[i] | ab[za], csub(mu[i], mu[za]), csub(x[i], x[za])));
+    wb[1] = cinv_s(csel(ab[i] | ab[zb], csub(mu[i], mu[zb]), csub(x[i], x[zb])));
 #pragma unroll
-    for (int z = 0; z < 3; z++)
-      if (z != i) w[z] = cinv_s(csel(ab[i] | ab[z], csub(mu[i], mu[z]), csub(x[i], x[z])));
+    for (int e = 2; e < 6; e++) { wa[e] = cmul(wa[e - 1], wa[1]); wb[e] = cmul(wb[e - 1], wb[1]); }
 #pragma unroll
     for (int c = 0; c < ND; c++) {
       const int mi = gms(c, i);
       if (mi == 0) continue;
-      const int k = gms(c, 0) - 1;
+      const int k = gms(c, 0) - 1, ma = gms(c, za), mb = gms(c, zb);
       cx fb = KIND == POW ? f0[k] : f0[0], ser[3];
       if (KIND == EXP) {
         ser[0] = fb; ser[1] = fb; ser[2] = cscl(fb, 0.5);
@@ -515,20 +562,29 @@ MF_D void gmf_record(const double *a, const GmfCoef &C, GmfRec &R) {
         ser[1] = cscl(cmul(fb, imu), C.al);
         ser[2] = cscl(cmul(ser[1], imu), (C.al - 1.0) / 2.0);
       }
-#pragma unroll
-      for (int z = 0; z < 3; z++) {
-        const int mz = gms(c, z);
-        if (z == i || mz == 0) continue;
-        cx wp = cmk(1.0, 0.0);
-#pragma unroll
-        for (int r = 0; r < mz; r++) wp = cmul(wp, w[z]);
-        cx p1 = cscl(cmul(wp, w[z]), (double)-mz);
-        cx p2 = cscl(cmul(cmul(wp, w[z]), w[z]), mz * (mz + 1) / 2.0);
-        cx n0 = cmul(ser[0], wp), n1 = cadd(cmul(ser[1], wp), cmul(ser[0], p1));
-        cx n2 = cadd(cadd(cmul(ser[2], wp), cmul(ser[1], p1)), cmul(ser[0], p2));
-        ser[0] = n0; ser[1] = n1; ser[2] = n2;
+      // coefficient mi - 1 of ser * Pa * Pb (truncated products, only the terms that are needed)
+      cx pa[3], pb[3];
+      pa[0] = wa[ma];
+      pb[0] = wb[mb];
+      if (mi >= 2) {
+        pa[1] = ma ? cscl(wa[ma + 1], (double)-ma) : cmk(0.0, 0.0);
+        pb[1] = mb ? cscl(wb[mb + 1], (double)-mb) : cmk(0.0, 0.0);
       }
-      D[c] = cadd(D[c], ser[mi - 1]);
+      if (mi >= 3) {
+        pa[2] = ma ? cscl(wa[ma + 2], ma * (ma + 1) / 2.0) : cmk(0.0, 0.0);
+        pb[2] = mb ? cscl(wb[mb + 2], mb * (mb + 1) / 2.0) : cmk(0.0, 0.0);
+      }
+      cx q[3];
+      q[0] = ma ? (mb ? cmul(pa[0], pb[0]) : pa[0]) : pb[0];
+      if (mi >= 2) q[1] = cadd(ma ? (mb ? cmul(pa[0], pb[1]) : cmk(0.0, 0.0)) : pb[1],
+                               mb ? (ma ? cmul(pa[1], pb[0]) : cmk(0.0, 0.0)) : pa[1]);
+      if (mi >= 3) q[2] = cadd(cadd(ma ? (mb ? cmul(pa[0], pb[2]) : cmk(0.0, 0.0)) : pb[2],
+                                    (ma && mb) ? cmul(pa[1], pb[1]) : cmk(0.0, 0.0)),
+                               mb ? (ma ? cmul(pa[2], pb[0]) : cmk(0.0, 0.0)) : pa[2]);
+      cx r = cmul(ser[0], q[mi - 1]);
+      if (mi >= 2) r = cadd(r, cmul(ser[1], q[mi - 2]));
+      if (mi >= 3) r = cadd(r, cmul(ser[2], q[0]));
+      D[c] = cadd(D[c], r);
     }
   }
 
@@ -610,6 +666,13 @@ MF_D void gmf_record(const double *a, const GmfCoef &C, GmfRec &R) {
 #pragma unroll
         for (int xx = 0; xx <= y; xx++) R.D3[sym3(xx, y, z)] = Dr[9 * xx + 3 * y + z];
   }
+}
+
+template <int KIND, int ORDER>
+MF_D void gmf_record(const double *a, const GmfCoef &C, GmfRec &R) {
+  GmfState St;
+  gmf_classify<KIND, ORDER>(a, C, St);
+  gmf_finish<KIND, ORDER>(St, C, R);
 }
 
 }  // namespace mf

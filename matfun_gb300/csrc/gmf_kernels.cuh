@@ -1,9 +1,12 @@
 // gmf_kernels.cuh -- general family (gmf_cuda_eval): F, J, H of f(A) for general real 3x3 matrices, FP64, matrix
 // layout.  Replaces gmf_eval_kernel of the reference (cuda/src/matfun_cuda.cu:144-190).
 //
-// One CTA = 64 matrices (two warps).
+// One CTA = 128 matrices (four warps).
 // Phase A: one thread per matrix computes the record of gmf_device.cuh -- F, the real basis r_1, r_2 (r_0 = I) and
-//   the symmetric reduced divided differences D2' (6), D3' (10) -- into shared memory (36 doubles per matrix).
+//   the symmetric reduced divided differences D2' (6), D3' (10) -- into shared memory (36 doubles per matrix), in two
+//   halves: after the spectral analysis (gmf_classify) the CTA ranks its matrices by class (no group / real series /
+//   complex series) and series length, and the second half (gmf_finish) runs in that order, so that a warp's lanes
+//   take the same branches and run series of similar length (unsorted, half of the lanes idled on average).
 // Phase B: each warp walks its 32 matrices; for one matrix the 32 lanes build, through shared memory,
 //   Y2[y][m]      = sum_n D2'_mn r_n[y]                       (27)
 //   T4[x, y]      = sum_m r_m[x] Y2[y][m]                      (symmetric: 45 distinct of 81)
@@ -23,14 +26,18 @@
 
 namespace mf {
 
-constexpr int GMF_TPB = 64;
+constexpr int GMF_TPB = 128;
+constexpr int GMF_WARPS = GMF_TPB / 32;
 constexpr int GMF_REC = 36;  // r1 (9), r2 (9), D2' (6), D3' (10), sc1, sc2
 
 // shared memory layout of one CTA (doubles unless noted)
 struct GmfSmem {
   double x[GMF_TPB * 9];          // input, then F
   double rec[GMF_TPB * GMF_REC];  // records
-  double work[2][54 + 135 + 165]; // per warp: Z, Y, T6 (J: Y2 in Z, T4 in Y)
+  GmfState state[GMF_TPB];        // the first half's results, by matrix
+  unsigned key[GMF_TPB];          // sort key of each matrix
+  int perm[GMF_TPB];              // processing slot -> matrix
+  double work[GMF_WARPS][54 + 135 + 165]; // per warp: Z, Y, T6 (J: Y2 in Z, T4 in Y)
   unsigned short hmap[729];       // H entry -> (T6 index of the first term) | (second) << 8
   unsigned short t6map[165];      // T6 item -> x | y << 4 | z << 8
   unsigned short ymap[135];       // Y item  -> y | z << 4 | m << 8
@@ -50,7 +57,8 @@ template <int KIND, int ORDER>
 __global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const double *__restrict__ A, double *__restrict__ F,
                                                       double *__restrict__ J, double *__restrict__ H,
                                                       const GmfCoef C) {
-  __shared__ GmfSmem S;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  GmfSmem &S = *reinterpret_cast<GmfSmem *>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t base = (int64_t)blockIdx.x * GMF_TPB;
   const int cnt = (int)min((int64_t)GMF_TPB, n - base);
@@ -74,17 +82,40 @@ __global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const double *_
   }
   __syncthreads();
 
-  // ---- phase A: one thread per matrix
+  // ---- phase A, first half: spectral analysis of matrix tid, and its sort key
+  unsigned key = 0xFFFFFFFFu;
   if (tid < cnt) {
     double a[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) a[k] = S.x[tid * 9 + k];
+    GmfState St;
+    gmf_classify<KIND, ORDER>(a, C, St);
+    S.state[tid] = St;
+    // class (no group < real series < complex series), longer series first, then the group's node pattern
+    const unsigned cls = St.K == 0 ? 0u : ((St.flags & 1024) ? 1u : 2u);
+    key = (cls << 16) | ((unsigned)(255 - St.K) << 6) | (unsigned)((St.flags >> 3) & 63);
+  }
+  S.key[tid] = key;
+  __syncthreads();
+  {
+    int rank = 0;
+    for (int j = 0; j < GMF_TPB; j++) {
+      const unsigned kj = S.key[j];
+      rank += (kj < key) | ((kj == key) & (j < tid));
+    }
+    S.perm[rank] = tid;
+  }
+  __syncthreads();
+
+  // ---- phase A, second half, in sorted order; results stored by matrix
+  const int mine = S.perm[tid];
+  if (mine < cnt) {
     GmfRec R;
-    gmf_record<KIND, ORDER>(a, C, R);
+    gmf_finish<KIND, ORDER>(S.state[mine], C, R);
 #pragma unroll
-    for (int k = 0; k < 9; k++) S.x[tid * 9 + k] = R.F[k];
+    for (int k = 0; k < 9; k++) S.x[mine * 9 + k] = R.F[k];
     if (ORDER >= 1) {
-      double *rc = S.rec + tid * GMF_REC;
+      double *rc = S.rec + mine * GMF_REC;
 #pragma unroll
       for (int k = 0; k < 9; k++) { rc[k] = R.r1[k]; rc[9 + k] = R.r2[k]; }
 #pragma unroll
@@ -103,7 +134,7 @@ __global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const double *_
 
   // ---- phase B: the warp's 32 matrices one after the other
   double *wk = S.work[warp];
-  const int m0 = warp * 32, m1 = min(cnt, m0 + 32);
+  const int m0 = warp * 32, m1 = min(cnt, m0 + 32);  // (phase B keeps the input order)
   for (int mi = m0; mi < m1; mi++) {
     const double *rc = S.rec + mi * GMF_REC;
     const double *r1 = rc, *r2 = rc + 9;
@@ -181,7 +212,14 @@ __global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const double *_
 template <int KIND, int ORDER>
 cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const double *A, double *F, double *J,
                            double *H, const GmfCoef &C) {
-  gmf_kernel<KIND, ORDER><<<blocks, GMF_TPB, 0, st>>>(n, A, F, J, H, C);
+  static bool attr = false;  // once per instantiation (idempotent; a racing second call sets the same value)
+  if (!attr) {
+    const cudaError_t e = cudaFuncSetAttribute(gmf_kernel<KIND, ORDER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)sizeof(GmfSmem));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  gmf_kernel<KIND, ORDER><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C);
   return cudaGetLastError();
 }
 

@@ -207,6 +207,21 @@ MF_D double smf_dd2(double li, double lj, double lk, double fi, double fj, doubl
   return out;
 }
 
+// f[l, l, l] = f''(l) / 2: the reference's cluster series at u = w = 0 is exactly scale * c2[0]; outside the
+// cluster its difference formula gives (D_ll - D_ll) / 1 (smf_kernel.hpp:148-192, specialised to three equal points)
+template <int KIND>
+MF_D double smf_dd2_same(double l, double fl, double Dll, const SmfCoef &C) {
+  if (KIND == POW || KIND == SQRT) l = sel(l > 0, l, 0.0);
+  bool cluster;
+  if (KIND == EXP) cluster = (l - l) <= 1.0;
+  else cluster = (l > 0) & (l - l <= C.tau * l) & (l - l <= C.tau * l);
+  double out;
+  if (KIND == EXP) out = sel(cluster, fl * C.c2[0], Dll - Dll);
+  else out = sel(cluster, ((KIND == LOG ? 1.0 : fl) / (l * l)) * C.c2[0], Dll - Dll);
+  if (KIND == POW || KIND == SQRT) out = sel(l > 0, out, C.z2);
+  return out;
+}
+
 // Voigt basis pair (k, l) of component p
 MF_D constexpr int vk_(int p) { return p < 3 ? p : (p == 5 ? 1 : 0); }
 MF_D constexpr int vl_(int p) { return p < 3 ? p : (p == 3 ? 1 : 2); }

@@ -4,7 +4,9 @@
 //
 // One CTA = 64 matrices (two warps).  Phase A: one thread per matrix computes the eigensystem, f, the divided
 // differences and the distinct entries of J (21 values of the symmetric form K) and H (56 values of the symmetric
-// form G'), see smf_device.cuh, into shared memory.  Phase B: the CTA expands them into the output layout with
+// form G'), see smf_device.cuh, into shared memory.  Both forms are evaluated through the product vectors
+// P_kl = (V_ka V_la)_a of rows of V: J from the 21 values of B(x, y) = sum D_ab x_a y_b, H from the 56 values of
+// T(x, y, z) = sum D2_amb x_a y_m z_b, about half the FP64 instructions of assembling V S V^T per index pair.  Phase B: the CTA expands them into the output layout with
 // fully coalesced stores (64 consecutive doubles per store instruction); the layout weights (powers of two) are
 // applied on the exponent bits, not on the FP64 pipe.
 #pragma once
@@ -14,6 +16,9 @@
 namespace mf {
 
 constexpr int SMF_TPB = 64;
+
+// index of the product vector of the Cartesian pair (k, l) (Voigt order 00 11 22 01 02 12)
+MF_D constexpr int pidx(int k, int l) { return k == l ? k : k + l + 2; }
 
 // x * 2^k for k in [-3, 1], exact; integer exponent arithmetic for normal x, a multiplication otherwise
 MF_D double mulpow2(double x, int k) {
@@ -84,78 +89,114 @@ __global__ void __launch_bounds__(SMF_TPB) smf_kernel(int64_t n, const double *_
       double D12 = smf_dd1<KIND>(lam[1], lam[2], fl[1], fl[2], C);
       double D00 = smf_deriv<KIND>(lam[0], fl[0], C), D11 = smf_deriv<KIND>(lam[1], fl[1], C);
       double D22 = smf_deriv<KIND>(lam[2], fl[2], C);
-      double Et[6][6];
-      smf_et(V, Et);
-      // K(I, p) = sum_ab D_ab Et_I,ab Et_p,ab  (off-diagonal pairs counted twice)
-      double Dw[6] = {D00, D11, D22, 2.0 * D01, 2.0 * D02, 2.0 * D12};
-      double *k_out = sK + tid * 21;
+      // product vectors P_s[a] = V[k][a] V[l][a] of the Voigt pairs s = (k, l): with them
+      //   K(I, p)     = B(P, P) sums,  B(x, y)    = sum_ab  D_ab  x_a y_b          (21 distinct values)
+      //   G'(I, p, q) = 2 T(P, P, P) sums, T(x, y, z) = sum_amb D2_amb x_a y_m z_b  (56 distinct values)
+      // because Et_p = V^T E_p V is a sum of one or two outer products of rows of V
+      double P[6][3];
 #pragma unroll
-      for (int I = 0; I < 6; I++) {
-        double de[6];
+      for (int s6 = 0; s6 < 6; s6++)
 #pragma unroll
-        for (int s = 0; s < 6; s++) de[s] = Dw[s] * Et[I][s];
+        for (int a = 0; a < 3; a++) P[s6][a] = V[vk_(s6)][a] * V[vl_(s6)][a];
+      const double Dm[3][3] = {{D00, D01, D02}, {D01, D11, D12}, {D02, D12, D22}};
+      {
+        double Bv[21];
 #pragma unroll
-        for (int p = I; p < 6; p++) {
-          double acc = de[0] * Et[p][0];
+        for (int g = 0; g < 6; g++) {
+          double dy[3];
 #pragma unroll
-          for (int s = 1; s < 6; s++) acc = fma(de[s], Et[p][s], acc);
-          k_out[sym2(I, p)] = acc;
+          for (int a = 0; a < 3; a++) dy[a] = Dm[a][0] * P[g][0] + Dm[a][1] * P[g][1] + Dm[a][2] * P[g][2];
+#pragma unroll
+          for (int b2 = 0; b2 <= g; b2++) Bv[sym2(b2, g)] = P[b2][0] * dy[0] + P[b2][1] * dy[1] + P[b2][2] * dy[2];
         }
+        double *k_out = sK + tid * 21;
+#pragma unroll
+        for (int I = 0; I < 6; I++)
+#pragma unroll
+          for (int p = I; p < 6; p++) {
+            // Et_I,ab Et_p,ab summed with D: the outer-product terms (s1, t1) of E_I and (s2, t2) of E_p give
+            // B(P[s1 s2], P[t1 t2])
+            double acc = 0.0;
+            bool first = true;
+#pragma unroll
+            for (int u1 = 0; u1 < 2; u1++)
+#pragma unroll
+              for (int u2 = 0; u2 < 2; u2++) {
+                if ((u1 && vk_(I) == vl_(I)) || (u2 && vk_(p) == vl_(p))) continue;
+                const int s1 = u1 ? vl_(I) : vk_(I), t1 = u1 ? vk_(I) : vl_(I);
+                const int s2 = u2 ? vl_(p) : vk_(p), t2 = u2 ? vk_(p) : vl_(p);
+                const int pa = pidx(s1, s2), pb = pidx(t1, t2);
+                const double v = Bv[sym2(min(pa, pb), max(pa, pb))];
+                acc = first ? v : acc + v;
+                first = false;
+              }
+            k_out[sym2(I, p)] = acc;
+          }
       }
       if (ORDER >= 2) {
         // second divided differences over the 10 distinct triples (smf_kernel.hpp:328-338)
         double D2[3][3][3];
-        double Dm[3][3] = {{D00, D01, D02}, {D01, D11, D12}, {D02, D12, D22}};
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
           for (int j = i; j < 3; j++)
 #pragma unroll
             for (int l = j; l < 3; l++) {
-              double d = smf_dd2<KIND>(lam[i], lam[j], lam[l], fl[i], fl[j], fl[l], Dm[i][j], Dm[i][l],
-                                             Dm[j][l], C);
+              const double d = (i == j && j == l)
+                                   ? smf_dd2_same<KIND>(lam[i], fl[i], Dm[i][i], C)
+                                   : smf_dd2<KIND>(lam[i], lam[j], lam[l], fl[i], fl[j], fl[l], Dm[i][j], Dm[i][l],
+                                                   Dm[j][l], C);
               D2[i][j][l] = D2[i][l][j] = D2[j][i][l] = D2[j][l][i] = D2[l][i][j] = D2[l][j][i] = d;
             }
-        // G'(I, y, z) = sum_ab Et_I,ab S^yz_ab,  S^yz = W + W^T,  W_ab = sum_m D2_amb Et_y,am Et_z,mb
-        double *g_out = sG + tid * 56;
+        // T over all sorted triples of product vectors: M_g[a][m] = sum_b D2_amb P_g[b], W_hg[a] = sum_m M_g[a][m]
+        // P_h[m], T_fhg = sum_a P_f[a] W_hg[a]
+        double Tv[56];
 #pragma unroll
-        for (int y = 0; y < 6; y++) {
-          double Ay[3][3][3];  // D2_amb Et_y,am
+        for (int g = 0; g < 6; g++) {
+          double M[3][3];
 #pragma unroll
           for (int a = 0; a < 3; a++)
 #pragma unroll
-            for (int m = 0; m < 3; m++) {
-              const int am = a == m ? a : a + m + 2;
+            for (int mm = a; mm < 3; mm++)
+              M[a][mm] = M[mm][a] = D2[a][mm][0] * P[g][0] + D2[a][mm][1] * P[g][1] + D2[a][mm][2] * P[g][2];
 #pragma unroll
-              for (int b = 0; b < 3; b++) Ay[a][m][b] = D2[a][m][b] * Et[y][am];
-            }
+          for (int h = 0; h <= g; h++) {
+            double W[3];
 #pragma unroll
-          for (int z = y; z < 6; z++) {
-            double S[6];
+            for (int a = 0; a < 3; a++) W[a] = M[a][0] * P[h][0] + M[a][1] * P[h][1] + M[a][2] * P[h][2];
 #pragma unroll
-            for (int s = 0; s < 6; s++) {
-              const int a = vk_(s), b = vl_(s);
-              double w = 0.0;
-#pragma unroll
-              for (int m = 0; m < 3; m++) {
-                const int mb = m == b ? m : m + b + 2, ma = m == a ? m : m + a + 2;
-                w = fma(Ay[a][m][b], Et[z][mb], w);
-                w = fma(Ay[b][m][a], Et[z][ma], w);
-              }
-              S[s] = w;
-            }
-#pragma unroll
-            for (int I = 0; I <= y; I++) {
-              double acc = Et[I][0] * S[0];
-              acc = fma(Et[I][1], S[1], acc);
-              acc = fma(Et[I][2], S[2], acc);
-              double off = Et[I][3] * S[3];
-              off = fma(Et[I][4], S[4], off);
-              off = fma(Et[I][5], S[5], off);
-              g_out[sym3(I, y, z)] = acc + (off + off);
-            }
+            for (int f = 0; f <= h; f++) Tv[sym3(f, h, g)] = P[f][0] * W[0] + P[f][1] * W[1] + P[f][2] * W[2];
           }
         }
+        // G'(I, y, z) / 2 = sum over the outer-product terms (s1, t1), (s2, t2), (s3, t3) of E_I, E_y, E_z of
+        // T(P[s1 s2], P[t2 s3], P[t1 t3]); the factor 2 goes into the output weight
+        double *g_out = sG + tid * 56;
+#pragma unroll
+        for (int z = 0; z < 6; z++)
+#pragma unroll
+          for (int y = 0; y <= z; y++)
+#pragma unroll
+            for (int I = 0; I <= y; I++) {
+              double acc = 0.0;
+              bool first = true;
+#pragma unroll
+              for (int u1 = 0; u1 < 2; u1++)
+#pragma unroll
+                for (int u2 = 0; u2 < 2; u2++)
+#pragma unroll
+                  for (int u3 = 0; u3 < 2; u3++) {
+                    if ((u1 && vk_(I) == vl_(I)) || (u2 && vk_(y) == vl_(y)) || (u3 && vk_(z) == vl_(z))) continue;
+                    const int s1 = u1 ? vl_(I) : vk_(I), t1 = u1 ? vk_(I) : vl_(I);
+                    const int s2 = u2 ? vl_(y) : vk_(y), t2 = u2 ? vk_(y) : vl_(y);
+                    const int s3 = u3 ? vl_(z) : vk_(z), t3 = u3 ? vk_(z) : vl_(z);
+                    int a1 = pidx(s1, s2), a2 = pidx(t2, s3), a3 = pidx(t1, t3);
+                    sort3(a1, a2, a3);
+                    const double v = Tv[sym3(a1, a2, a3)];
+                    acc = first ? v : acc + v;
+                    first = false;
+                  }
+              g_out[sym3(I, y, z)] = acc;
+            }
       }
     }
   }
@@ -198,10 +239,10 @@ __global__ void __launch_bounds__(SMF_TPB) smf_kernel(int64_t n, const double *_
       if (MAT) {
         const int m = w / 81, c = (w / 9) % 9, e = w % 9;
         I = midx(m); p = midx(c); q = midx(e);
-        ex = (I >= 3 ? -1 : 0) + mwt_log2(c) + mwt_log2(e);
+        ex = 1 + (I >= 3 ? -1 : 0) + mwt_log2(c) + mwt_log2(e);
       } else {
         I = w / 36; p = (w / 6) % 6; q = w % 6;
-        ex = I >= 3 ? -1 : 0;
+        ex = 1 + (I >= 3 ? -1 : 0);
       }
       sort3(I, p, q);
       hidx[k] = sym3(I, p, q);
