@@ -6,7 +6,8 @@ libmatfun_cuda (gmf_cuda_eval).
 
 One JSON line on rank 0.  `value` is whole-job matrices/s with inputs resident in HBM (CUDA events on the launching
 stream; the per-step traffic of 6.9 GB is far above the 126 MB L2, so no flush is needed); `e2e` is the same metric
-through the same C ABI from pinned HOST buffers with the host-device copies inside the timed region.  Multi-GPU
+through the host-buffer C ABI (gmf_cuda_eval_host, the reference's gmf_eval signature on host arrays) from page-locked
+HOST arrays, with all host-device copies inside the timed region (host wall clock around the synchronous call).  Multi-GPU
 (torchrun): every rank evaluates its own n matrices (independent matrices, no collective on the data path).
 --impl reference times the CPU implementation of the same path on the host cores (the reference's compiled library
 where it was built, otherwise the oracle restatement of it), on bounded samples of the same workload.
@@ -27,6 +28,9 @@ sys.path.insert(0, ROOT)
 KINDS = {"exp": 0, "log": 1, "pow": 2, "sqrt": 3}
 BYTES_PER_MATRIX = {0: 72 + 72, 1: 72 + 72 + 648, 2: 72 + 72 + 648 + 5832}  # FP64 in + F (+ J) (+ H)
 METRIC = "gmf log order-2 matrices/s (FP64)"
+# FP64 floating-point operations per matrix executed by gmf_kernel<KIND, 2> on this workload (2 per DFMA), from the
+# ncu counters smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum (profiles/gmf_kernel_log_o2_c1.md)
+FP64_FLOP_PER_MATRIX = {"log": 2 * 3434 + 1789 + 2176}
 
 
 def peaks():
@@ -212,37 +216,34 @@ def run_ours(args, rank, world, local):
     ms = max_over_ranks(ms, world)
     value = world * n / (ms * 1e-3)
 
-    # e2e: the same C ABI call fed from pinned host buffers, copies inside the timed region
+    # e2e: the host-buffer C ABI (gmf_cuda_eval_host: the reference's gmf_eval signature on host arrays; chunks
+    # copied in, evaluated and copied out on two streams) on page-locked host arrays, copies inside the timed region
     hA = torch.from_numpy(X).pin_memory()
     hF = torch.empty((n, 9), dtype=torch.float64).pin_memory()
     hJ = torch.empty((n, 81), dtype=torch.float64).pin_memory()
     hH = torch.empty((n, 729), dtype=torch.float64).pin_memory()
 
     def e2e_step():
-        with torch.cuda.stream(stream):
-            dA.copy_(hA, non_blocking=True)
-            step()
-            hF.copy_(dF, non_blocking=True)
-            hJ.copy_(dJ, non_blocking=True)
-            hH.copy_(dH, non_blocking=True)
+        r = lib.gmf_cuda_eval_host(kind, args.alpha, n, hA.data_ptr(), hF.data_ptr(), hJ.data_ptr(), hH.data_ptr())
+        if r != 0:
+            raise RuntimeError(f"gmf_cuda_eval_host returned {r}")
 
     for _ in range(max(1, args.warmup // 2)):
         e2e_step()
-    stream.synchronize()
     barrier(world)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2e_steps = max(2, args.steps // 2)
-    e0.record(stream)
+    t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        e2e_step()
-    e1.record(stream)
-    e1.synchronize()
-    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, world)
+        e2e_step()  # synchronous: returns when the results are in host memory
+    e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0) / e2e_steps, world)
     e2e_value = world * n / (e2e_ms * 1e-3)
     # result check of the last e2e step against the device result
-    assert torch.equal(hH[:4].to(dev), dH[:4])
+    assert torch.equal(hH[:4].to(dev), dH[:4]) and torch.equal(hF[-4:].to(dev), dF[-4:])
 
     hbm, peak_kind = peaks()
+    import ctypes
+    fp64_peak = ctypes.c_double(0.0)
+    fp64_ok = lib.matfun_cuda_fp64_peak(ctypes.byref(fp64_peak)) == 0
     achieved = BYTES_PER_MATRIX[2] * n / (ms * 1e-3) / 1e9
     out = None
     if rank == 0:
@@ -259,10 +260,15 @@ def run_ours(args, rank, world, local):
                             "traffic": None,
                             "note": "algorithmic bytes (72 in + 6552 out per matrix) / event time; the kernel is "
                                     "bound by the FP64 pipe (see fp64), not by HBM"},
-               "fp64": {"peak_tflops": 1.006, "peak_source": "measured DFMA throughput on this GPU model"},
+               "fp64": {"peak_tflops": fp64_peak.value if fp64_ok else None,
+                        "peak_source": "measured live: 8 independent DFMA chains per thread (matfun_cuda_fp64_peak)",
+                        "achieved_tflops": FP64_FLOP_PER_MATRIX.get(args.kind, 0) * n / (ms * 1e-3) / 1e12 or None,
+                        "flop_per_matrix": FP64_FLOP_PER_MATRIX.get(args.kind),
+                        "flop_source": "ncu dfma x2 + dadd + dmul per matrix, gmf_kernel<LOG,2>, this workload"},
                "e2e": {"value": e2e_value, "unit": "matrices/s", "h2d_bytes_per_step": int(hA.numel() * 8),
                        "d2h_bytes_per_step": int((hF.numel() + hJ.numel() + hH.numel()) * 8),
-                       "ms_per_step": e2e_ms},
+                       "ms_per_step": e2e_ms, "api": "gmf_cuda_eval_host",
+                       "timer": "host wall clock around the synchronous call"},
                "gpu_launches": args.steps,
                "clocks": clk.summary()}
     del dA, dF, dJ, dH

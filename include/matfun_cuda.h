@@ -36,15 +36,29 @@ extern "C" {
 enum smf_kind { SMF_EXP = 0, SMF_LOG = 1, SMF_POW = 2, SMF_SQRT = 3 };
 #endif
 
-/* replaces smf_cuda_eval, cuda/include/matfun/matfun_cuda.h:17 (implementation cuda/src/matfun_cuda.cu:199-202) */
+/* replaces smf_cuda_eval, cuda/include/matfun/matfun_cuda.h:16 (implementation cuda/src/matfun_cuda.cu:199-202) */
 int smf_cuda_eval(int kind, double alpha, int64_t n, const double *v, double *F, double *J, double *H, void *stream);
 
-/* replaces smf_cuda_eval_matrix, cuda/include/matfun/matfun_cuda.h:19-20 (cuda/src/matfun_cuda.cu:204-207) */
+/* replaces smf_cuda_eval_matrix, cuda/include/matfun/matfun_cuda.h:18-19 (cuda/src/matfun_cuda.cu:204-207) */
 int smf_cuda_eval_matrix(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H,
                          void *stream);
 
 /* replaces gmf_cuda_eval, cuda/include/matfun/matfun_cuda.h:22 (cuda/src/matfun_cuda.cu:194-197) */
 int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H, void *stream);
+
+/* Host-buffer forms: the reference's CPU entry points smf_eval, smf_eval_matrix and gmf_eval
+ * (c/include/matfun/matfun.h:28-41; implementation c/src/matfun.cc:87-97) evaluated on the current GPU: HOST arrays
+ * in and out, synchronous, same return codes as the CPU library (0, -1 invalid arguments, -3 when a matrix given to
+ * smf_cuda_eval_matrix_host is not symmetric -- its results are NaN), and -2 for a CUDA error.  The batch is
+ * streamed through the GPU in chunks on two streams, so copies overlap the kernels; page-locked host arrays make the
+ * copies fastest.  libmatfun.so of this package exports the same functions under the reference's names. */
+int smf_cuda_eval_host(int kind, double alpha, int64_t n, const double *v, double *F, double *J, double *H);
+int smf_cuda_eval_matrix_host(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H);
+int gmf_cuda_eval_host(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H);
+
+/* Diagnostic (no counterpart in the reference): the measured FP64 fused-multiply-add throughput of the current GPU
+ * in TFLOP/s, the bound of the FP64 kernels of this library.  Returns 0, or -1 / -2 like the entry points above. */
+int matfun_cuda_fp64_peak(double *tflops);
 
 /* version string of this library (no counterpart in the reference's CUDA header; cf. smf_version, matfun.h:51) */
 const char *matfun_cuda_version(void);

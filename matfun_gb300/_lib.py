@@ -18,6 +18,10 @@ SIGNATURES = {
     "smf_cuda_eval": (ctypes.c_int, _EVAL),
     "smf_cuda_eval_matrix": (ctypes.c_int, _EVAL),
     "gmf_cuda_eval": (ctypes.c_int, _EVAL),
+    "smf_cuda_eval_host": (ctypes.c_int, _EVAL[:-1]),
+    "smf_cuda_eval_matrix_host": (ctypes.c_int, _EVAL[:-1]),
+    "gmf_cuda_eval_host": (ctypes.c_int, _EVAL[:-1]),
+    "matfun_cuda_fp64_peak": (ctypes.c_int, [ctypes.c_void_p]),
     "matfun_cuda_version": (ctypes.c_char_p, []),
 }
 

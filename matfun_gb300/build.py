@@ -83,6 +83,19 @@ def build_cuda(verbose=False, jobs=None):
     return LIB
 
 
+def build_shim():
+    """matfun_gb300/libmatfun.so: the reference's CPU API names (include/matfun.h) forwarding to libmatfun_cuda.so"""
+    src = os.path.join(HERE, "shim", "matfun_shim.c")
+    lib = os.path.join(HERE, "libmatfun.so")
+    if _fresh(lib, max(os.path.getmtime(src), os.path.getmtime(LIB))):
+        return lib
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-o", lib + ".tmp", src, "-L" + HERE, "-l:libmatfun_cuda.so",
+           "-Wl,-rpath,$ORIGIN"]
+    subprocess.run(cmd, check=True)
+    os.replace(lib + ".tmp", lib)
+    return lib
+
+
 def build_oracle():
     """the CPU restatement (oracle/oracle.c) as oracle/liboracle.so: test infrastructure, never the product path"""
     src = os.path.join(ROOT, "oracle", "oracle.c")
@@ -122,4 +135,5 @@ def build_ref_gpu_timer():
 
 if __name__ == "__main__":
     print(build_cuda(verbose=True))
+    print(build_shim())
     print(build_oracle())

@@ -36,7 +36,8 @@ MF_D constexpr int mwt_log2(int m) { return m % 4 == 0 ? 0 : -1; }
 template <int KIND, int ORDER, bool MAT>
 __global__ void __launch_bounds__(SMF_TPB) smf_kernel(int64_t n, const double *__restrict__ x,
                                                       double *__restrict__ F, double *__restrict__ J,
-                                                      double *__restrict__ H, const SmfCoef C) {
+                                                      double *__restrict__ H, const SmfCoef C,
+                                                      int *__restrict__ asym) {
   constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6, NJ = NF * NF, NH = NJ * NF;
   __shared__ double sX[SMF_TPB * NIN];
   __shared__ double sF[SMF_TPB * NF];
@@ -62,6 +63,7 @@ __global__ void __launch_bounds__(SMF_TPB) smf_kernel(int64_t n, const double *_
       v[3] = 0.5 * (xi[1] + xi[3]); v[4] = 0.5 * (xi[2] + xi[6]); v[5] = 0.5 * (xi[5] + xi[7]);
 #pragma unroll
       for (int k = 0; k < 6; k++) v[k] = sel(sym, v[k], __longlong_as_double(0x7FF8000000000000ll));
+      if (!sym && asym) atomicAdd(asym, 1);  // counted for the host entry points (-3), NaN results either way
     } else {
 #pragma unroll
       for (int k = 0; k < 6; k++) v[k] = xi[k];
@@ -260,10 +262,10 @@ __global__ void __launch_bounds__(SMF_TPB) smf_kernel(int64_t n, const double *_
 
 template <int KIND, bool MAT>
 cudaError_t smf_launch_kind(int order, cudaStream_t st, unsigned blocks, int64_t n, const double *x,
-                                   double *F, double *J, double *H, const SmfCoef &C) {
-  if (order == 2) smf_kernel<KIND, 2, MAT><<<blocks, SMF_TPB, 0, st>>>(n, x, F, J, H, C);
-  else if (order == 1) smf_kernel<KIND, 1, MAT><<<blocks, SMF_TPB, 0, st>>>(n, x, F, J, H, C);
-  else smf_kernel<KIND, 0, MAT><<<blocks, SMF_TPB, 0, st>>>(n, x, F, J, H, C);
+                                   double *F, double *J, double *H, const SmfCoef &C, int *asym) {
+  if (order == 2) smf_kernel<KIND, 2, MAT><<<blocks, SMF_TPB, 0, st>>>(n, x, F, J, H, C, asym);
+  else if (order == 1) smf_kernel<KIND, 1, MAT><<<blocks, SMF_TPB, 0, st>>>(n, x, F, J, H, C, asym);
+  else smf_kernel<KIND, 0, MAT><<<blocks, SMF_TPB, 0, st>>>(n, x, F, J, H, C, asym);
   return cudaGetLastError();
 }
 
@@ -291,13 +293,13 @@ inline void smf_coef(int kind, double al, SmfCoef &C) {
 // one kind (instantiated in smf_<kind>.cu so that the kinds compile in parallel)
 template <int KIND>
 cudaError_t smf_launch_t(double al, int64_t n, const double *x, bool mat, double *F, double *J, double *H,
-                         cudaStream_t st) {
+                         cudaStream_t st, int *asym) {
   SmfCoef C;
   smf_coef(KIND, al, C);
   const int order = H ? 2 : (J ? 1 : 0);
   const unsigned blocks = (unsigned)((n + SMF_TPB - 1) / SMF_TPB);
-  return mat ? smf_launch_kind<KIND, true>(order, st, blocks, n, x, F, J, H, C)
-             : smf_launch_kind<KIND, false>(order, st, blocks, n, x, F, J, H, C);
+  return mat ? smf_launch_kind<KIND, true>(order, st, blocks, n, x, F, J, H, C, asym)
+             : smf_launch_kind<KIND, false>(order, st, blocks, n, x, F, J, H, C, nullptr);
 }
 
 }  // namespace mf

@@ -27,10 +27,28 @@ def test_headers_declare_the_reference_entry_points():
     assert {"smf_cuda_eval", "smf_cuda_eval_matrix", "gmf_cuda_eval"} <= names
 
 
+# which in-tree library implements each public header
+HEADER_LIBRARY = {"matfun_cuda.h": "libmatfun_cuda.so", "matfun.h": "libmatfun.so"}
+
+
 def test_library_exports_every_declared_symbol(lib):
+    import ctypes
+
+    from matfun_gb300 import build
+    build.build_shim()
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        so = HEADER_LIBRARY[os.path.basename(h)]
+        handle = ctypes.CDLL(os.path.join(ROOT, "matfun_gb300", so))
         for name in header_functions(h):
-            assert hasattr(lib, name), f"{name} declared in {os.path.basename(h)} but not exported"
+            assert hasattr(handle, name), f"{name} declared in {os.path.basename(h)} but not exported by {so}"
+
+
+def test_host_entry_points_reject_bad_arguments_without_device(lib):
+    """argument errors of the host-buffer forms come back before any CUDA call"""
+    assert lib.gmf_cuda_eval_host(9, 0.0, 10, None, None, None, None) == -1
+    assert lib.smf_cuda_eval_host(2, 0.0, 10, None, None, None, None) == -1
+    assert lib.smf_cuda_eval_matrix_host(0, 0.0, -5, None, None, None, None) == -1
+    assert lib.gmf_cuda_eval_host(0, 0.0, 0, None, None, None, None) == 0
 
 
 def test_version(lib):
