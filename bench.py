@@ -176,6 +176,50 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def mixed_vs_fp64(lib, args, dev, hbm):
+    """smf log order 2 (Voigt) on the C2 workload (n = 2^24 SPD, condition number log-uniform in [1, 1e6], smallest
+    eigenvalue gap log-uniform in [1e-12, 1], stored as FP32): the mixed-precision path (FP32 storage and bulk
+    arithmetic) against the FP64 path on the same values, with the max relative error of the mixed results against
+    the FP64 results on a sample"""
+    import torch
+
+    from matfun_gb300 import workloads as w
+    n = args.mixed_n
+    X32 = w.c2_smf_spd(n, seed=2)
+    d32 = torch.from_numpy(X32).to(dev)
+    d64 = d32.double()
+    outs = {}
+    for tag, dt, x, fn in (("f32", torch.float32, d32, lib.smf_cuda_eval_f32), ("f64", torch.float64, d64, lib.smf_cuda_eval)):
+        F = torch.empty((n, 6), dtype=dt, device=dev)
+        J = torch.empty((n, 36), dtype=dt, device=dev)
+        H = torch.empty((n, 216), dtype=dt, device=dev)
+        call = lambda: fn(1, 0.0, n, x.data_ptr(), F.data_ptr(), J.data_ptr(), H.data_ptr(), None)
+        for _ in range(2):
+            assert call() == 0
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.mixed_steps):
+            call()
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.mixed_steps
+        outs[tag] = (ms, F, J, H)
+    idx = torch.arange(0, n, max(1, n // 65536), device=dev)
+    err = {}
+    for k, name in ((1, "F"), (2, "J"), (3, "H")):
+        a, b = outs["f32"][k][idx].double(), outs["f64"][k][idx]
+        err[name] = float((a - b).abs().max() / b.abs().max())
+    ms32, ms64 = outs["f32"][0], outs["f64"][0]
+    bytes32 = (6 + 6 + 36 + 216) * 4
+    return {"workload": f"smf log order 2, Voigt, n={n} SPD, condition log-uniform [1,1e6], smallest gap "
+                        "log-uniform [1e-12,1], FP32 storage (C2)",
+            "mixed_matrices_per_s": n / (ms32 * 1e-3), "fp64_matrices_per_s": n / (ms64 * 1e-3),
+            "speedup_vs_fp64": ms64 / ms32, "mixed_ms": ms32, "fp64_ms": ms64,
+            "max_rel_err_vs_fp64": err, "err_sample": int(idx.numel()),
+            "mixed_hbm_frac": bytes32 * n / (ms32 * 1e-3) / 1e9 / hbm, "bytes_per_matrix_fp32": bytes32}
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -272,6 +316,8 @@ def run_ours(args, rank, world, local):
                "gpu_launches": args.steps,
                "clocks": clk.summary()}
     del dA, dF, dJ, dH
+    if rank == 0 and not args.no_mixed:
+        out["mixed"] = mixed_vs_fp64(lib, args, dev, hbm)
     if rank == 0 and not args.no_cpu:
         Xs = np.ascontiguousarray(X[np.concatenate([np.arange(g * n // 4, g * n // 4 + args.cpu_sample // 4)
                                                     for g in range(4)])])
@@ -294,6 +340,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1 << 14)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--mixed-n", type=int, default=1 << 24)
+    ap.add_argument("--mixed-steps", type=int, default=5)
     args = ap.parse_args()
     args.alpha = 0.5 if args.kind == "sqrt" else 0.0
     if args.kind == "sqrt":

@@ -46,6 +46,15 @@ int smf_cuda_eval_matrix(int kind, double alpha, int64_t n, const double *A, dou
 /* replaces gmf_cuda_eval, cuda/include/matfun/matfun_cuda.h:22 (cuda/src/matfun_cuda.cu:194-197) */
 int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H, void *stream);
 
+/* Mixed precision (spec extension; no counterpart in the reference): FP32 arrays in and out, the bulk of the
+ * arithmetic in FP32, FP64 kept for the eigensystem and for the eigenvalue differences of the near-coalescent
+ * divided-difference branches.  Same layouts, kinds and return codes as smf_cuda_eval / smf_cuda_eval_matrix.
+ * Max relative error (max-norm per call) against the FP64 results: <= 1e-6 on the tested workloads, stated per kind
+ * and order in the design doc. */
+int smf_cuda_eval_f32(int kind, double alpha, int64_t n, const float *v, float *F, float *J, float *H, void *stream);
+int smf_cuda_eval_matrix_f32(int kind, double alpha, int64_t n, const float *A, float *F, float *J, float *H,
+                             void *stream);
+
 /* Host-buffer forms: the reference's CPU entry points smf_eval, smf_eval_matrix and gmf_eval
  * (c/include/matfun/matfun.h:28-41; implementation c/src/matfun.cc:87-97) evaluated on the current GPU: HOST arrays
  * in and out, synchronous, same return codes as the CPU library (0, -1 invalid arguments, -3 when a matrix given to

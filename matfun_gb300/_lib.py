@@ -18,6 +18,8 @@ SIGNATURES = {
     "smf_cuda_eval": (ctypes.c_int, _EVAL),
     "smf_cuda_eval_matrix": (ctypes.c_int, _EVAL),
     "gmf_cuda_eval": (ctypes.c_int, _EVAL),
+    "smf_cuda_eval_f32": (ctypes.c_int, _EVAL),
+    "smf_cuda_eval_matrix_f32": (ctypes.c_int, _EVAL),
     "smf_cuda_eval_host": (ctypes.c_int, _EVAL[:-1]),
     "smf_cuda_eval_matrix_host": (ctypes.c_int, _EVAL[:-1]),
     "gmf_cuda_eval_host": (ctypes.c_int, _EVAL[:-1]),

@@ -63,4 +63,34 @@ extern "C" int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A,
   return e == cudaSuccess ? 0 : -2;
 }
 
+namespace {
+int smf_call_f32(int kind, double alpha, int64_t n, const float *x, bool mat, float *F, float *J, float *H,
+                 void *stream) {
+  if (kind < SMF_EXP || kind > SMF_SQRT || n < 0 || (H && !J) || (kind == SMF_POW && !(alpha > 0))) return -1;
+  if (n > 0 && (!x || !F)) return -1;
+  if (kind != SMF_POW) alpha = kind == SMF_SQRT ? 0.5 : 0.0;
+  if (n == 0) return 0;
+  if (n > SMF_MAX_N) return -2;
+  const cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  switch (kind) {
+    case SMF_EXP: e = mf::smf_mixed_launch_exp(alpha, n, x, mat, F, J, H, st); break;
+    case SMF_LOG: e = mf::smf_mixed_launch_log(alpha, n, x, mat, F, J, H, st); break;
+    case SMF_SQRT: e = mf::smf_mixed_launch_sqrt(alpha, n, x, mat, F, J, H, st); break;
+    default: e = mf::smf_mixed_launch_pow(alpha, n, x, mat, F, J, H, st); break;
+  }
+  return e == cudaSuccess ? 0 : -2;
+}
+}  // namespace
+
+extern "C" int smf_cuda_eval_f32(int kind, double alpha, int64_t n, const float *v, float *F, float *J, float *H,
+                                 void *stream) {
+  return smf_call_f32(kind, alpha, n, v, false, F, J, H, stream);
+}
+
+extern "C" int smf_cuda_eval_matrix_f32(int kind, double alpha, int64_t n, const float *A, float *F, float *J,
+                                        float *H, void *stream) {
+  return smf_call_f32(kind, alpha, n, A, true, F, J, H, stream);
+}
+
 extern "C" const char *matfun_cuda_version(void) { return "matfun-gb300 0.1.0 (sm_103a)"; }

@@ -20,4 +20,13 @@ MF_GMF_DECL(exp)
 MF_GMF_DECL(log)
 MF_GMF_DECL(pow)
 #undef MF_GMF_DECL
+// mixed precision (FP32 storage, FP32 bulk arithmetic, FP64 eigensystem), symmetric family
+#define MF_SMFX_DECL(k)                                                                                            \
+  cudaError_t smf_mixed_launch_##k(double al, int64_t n, const float *x, bool mat, float *F, float *J, float *H, \
+                                   cudaStream_t st);
+MF_SMFX_DECL(exp)
+MF_SMFX_DECL(log)
+MF_SMFX_DECL(sqrt)
+MF_SMFX_DECL(pow)
+#undef MF_SMFX_DECL
 }  // namespace mf

@@ -36,9 +36,14 @@ MF_D double smf_fun(double x, double al) {
   return KIND == SQRT ? sqrt(x) : pow(x, al);
 }
 
-// eigenvalues lam, f(lam), eigenvectors V (columns) of the symmetric matrix with Voigt vector v
+// eigenvalues lam and eigenvectors V (columns) of the symmetric matrix with Voigt vector v; for log also the
+// deviator's Rayleigh quotients xd[i] = lam[i] / sig - m and m, sig (the log1p form near the mean)
+struct SmfEig {
+  double lam[3], V[3][3], xd[3], m, sig;
+};
+
 template <int KIND>
-MF_D void smf_eigen(const double *v, double al, double lam[3], double fl[3], double V[3][3]) {
+MF_D void smf_eigsys(const double *v, SmfEig &E) {
   constexpr double SQRT6 = 2.449489742783178, TWO_PI_3 = 2.0943951023931957;
   // power-of-two scale sig ~ max|v| (exact; the pairwise select tree keeps the reference's NaN behaviour)
   double s01 = tmax(fabs(v[0]), fabs(v[1])), s23 = tmax(fabs(v[2]), fabs(v[3]));
@@ -108,23 +113,38 @@ MF_D void smf_eigen(const double *v, double al, double lam[3], double fl[3], dou
   double big = sqrt((jrs + fabs(jx)) / (2.0 * jrs)), sml = jy / (2.0 * jrs * big);
   double sgn = sel((jy > 0) | ((jy == 0) & (__double_as_longlong(jy) >= 0)), 1.0, -1.0);
   double cs = sel(jz, 1.0, sel(jpos, big, sgn * sml)), sn = sel(jz, 0.0, sel(jpos, sml, sgn * big));
-  lam[0] = lv * sig;
-  lam[1] = (cs * cs * a11 + 2.0 * cs * sn * a12 + sn * sn * a22) * sig;
-  lam[2] = (sn * sn * a11 - 2.0 * cs * sn * a12 + cs * cs * a22) * sig;
-  V[0][0] = vx; V[0][1] = cs * ux + sn * wx; V[0][2] = cs * wx - sn * ux;
-  V[1][0] = vy; V[1][1] = cs * uy + sn * wy; V[1][2] = cs * wy - sn * uy;
-  V[2][0] = vz; V[2][1] = cs * uz + sn * wz; V[2][2] = cs * wz - sn * uz;
+  E.lam[0] = lv * sig;
+  E.lam[1] = (cs * cs * a11 + 2.0 * cs * sn * a12 + sn * sn * a22) * sig;
+  E.lam[2] = (sn * sn * a11 - 2.0 * cs * sn * a12 + cs * cs * a22) * sig;
+  E.V[0][0] = vx; E.V[0][1] = cs * ux + sn * wx; E.V[0][2] = cs * wx - sn * ux;
+  E.V[1][0] = vy; E.V[1][1] = cs * uy + sn * wy; E.V[1][2] = cs * wy - sn * uy;
+  E.V[2][0] = vz; E.V[2][1] = cs * uz + sn * wz; E.V[2][2] = cs * wz - sn * uz;
+  E.m = m;
+  E.sig = sig;
+  if (KIND == LOG) {
+    E.xd[0] = vx * (d0 * vx + a3 * vy + a4 * vz) + vy * (a3 * vx + d1 * vy + a5 * vz) + vz * (a4 * vx + a5 * vy + d2 * vz);
+    E.xd[1] = cs * cs * b11 + 2.0 * cs * sn * b12 + sn * sn * b22;
+    E.xd[2] = sn * sn * b11 - 2.0 * cs * sn * b12 + cs * cs * b22;
+  }
+}
+
+// eigenvalues lam, f(lam), eigenvectors V (columns) of the symmetric matrix with Voigt vector v (FP64)
+template <int KIND>
+MF_D void smf_eigen(const double *v, double al, double lam[3], double fl[3], double V[3][3]) {
+  SmfEig E;
+  smf_eigsys<KIND>(v, E);
 #pragma unroll
-  for (int i = 0; i < 3; i++) fl[i] = smf_fun<KIND>(lam[i], al);
+  for (int i = 0; i < 3; i++) {
+    lam[i] = E.lam[i];
+#pragma unroll
+    for (int j = 0; j < 3; j++) V[i][j] = E.V[i][j];
+    fl[i] = smf_fun<KIND>(lam[i], al);
+  }
   if (KIND == LOG) {  // near m: log(m sig) + log1p(x / m), x from the deviator
-    double bv = vx * (d0 * vx + a3 * vy + a4 * vz) + vy * (a3 * vx + d1 * vy + a5 * vz) +
-                      vz * (a4 * vx + a5 * vy + d2 * vz);
-    double xd[3] = {bv, cs * cs * b11 + 2.0 * cs * sn * b12 + sn * sn * b22,
-                          sn * sn * b11 - 2.0 * cs * sn * b12 + cs * cs * b22};
-    double lms = log(m * sig);
+    double lms = log(E.m * E.sig);
 #pragma unroll
     for (int i = 0; i < 3; i++)
-      fl[i] = sel(fabs(xd[i]) <= 0.5 * m, lms + log1p(xd[i] / m), fl[i]);
+      fl[i] = sel(fabs(E.xd[i]) <= 0.5 * E.m, lms + log1p(E.xd[i] / E.m), fl[i]);
   }
 }
 

@@ -1,0 +1,9 @@
+// smf_mixed_sqrt.cu -- the sqrt instantiations of the mixed-precision smf kernel (smf_mixed.cuh).
+#include "smf_mixed.cuh"
+
+namespace mf {
+cudaError_t smf_mixed_launch_sqrt(double al, int64_t n, const float *x, bool mat, float *F, float *J, float *H,
+                                cudaStream_t st) {
+  return smf_mixed_launch_t<SQRT>(al, n, x, mat, F, J, H, st);
+}
+}  // namespace mf

@@ -60,3 +60,21 @@ def c1_gmf_groups(n, seed=1):
     src = g3[np.arange(sizes[3]) % sizes[2]]
     g4 = src * (1.0 + 1e-10 * rng.standard_normal((sizes[3], 3, 3)))
     return np.ascontiguousarray(np.concatenate([g1, g2, g3, g4]))
+
+
+def c2_smf_spd(n, seed=2, as_voigt=True, dtype=np.float32):
+    """SPD matrices with condition number log-uniform in [1, 1e6] and smallest eigenvalue gap log-uniform in
+    [1e-12, 1] (relative), Haar eigenvectors, overall scale e^U(-1, 1); stored as `dtype`"""
+    rng = np.random.default_rng(seed)
+    Q = haar(rng, n)
+    kappa = 10.0 ** rng.uniform(0.0, 6.0, n)
+    gap = 10.0 ** rng.uniform(-12.0, 0.0, n)
+    lo, hi = 1.0 / kappa, np.ones(n)
+    near_lo = rng.uniform(size=n) < 0.5
+    mid = np.where(near_lo, lo * (1.0 + gap), hi * (1.0 - gap))
+    mid = np.clip(mid, lo, hi)
+    lam = np.stack([lo, mid, hi], axis=1) * np.exp(rng.uniform(-1.0, 1.0, (n, 1)))
+    A = np.einsum("nij,nj,nkj->nik", Q, lam, Q)
+    A = 0.5 * (A + A.transpose(0, 2, 1))
+    out = voigt(A) if as_voigt else A
+    return np.ascontiguousarray(out.astype(dtype))
