@@ -220,6 +220,70 @@ def mixed_vs_fp64(lib, args, dev, hbm):
             "mixed_hbm_frac": bytes32 * n / (ms32 * 1e-3) / 1e9 / hbm, "bytes_per_matrix_fp32": bytes32}
 
 
+def adjoint_vs_materialised(lib, args, dev):
+    """C4: the gradient of L = sum <W, f(A)> and its Hessian-vector product along V, for smf log (SPD, the C0
+    generator) and gmf pow 0.3 (real and rotation groups of C1), n = 2^22 FP64: the adjoint kernels (no J, H formed)
+    against evaluating J (resp. H) with the eval kernels and contracting it with W (resp. W and V)"""
+    import torch
+
+    from matfun_gb300 import workloads as w
+    n = args.adj_n
+    res = {}
+    for fam, kind, alpha in (("smf", 1, 0.0), ("gmf", 2, 0.3)):
+        if fam == "smf":
+            A = torch.from_numpy(w.c0_smf_spd(n, seed=4, as_voigt=False)).to(dev)
+        else:
+            A = torch.from_numpy(w.c1_gmf_groups(2 * n, seed=4)[: n]).to(dev)
+        g = torch.Generator(device=dev).manual_seed(5)
+        W = torch.randn(A.shape, dtype=torch.float64, device=dev, generator=g)
+        V = torch.randn(A.shape, dtype=torch.float64, device=dev, generator=g)
+        Abar, HWV, JV = torch.empty_like(A), torch.empty_like(A), torch.empty_like(A)
+        fn = lib.smf_cuda_adjoint if fam == "smf" else lib.gmf_cuda_adjoint
+        ev = lib.smf_cuda_eval_matrix if fam == "smf" else lib.gmf_cuda_eval
+        vjp = lambda: fn(kind, alpha, n, A.data_ptr(), W.data_ptr(), None, None, Abar.data_ptr(), None, None, None)
+        hvp = lambda: fn(kind, alpha, n, A.data_ptr(), W.data_ptr(), V.data_ptr(), None, None, JV.data_ptr(),
+                         HWV.data_ptr(), None)
+
+        def timeit(f, reps=3):
+            assert f() in (0, None)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                f()
+            e1.record()
+            e1.synchronize()
+            return e0.elapsed_time(e1) / reps
+
+        t_vjp, t_hvp = timeit(vjp), timeit(hvp)
+        # materialised: J (and H) by the eval kernel in chunks of 2^20, then the contractions
+        ch = 1 << 20
+        Fm = torch.empty((ch, 9), dtype=torch.float64, device=dev)
+        Jm = torch.empty((ch, 81), dtype=torch.float64, device=dev)
+        Hm = torch.empty((ch, 729), dtype=torch.float64, device=dev)
+
+        def mat_vjp():
+            for lo in range(0, n, ch):
+                ev(kind, alpha, ch, A[lo:].data_ptr(), Fm.data_ptr(), Jm.data_ptr(), None, None)
+                torch.einsum("nab,nabcd->ncd", W[lo:lo + ch], Jm.view(ch, 3, 3, 3, 3), out=Abar[lo:lo + ch])
+
+        def mat_hvp():
+            for lo in range(0, n, ch):
+                ev(kind, alpha, ch, A[lo:].data_ptr(), Fm.data_ptr(), Jm.data_ptr(), Hm.data_ptr(), None)
+                HV = torch.einsum("nabcdef,ncd->nabef", Hm.view(ch, 3, 3, 3, 3, 3, 3), V[lo:lo + ch])
+                torch.einsum("nab,nabef->nef", W[lo:lo + ch], HV, out=HWV[lo:lo + ch])
+                torch.einsum("nabcd,ncd->nab", Jm.view(ch, 3, 3, 3, 3), V[lo:lo + ch], out=JV[lo:lo + ch])
+
+        t_mvjp, t_mhvp = timeit(mat_vjp, 1), timeit(mat_hvp, 1)
+        res[f"{fam}_{'log' if kind == 1 else 'pow0.3'}"] = {
+            "n": n, "vjp_matrices_per_s": n / (t_vjp * 1e-3), "hvp_matrices_per_s": n / (t_hvp * 1e-3),
+            "materialised_vjp_matrices_per_s": n / (t_mvjp * 1e-3),
+            "materialised_hvp_matrices_per_s": n / (t_mhvp * 1e-3),
+            "vjp_speedup": t_mvjp / t_vjp, "hvp_speedup": t_mhvp / t_hvp,
+            "bytes_per_matrix": {"vjp": 216, "hvp": 288}}
+    return res
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -318,6 +382,8 @@ def run_ours(args, rank, world, local):
     del dA, dF, dJ, dH
     if rank == 0 and not args.no_mixed:
         out["mixed"] = mixed_vs_fp64(lib, args, dev, hbm)
+    if rank == 0 and not args.no_adjoint:
+        out["adjoint"] = adjoint_vs_materialised(lib, args, dev)
     if rank == 0 and not args.no_cpu:
         Xs = np.ascontiguousarray(X[np.concatenate([np.arange(g * n // 4, g * n // 4 + args.cpu_sample // 4)
                                                     for g in range(4)])])
@@ -341,6 +407,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adj-n", type=int, default=1 << 22)
     ap.add_argument("--mixed-n", type=int, default=1 << 24)
     ap.add_argument("--mixed-steps", type=int, default=5)
     args = ap.parse_args()

@@ -55,6 +55,19 @@ int smf_cuda_eval_f32(int kind, double alpha, int64_t n, const float *v, float *
 int smf_cuda_eval_matrix_f32(int kind, double alpha, int64_t n, const float *A, float *F, float *J, float *H,
                              void *stream);
 
+/* Adjoints (spec extension; no counterpart in the reference): contractions of J and H with directions, without
+ * forming J or H.  Matrix layout (n, 3, 3) for every array; W, V device arrays of directions; outputs, each optional:
+ *   F    = f(A)
+ *   Abar = J^T W    (Abar_cd = sum_ab W_ab dF_ab/dA_cd: the gradient of sum <W, f(A)>)     needs W
+ *   JV   = J V      ((JV)_ab = sum_cd dF_ab/dA_cd V_cd: the derivative of f(A) along V)    needs V
+ *   HWV  = W.H.V    (HWV_ef = sum_abcd W_ab d2F_ab/dA_cd dA_ef V_cd)                       needs W and V
+ * smf_cuda_adjoint treats A as symmetric (the derivatives of A -> f((A + A^T)/2), as smf_cuda_eval_matrix).
+ * Returns 0, -1 (invalid kind / alpha, n < 0, an output without its directions), -2 (CUDA error). */
+int smf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const double *W, const double *V, double *F,
+                     double *Abar, double *JV, double *HWV, void *stream);
+int gmf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const double *W, const double *V, double *F,
+                     double *Abar, double *JV, double *HWV, void *stream);
+
 /* Host-buffer forms: the reference's CPU entry points smf_eval, smf_eval_matrix and gmf_eval
  * (c/include/matfun/matfun.h:28-41; implementation c/src/matfun.cc:87-97) evaluated on the current GPU: HOST arrays
  * in and out, synchronous, same return codes as the CPU library (0, -1 invalid arguments, -3 when a matrix given to

@@ -1,0 +1,398 @@
+// adjoint.cuh -- adjoint kernels: contractions of J and H with given directions, without forming J or H.
+//   VJP  Abar = J^T W     (Abar_cd = sum_ab W_ab J_abcd)           the gradient of <W, f(A)>
+//   JVP  JV   = J V       ((JV)_ab = sum_cd J_abcd V_cd)            the derivative of f(A) along V
+//   HVP  HWV  = W . H . V (HWV_ef = sum_abcd W_ab H_abcdef V_cd)   the derivative of the gradient along V
+// (matrix layout, 3x3 row-major arrays, one matrix after another).
+//
+// General matrices, from the record of gmf_device.cuh (real basis r_0 = I, r_1, r_2; reduced D2', D3'):
+//   Abar = sc1 sum_mn D2'_mn r_m^T W r_n^T,   JV = sc1 sum_mn D2'_mn r_m V r_n,
+//   HWV  = sc2 sum_p (X_p^T W r_p^T + r_p^T W X_p^T),   X_p = sum_mn D3'_mnp r_m V r_n
+// (the transposes of J_abcd = sc1 sum D2'_mn r_m[ac] r_n[db] and H_abcdef = sc2 (T6[ac,de,fb] + T6[ae,fc,db])).
+// Symmetric matrices (derivatives of A -> f((A + A^T)/2)), with U the eigenvectors, D, D2 the divided differences,
+// Wt = U^T sym(W) U, Vt = U^T sym(V) U:
+//   Abar = U (D o Wt) U^T,   JV = U (D o Vt) U^T,   HWV = U (Q + Q^T) U^T,  Q_xy = sum_z D2_xyz Wt_xz Vt_yz
+// (Daleckii-Krein and its second-order form; the first-order map is self-adjoint on symmetric directions).
+#pragma once
+#include "gmf_kernels.cuh"
+#include "smf_kernels.cuh"
+
+namespace mf {
+
+MF_D void mm3(const double *X, const double *Y, double *Z) {  // Z = X Y
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) Z[3 * i + j] = X[3 * i] * Y[j] + X[3 * i + 1] * Y[3 + j] + X[3 * i + 2] * Y[6 + j];
+}
+MF_D void mmT3(const double *X, const double *Y, double *Z) {  // Z = X Y^T
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      Z[3 * i + j] = X[3 * i] * Y[3 * j] + X[3 * i + 1] * Y[3 * j + 1] + X[3 * i + 2] * Y[3 * j + 2];
+}
+MF_D void mTm3(const double *X, const double *Y, double *Z) {  // Z = X^T Y
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) Z[3 * i + j] = X[i] * Y[j] + X[3 + i] * Y[3 + j] + X[6 + i] * Y[6 + j];
+}
+
+// the output factor of a record, applied last as in the reference (NaN for a matrix outside the domain)
+MF_D double scale_out(double v, double sc) { return v * sc; }
+
+enum { ADJ_F = 1, ADJ_VJP = 2, ADJ_JVP = 4, ADJ_HVP = 8 };
+
+// ------------------------------------------------------------------------------------------------ general
+constexpr int GADJ_TPB = 128;
+
+struct GadjSmem {
+  double x[GADJ_TPB * 9], w[GADJ_TPB * 9], v[GADJ_TPB * 9];
+  double out[4][GADJ_TPB * 9];  // F, Abar, JV, HWV staging
+  GmfState state[GADJ_TPB];
+  unsigned key[GADJ_TPB];
+  int perm[GADJ_TPB];
+};
+
+template <int KIND, int ORDER>
+__global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const double *__restrict__ A,
+                                                               const double *__restrict__ W,
+                                                               const double *__restrict__ V, double *__restrict__ F,
+                                                               double *__restrict__ Abar, double *__restrict__ JV,
+                                                               double *__restrict__ HWV, const GmfCoef C) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  GadjSmem &S = *reinterpret_cast<GadjSmem *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * GADJ_TPB;
+  const int cnt = (int)min((int64_t)GADJ_TPB, n - base);
+  for (int e = tid; e < cnt * 9; e += GADJ_TPB) {
+    S.x[e] = A[base * 9 + e];
+    if (W) S.w[e] = W[base * 9 + e];
+    if (V) S.v[e] = V[base * 9 + e];
+  }
+  __syncthreads();
+  unsigned key = 0xFFFFFFFFu;
+  if (tid < cnt) {
+    double a[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) a[k] = S.x[tid * 9 + k];
+    GmfState St;
+    gmf_classify<KIND, ORDER>(a, C, St);
+    S.state[tid] = St;
+    const unsigned cls = St.K == 0 ? 0u : ((St.flags & 1024) ? 1u : 2u);
+    key = (cls << 16) | ((unsigned)(255 - St.K) << 6) | (unsigned)((St.flags >> 3) & 63);
+  }
+  S.key[tid] = key;
+  __syncthreads();
+  {
+    int rank = 0;
+    for (int j = 0; j < GADJ_TPB; j++) {
+      const unsigned kj = S.key[j];
+      rank += (kj < key) | ((kj == key) & (j < tid));
+    }
+    S.perm[rank] = tid;
+  }
+  __syncthreads();
+  const int mine = S.perm[tid];
+  if (mine < cnt) {
+    GmfRec R;
+    gmf_finish<KIND, ORDER>(S.state[mine], C, R);
+    double r[3][9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      r[0][k] = k % 4 == 0 ? 1.0 : 0.0;
+      r[1][k] = R.r1[k];
+      r[2][k] = R.r2[k];
+    }
+    const double D2m[3][3] = {{R.D2[0], R.D2[3], R.D2[4]}, {R.D2[3], R.D2[1], R.D2[5]}, {R.D2[4], R.D2[5], R.D2[2]}};
+    if (F) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) S.out[0][mine * 9 + k] = R.F[k];
+    }
+    const double *w = S.w + mine * 9, *v = S.v + mine * 9;
+    double Wl[9], Vl[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) { Wl[k] = W ? w[k] : 0.0; Vl[k] = V ? v[k] : 0.0; }
+    double Gw[3][9];  // W r_n^T
+    if (Abar || HWV) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) Gw[0][k] = Wl[k];
+      mmT3(Wl, r[1], Gw[1]);
+      mmT3(Wl, r[2], Gw[2]);
+    }
+    if (Abar) {  // sc1 sum_m r_m^T (sum_n D2'_mn W r_n^T)
+      double acc[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) acc[k] = 0.0;
+#pragma unroll
+      for (int mm = 0; mm < 3; mm++) {
+        double Hm[9], T[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gw[0][k] + D2m[mm][1] * Gw[1][k] + D2m[mm][2] * Gw[2][k];
+        if (mm == 0) {
+#pragma unroll
+          for (int k = 0; k < 9; k++) acc[k] += Hm[k];
+        } else {
+          mTm3(r[mm], Hm, T);
+#pragma unroll
+          for (int k = 0; k < 9; k++) acc[k] += T[k];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 9; k++) S.out[1][mine * 9 + k] = scale_out(acc[k], R.sc1);
+    }
+    double Gv[3][9];  // V r_n
+    if (JV || HWV) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) Gv[0][k] = Vl[k];
+      mm3(Vl, r[1], Gv[1]);
+      mm3(Vl, r[2], Gv[2]);
+    }
+    if (JV) {  // sc1 sum_m r_m (sum_n D2'_mn V r_n)
+      double acc[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) acc[k] = 0.0;
+#pragma unroll
+      for (int mm = 0; mm < 3; mm++) {
+        double Hm[9], T[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gv[0][k] + D2m[mm][1] * Gv[1][k] + D2m[mm][2] * Gv[2][k];
+        if (mm == 0) {
+#pragma unroll
+          for (int k = 0; k < 9; k++) acc[k] += Hm[k];
+        } else {
+          mm3(r[mm], Hm, T);
+#pragma unroll
+          for (int k = 0; k < 9; k++) acc[k] += T[k];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 9; k++) S.out[2][mine * 9 + k] = scale_out(acc[k], R.sc1);
+    }
+    if (ORDER >= 2 && HWV) {
+      // M_mn = r_m V r_n ; X_p = sum_mn D3'_mnp M_mn ; HWV = sc2 sum_p (X_p^T W r_p^T + r_p^T W X_p^T)
+      double X[3][9];
+#pragma unroll
+      for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int k = 0; k < 9; k++) X[p][k] = 0.0;
+#pragma unroll
+      for (int mm = 0; mm < 3; mm++)
+#pragma unroll
+        for (int nn = 0; nn < 3; nn++) {
+          double M[9];
+          if (mm == 0) {
+#pragma unroll
+            for (int k = 0; k < 9; k++) M[k] = Gv[nn][k];
+          } else {
+            mm3(r[mm], Gv[nn], M);
+          }
+#pragma unroll
+          for (int p = 0; p < 3; p++) {
+            int i0 = mm, i1 = nn, i2 = p;
+            sort3(i0, i1, i2);
+            const double d = R.D3[sym3(i0, i1, i2)];
+#pragma unroll
+            for (int k = 0; k < 9; k++) X[p][k] += d * M[k];
+          }
+        }
+      double acc[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) acc[k] = 0.0;
+#pragma unroll
+      for (int p = 0; p < 3; p++) {
+        double T1[9], T2[9], T3[9];
+        mTm3(X[p], Gw[p], T1);  // X_p^T (W r_p^T)
+        mmT3(Wl, X[p], T2);     // W X_p^T
+        if (p == 0) {
+#pragma unroll
+          for (int k = 0; k < 9; k++) T3[k] = T2[k];
+        } else {
+          mTm3(r[p], T2, T3);   // r_p^T W X_p^T
+        }
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[k] += T1[k] + T3[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 9; k++) S.out[3][mine * 9 + k] = scale_out(acc[k], R.sc2);
+    }
+  }
+  __syncthreads();
+  double *dst[4] = {F, Abar, JV, HWV};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (!dst[q]) continue;
+    for (int e = tid; e < cnt * 9; e += GADJ_TPB) dst[q][base * 9 + e] = S.out[q][e];
+  }
+}
+
+// ------------------------------------------------------------------------------------------------ symmetric
+constexpr int SADJ_TPB = 64;
+
+template <int KIND, int ORDER>
+__global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel(int64_t n, const double *__restrict__ A,
+                                                               const double *__restrict__ W,
+                                                               const double *__restrict__ V, double *__restrict__ F,
+                                                               double *__restrict__ Abar, double *__restrict__ JV,
+                                                               double *__restrict__ HWV, const SmfCoef C) {
+  __shared__ double sx[SADJ_TPB * 9], sw[SADJ_TPB * 9], sv[SADJ_TPB * 9], so[4][SADJ_TPB * 9];
+  const int tid = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * SADJ_TPB;
+  const int cnt = (int)min((int64_t)SADJ_TPB, n - base);
+  for (int e = tid; e < cnt * 9; e += SADJ_TPB) {
+    sx[e] = A[base * 9 + e];
+    if (W) sw[e] = W[base * 9 + e];
+    if (V) sv[e] = V[base * 9 + e];
+  }
+  __syncthreads();
+  if (tid < cnt) {
+    const double *xi = sx + tid * 9;
+    double v6[6];  // symmetric part (NaN if not symmetric, smf_kernel.hpp:408-421)
+    {
+      double mx = 0.0;
+#pragma unroll
+      for (int k = 0; k < 9; k++) mx = sel(fabs(xi[k]) > mx, fabs(xi[k]), mx);
+      const double tol = 1e-8 * mx;
+      bool sym = !(fabs(xi[1] - xi[3]) > tol) & !(fabs(xi[2] - xi[6]) > tol) & !(fabs(xi[5] - xi[7]) > tol);
+      v6[0] = xi[0]; v6[1] = xi[4]; v6[2] = xi[8];
+      v6[3] = 0.5 * (xi[1] + xi[3]); v6[4] = 0.5 * (xi[2] + xi[6]); v6[5] = 0.5 * (xi[5] + xi[7]);
+#pragma unroll
+      for (int k = 0; k < 6; k++) v6[k] = sel(sym, v6[k], __longlong_as_double(0x7FF8000000000000ll));
+    }
+    double lam[3], fl[3], U[3][3];
+    smf_eigen<KIND>(v6, C.al, lam, fl, U);
+    if (F) {
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+          so[0][tid * 9 + 3 * a + b] = U[a][0] * fl[0] * U[b][0] + U[a][1] * fl[1] * U[b][1] + U[a][2] * fl[2] * U[b][2];
+    }
+    if (Abar || JV || HWV) {
+      const double D01 = smf_dd1<KIND>(lam[0], lam[1], fl[0], fl[1], C);
+      const double D02 = smf_dd1<KIND>(lam[0], lam[2], fl[0], fl[2], C);
+      const double D12 = smf_dd1<KIND>(lam[1], lam[2], fl[1], fl[2], C);
+      const double Dm[3][3] = {{smf_deriv<KIND>(lam[0], fl[0], C), D01, D02},
+                               {D01, smf_deriv<KIND>(lam[1], fl[1], C), D12},
+                               {D02, D12, smf_deriv<KIND>(lam[2], fl[2], C)}};
+      // Xt = U^T sym(X) U for X = W, V
+      double Wt[3][3], Vt[3][3];
+      auto rotate = [&](const double *Xg, double Xt[3][3]) {
+        double Xs[3][3], T[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) Xs[i][j] = 0.5 * (Xg[3 * i + j] + Xg[3 * j + i]);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) T[i][b] = Xs[i][0] * U[0][b] + Xs[i][1] * U[1][b] + Xs[i][2] * U[2][b];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) Xt[a][b] = U[0][a] * T[0][b] + U[1][a] * T[1][b] + U[2][a] * T[2][b];
+      };
+      auto back = [&](double Y[3][3], double *out) {  // out = U Y U^T
+        double T[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) T[i][b] = U[i][0] * Y[0][b] + U[i][1] * Y[1][b] + U[i][2] * Y[2][b];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) out[3 * i + j] = T[i][0] * U[j][0] + T[i][1] * U[j][1] + T[i][2] * U[j][2];
+      };
+      if (Abar || HWV) rotate(sw + tid * 9, Wt);
+      if (JV || HWV) rotate(sv + tid * 9, Vt);
+      if (Abar) {
+        double Y[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) Y[a][b] = Dm[a][b] * Wt[a][b];
+        back(Y, so[1] + tid * 9);
+      }
+      if (JV) {
+        double Y[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) Y[a][b] = Dm[a][b] * Vt[a][b];
+        back(Y, so[2] + tid * 9);
+      }
+      if (ORDER >= 2 && HWV) {
+        double D2[3][3][3];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = i; j < 3; j++)
+#pragma unroll
+            for (int l = j; l < 3; l++) {
+              const double d = (i == j && j == l) ? smf_dd2_same<KIND>(lam[i], fl[i], Dm[i][i], C)
+                                                  : smf_dd2<KIND>(lam[i], lam[j], lam[l], fl[i], fl[j], fl[l],
+                                                                  Dm[i][j], Dm[i][l], Dm[j][l], C);
+              D2[i][j][l] = D2[i][l][j] = D2[j][i][l] = D2[j][l][i] = D2[l][i][j] = D2[l][j][i] = d;
+            }
+        double Q[3][3], Y[3][3];
+#pragma unroll
+        for (int x = 0; x < 3; x++)
+#pragma unroll
+          for (int y = 0; y < 3; y++)
+            Q[x][y] = D2[x][y][0] * Wt[x][0] * Vt[y][0] + D2[x][y][1] * Wt[x][1] * Vt[y][1] +
+                      D2[x][y][2] * Wt[x][2] * Vt[y][2];
+#pragma unroll
+        for (int x = 0; x < 3; x++)
+#pragma unroll
+          for (int y = 0; y < 3; y++) Y[x][y] = Q[x][y] + Q[y][x];
+        back(Y, so[3] + tid * 9);
+      }
+    }
+  }
+  __syncthreads();
+  double *dst[4] = {F, Abar, JV, HWV};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (!dst[q]) continue;
+    for (int e = tid; e < cnt * 9; e += SADJ_TPB) dst[q][base * 9 + e] = so[q][e];
+  }
+}
+
+// ------------------------------------------------------------------------------------------------ launchers
+template <int KIND, int ORDER>
+cudaError_t gmf_adjoint_one(unsigned blocks, int64_t n, const double *A, const double *W, const double *V, double *F,
+                            double *Abar, double *JV, double *HWV, const GmfCoef &C, cudaStream_t st) {
+  static bool attr = false;  // per instantiation (idempotent)
+  if (!attr) {
+    const cudaError_t e = cudaFuncSetAttribute(gmf_adjoint_kernel<KIND, ORDER>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GadjSmem));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  gmf_adjoint_kernel<KIND, ORDER><<<blocks, GADJ_TPB, sizeof(GadjSmem), st>>>(n, A, W, V, F, Abar, JV, HWV, C);
+  return cudaGetLastError();
+}
+
+template <int KIND>
+cudaError_t gmf_adjoint_t(double al, int64_t n, const double *A, const double *W, const double *V, double *F,
+                          double *Abar, double *JV, double *HWV, cudaStream_t st) {
+  const int order = HWV ? 2 : 1;
+  GmfCoef C;
+  gmf_coef(KIND, al, order, C);
+  const unsigned blocks = (unsigned)((n + GADJ_TPB - 1) / GADJ_TPB);
+  return order == 2 ? gmf_adjoint_one<KIND, 2>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st)
+                    : gmf_adjoint_one<KIND, 1>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st);
+}
+
+template <int KIND>
+cudaError_t smf_adjoint_t(double al, int64_t n, const double *A, const double *W, const double *V, double *F,
+                          double *Abar, double *JV, double *HWV, cudaStream_t st) {
+  SmfCoef C;
+  smf_coef(KIND, al, C);
+  const unsigned blocks = (unsigned)((n + SADJ_TPB - 1) / SADJ_TPB);
+  if (HWV) smf_adjoint_kernel<KIND, 2><<<blocks, SADJ_TPB, 0, st>>>(n, A, W, V, F, Abar, JV, HWV, C);
+  else smf_adjoint_kernel<KIND, 1><<<blocks, SADJ_TPB, 0, st>>>(n, A, W, V, F, Abar, JV, HWV, C);
+  return cudaGetLastError();
+}
+
+}  // namespace mf

@@ -1,0 +1,14 @@
+// adjoint_smf.cu -- instantiations of the symmetric-family adjoint kernels (adjoint.cuh).
+#include "adjoint.cuh"
+
+namespace mf {
+cudaError_t smf_adjoint_launch(int kind, double al, int64_t n, const double *A, const double *W, const double *V,
+                               double *F, double *Abar, double *JV, double *HWV, cudaStream_t st) {
+  switch (kind) {
+    case EXP: return smf_adjoint_t<EXP>(al, n, A, W, V, F, Abar, JV, HWV, st);
+    case LOG: return smf_adjoint_t<LOG>(al, n, A, W, V, F, Abar, JV, HWV, st);
+    case SQRT: return smf_adjoint_t<SQRT>(al, n, A, W, V, F, Abar, JV, HWV, st);
+    default: return smf_adjoint_t<POW>(al, n, A, W, V, F, Abar, JV, HWV, st);
+  }
+}
+}  // namespace mf

@@ -93,4 +93,30 @@ extern "C" int smf_cuda_eval_matrix_f32(int kind, double alpha, int64_t n, const
   return smf_call_f32(kind, alpha, n, A, true, F, J, H, stream);
 }
 
+namespace {
+int adjoint_call(bool general, int kind, double alpha, int64_t n, const double *A, const double *W, const double *V,
+                 double *F, double *Abar, double *JV, double *HWV, void *stream) {
+  if (kind < SMF_EXP || kind > SMF_SQRT || n < 0 || (kind == SMF_POW && !(alpha > 0))) return -1;
+  if ((Abar && !W) || (JV && !V) || (HWV && !(W && V))) return -1;
+  if (n > 0 && !A) return -1;
+  if (general && kind == SMF_SQRT) kind = SMF_POW, alpha = 0.5;
+  if (kind != SMF_POW) alpha = kind == SMF_SQRT ? 0.5 : 0.0;
+  if (n == 0 || !(F || Abar || JV || HWV)) return 0;
+  if (n > SMF_MAX_N) return -2;
+  const cudaError_t e = general ? mf::gmf_adjoint_launch(kind, alpha, n, A, W, V, F, Abar, JV, HWV, (cudaStream_t)stream)
+                                : mf::smf_adjoint_launch(kind, alpha, n, A, W, V, F, Abar, JV, HWV, (cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : -2;
+}
+}  // namespace
+
+extern "C" int gmf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const double *W, const double *V,
+                                double *F, double *Abar, double *JV, double *HWV, void *stream) {
+  return adjoint_call(true, kind, alpha, n, A, W, V, F, Abar, JV, HWV, stream);
+}
+
+extern "C" int smf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const double *W, const double *V,
+                                double *F, double *Abar, double *JV, double *HWV, void *stream) {
+  return adjoint_call(false, kind, alpha, n, A, W, V, F, Abar, JV, HWV, stream);
+}
+
 extern "C" const char *matfun_cuda_version(void) { return "matfun-gb300 0.1.0 (sm_103a)"; }

@@ -29,4 +29,9 @@ MF_SMFX_DECL(log)
 MF_SMFX_DECL(sqrt)
 MF_SMFX_DECL(pow)
 #undef MF_SMFX_DECL
+// adjoints (matrix layout): any of F, Abar = J^T W, JV = J V, HWV = W . H . V; kind normalised as above
+cudaError_t gmf_adjoint_launch(int kind, double al, int64_t n, const double *A, const double *W, const double *V,
+                               double *F, double *Abar, double *JV, double *HWV, cudaStream_t st);
+cudaError_t smf_adjoint_launch(int kind, double al, int64_t n, const double *A, const double *W, const double *V,
+                               double *F, double *Abar, double *JV, double *HWV, cudaStream_t st);
 }  // namespace mf
