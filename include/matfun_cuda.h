@@ -68,6 +68,33 @@ int smf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const d
 int gmf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const double *W, const double *V, double *F,
                      double *Abar, double *JV, double *HWV, void *stream);
 
+/* Batched evaluation (spec extension; no counterpart in the reference): many requests of uneven size and
+ * mixed family / kind / order / precision in ONE launch of a persistent kernel.  A request: */
+typedef struct mf_request {
+  int32_t family;  /* 0: smf Voigt (smf_cuda_eval), 1: smf matrix (smf_cuda_eval_matrix), 2: gmf (gmf_cuda_eval) */
+  int32_t kind;    /* SMF_EXP, SMF_LOG, SMF_POW, SMF_SQRT */
+  int32_t order;   /* 0: F; 1: F, J; 2: F, J, H */
+  int32_t dtype;   /* 0: FP64 arrays; 1: FP32 arrays (the mixed-precision path, smf only) */
+  double alpha;    /* exponent of SMF_POW */
+  int64_t n;       /* matrices */
+  const void *x;   /* device input, layouts as above */
+  void *F, *J, *H; /* device outputs (J for order >= 1, H for order 2) */
+} mf_request;
+
+/* All requests queued on `stream` as one launch (the request table is uploaded on `stream` first).  Returns 0, -1 when
+ * a request breaks the rules of its single entry point (then nothing runs), -2 for a CUDA error.  Results equal those
+ * of the single entry points. */
+int matfun_cuda_batched(const mf_request *requests, int count, void *stream);
+/* The same as a plan: the table is validated and uploaded once (synchronously); matfun_cuda_batched_run then only
+ * clears the tile cursor and launches, so it can be captured in a CUDA graph and replayed.  The arrays the requests
+ * name must stay allocated while the plan is used. */
+int matfun_cuda_batched_plan(const mf_request *requests, int count, void **plan);
+int matfun_cuda_batched_run(void *plan, void *stream);
+int matfun_cuda_batched_free(void *plan);
+/* Tuning of the persistent launch (set by the autotuner, matfun_gb300/autotune.py): CTAs per SM (1..8) and whether
+ * requests are laid out longest first (1) or as given (0).  Returns 0 or -1. */
+int matfun_cuda_batched_tune(int ctas_per_sm, int longest_first);
+
 /* Host-buffer forms: the reference's CPU entry points smf_eval, smf_eval_matrix and gmf_eval
  * (c/include/matfun/matfun.h:28-41; implementation c/src/matfun.cc:87-97) evaluated on the current GPU: HOST arrays
  * in and out, synchronous, same return codes as the CPU library (0, -1 invalid arguments, -3 when a matrix given to

@@ -12,6 +12,13 @@ _lib = None
 
 KINDS = {"exp": 0, "log": 1, "pow": 2, "sqrt": 3}
 
+class Request(ctypes.Structure):
+    """mf_request of include/matfun_cuda.h"""
+    _fields_ = [("family", ctypes.c_int32), ("kind", ctypes.c_int32), ("order", ctypes.c_int32),
+                ("dtype", ctypes.c_int32), ("alpha", ctypes.c_double), ("n", ctypes.c_int64),
+                ("x", ctypes.c_void_p), ("F", ctypes.c_void_p), ("J", ctypes.c_void_p), ("H", ctypes.c_void_p)]
+
+
 # exported symbol -> (restype, argtypes)
 _EVAL = [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [ctypes.c_void_p] * 5
 SIGNATURES = {
@@ -26,6 +33,11 @@ SIGNATURES = {
     "smf_cuda_eval_matrix_host": (ctypes.c_int, _EVAL[:-1]),
     "gmf_cuda_eval_host": (ctypes.c_int, _EVAL[:-1]),
     "matfun_cuda_fp64_peak": (ctypes.c_int, [ctypes.c_void_p]),
+    "matfun_cuda_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "matfun_cuda_batched_plan": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "matfun_cuda_batched_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "matfun_cuda_batched_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "matfun_cuda_batched_tune": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "matfun_cuda_version": (ctypes.c_char_p, []),
 }
 

@@ -51,11 +51,16 @@ def _newest_header():
     return max((os.path.getmtime(h) for h in hs), default=0.0)
 
 
+def _rdc(src):
+    """the batched kernel and its tile routines: relocatable device code, device-linked together"""
+    return os.path.basename(src).startswith("batched")
+
+
 def _compile(src, hdr_time, verbose):
     obj = os.path.join(OBJ, os.path.basename(src)[:-3] + ".o")
     if _fresh(obj, max(os.path.getmtime(src), hdr_time)):
         return obj, ""
-    cmd = [_nvcc()] + NVFLAGS + ["-c", src, "-o", obj]
+    cmd = [_nvcc()] + NVFLAGS + (["-rdc=true"] if _rdc(src) else []) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -73,6 +78,15 @@ def build_cuda(verbose=False, jobs=None):
     for _, log in res:
         if log:
             print(log)
+    rdc = [o for s, o in zip(srcs, objs) if _rdc(s)]
+    if rdc:
+        dl = os.path.join(OBJ, "device_link.o")
+        if not _fresh(dl, max(os.path.getmtime(o) for o in rdc)):
+            r = subprocess.run([_nvcc()] + ARCH + ["-Xcompiler", "-fPIC", "-dlink", "-o", dl] + rdc,
+                               capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"device link failed:\n{r.stdout}\n{r.stderr}")
+        objs = objs + [dl]
     if not _fresh(LIB, max(os.path.getmtime(o) for o in objs)):
         tmp = LIB + ".tmp"
         cmd = [_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs

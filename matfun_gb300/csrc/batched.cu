@@ -1,0 +1,300 @@
+// batched.cu -- many requests of uneven size and mixed family / kind / order / precision in one launch.
+//
+// The host cuts every request into tiles of 128 matrices and writes a table (requests, their coefficient blocks,
+// the prefix sum of their tile counts) into device memory.  One persistent kernel (grid = SMs x CTAs per SM) then
+// pulls tiles from a global atomic cursor until all are taken; each tile runs the same tile routine as the
+// standalone kernel of its request (smf FP64 / mixed FP32 in either layout, gmf FP64).  There is no waiting between
+// CTAs: a CTA only increments the cursor and stops when it passes the tile count, so no wait can hang.
+//
+// Two ways to run it:
+//   matfun_cuda_batched(requests, count, stream)          table in a per-device cached buffer, uploaded on `stream`
+//   matfun_cuda_batched_plan / _run / _free                 table uploaded once; _run only clears the cursor and
+//                                                           launches, so it can be captured in a CUDA graph
+// The CTAs per SM and the order in which requests are laid out (as given, or longest tile work first) come from
+// matfun_cuda_batched_tune (set by the autotuner of matfun_gb300/autotune.py).
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/matfun_cuda.h"
+#include "batched_tiles.cuh"
+
+namespace mf {
+namespace {
+
+// dispatch of a tile to its variant
+#define MF_SMF_CALL(pfx, K, suf)                                                        \
+  switch (R.order) {                                                                    \
+    case 2: pfx##_##K##_2_##suf(base, cnt, R, coef, smem); break;                        \
+    case 1: pfx##_##K##_1_##suf(base, cnt, R, coef, smem); break;                        \
+    default: pfx##_##K##_0_##suf(base, cnt, R, coef, smem); break;                       \
+  }
+#define MF_SMF_KIND(pfx, suf)                                                           \
+  switch (R.kind) {                                                                     \
+    case 0: MF_SMF_CALL(pfx, 0, suf) break;                                              \
+    case 1: MF_SMF_CALL(pfx, 1, suf) break;                                              \
+    case 3: MF_SMF_CALL(pfx, 3, suf) break;                                              \
+    default: MF_SMF_CALL(pfx, 2, suf) break;                                             \
+  }
+#define MF_GMF_CALL(K)                                                                  \
+  switch (R.order) {                                                                    \
+    case 2: bt_gmf_##K##_2(base, cnt, R, coef, smem); break;                             \
+    case 1: bt_gmf_##K##_1(base, cnt, R, coef, smem); break;                             \
+    default: bt_gmf_##K##_0(base, cnt, R, coef, smem); break;                            \
+  }
+
+__device__ void run_tile(const DevReq &R, long long base, int cnt, const unsigned char *coef, unsigned char *smem) {
+  if (R.family == 2) {
+    switch (R.kind) {
+      case 0: MF_GMF_CALL(0) break;
+      case 1: MF_GMF_CALL(1) break;
+      default: MF_GMF_CALL(2) break;
+    }
+  } else if (R.family == 1) {
+    if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, m) } else { MF_SMF_KIND(bt_smf32, m) }
+  } else {
+    if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, v) } else { MF_SMF_KIND(bt_smf32, v) }
+  }
+}
+
+__global__ void __launch_bounds__(BT_TPB) batched_kernel(const DevReq *__restrict__ reqs, int nreq,
+                                                         const long long *__restrict__ tile_start,
+                                                         unsigned long long *__restrict__ cursor,
+                                                         const unsigned char *__restrict__ coefs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ long long s_tile;
+  const long long total = tile_start[nreq];
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (long long)atomicAdd(cursor, 1ull);
+    __syncthreads();
+    const long long t = s_tile;
+    __syncthreads();
+    if (t >= total) break;
+    int lo = 0, hi = nreq;  // request of tile t: tile_start[lo] <= t < tile_start[lo + 1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (tile_start[mid] <= t) lo = mid;
+      else hi = mid;
+    }
+    const DevReq R = reqs[lo];
+    const long long base = (t - tile_start[lo]) * BT_TPB;
+    const int cnt = (int)min((long long)BT_TPB, R.n - base);
+    run_tile(R, base, cnt, coefs + R.coef_off, smem);
+    __syncthreads();  // the tile's shared memory is reused by the next tile
+  }
+}
+
+constexpr size_t smem_bytes() {
+  size_t m = sizeof(GmfSmem);
+  m = std::max(m, sizeof(SmfS<2, true>));
+  m = std::max(m, sizeof(SmfS<2, false>));
+  m = std::max(m, sizeof(SmfxS<2, true>));
+  return m;
+}
+
+// ------------------------------------------------------------------------------------------------ host side
+struct Tuning {
+  int ctas_per_sm = 2;
+  int longest_first = 1;
+};
+Tuning g_tune;
+
+struct Table {                  // a validated request list laid out for the device
+  std::vector<unsigned char> bytes;  // DevReq[count] | tile_start[count + 1] | coefficient blocks
+  size_t off_tiles = 0, off_coef = 0;
+  int count = 0;
+};
+
+size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// -1: invalid request (the rules of the single entry points), 0: ok
+int build_table(const mf_request *req, int count, Table &T) {
+  if (count < 0 || (count > 0 && !req)) return -1;
+  struct Item {
+    DevReq d;
+    std::vector<unsigned char> coef;
+    long long tiles;
+    double work;
+  };
+  std::vector<Item> items;
+  items.reserve(count);
+  for (int i = 0; i < count; i++) {
+    const mf_request &r = req[i];
+    int kind = r.kind;
+    double al = r.alpha;
+    if (r.family < 0 || r.family > 2 || kind < SMF_EXP || kind > SMF_SQRT || r.order < 0 || r.order > 2 ||
+        r.n < 0 || (r.dtype != 0 && r.dtype != 1) || (r.family == 2 && r.dtype != 0) ||
+        (kind == SMF_POW && !(al > 0)))
+      return -1;
+    if (r.n > 0 && (!r.x || !r.F || (r.order >= 1 && !r.J) || (r.order >= 2 && !r.H))) return -1;
+    if (r.n > (long long)INT_MAX * 32) return -1;
+    if (r.n == 0) continue;
+    if (r.family == 2 && kind == SMF_SQRT) kind = SMF_POW, al = 0.5;
+    if (kind != SMF_POW) al = kind == SMF_SQRT ? 0.5 : 0.0;
+    Item it;
+    it.d = DevReq{r.family, kind, r.order, r.dtype, al, (long long)r.n, r.x, r.F, r.order >= 1 ? r.J : nullptr,
+                  r.order >= 2 ? r.H : nullptr, 0};
+    if (r.family == 2) {
+      GmfCoef C;
+      gmf_coef(kind, al, r.order, C);
+      it.coef.resize(sizeof C);
+      std::memcpy(it.coef.data(), &C, sizeof C);
+    } else if (r.dtype == 0) {
+      SmfCoef C;
+      smf_coef(kind, al, C);
+      it.coef.resize(sizeof C);
+      std::memcpy(it.coef.data(), &C, sizeof C);
+    } else {
+      SmfCoefF C;
+      smf_coef_f(kind, al, C);
+      it.coef.resize(sizeof C);
+      std::memcpy(it.coef.data(), &C, sizeof C);
+    }
+    it.tiles = (r.n + BT_TPB - 1) / BT_TPB;
+    // relative work per matrix (measured orders of magnitude): gmf order 2 >> smf order 2 >> first orders
+    const double per = (r.family == 2 ? 4.0 : 1.0) * (r.order == 2 ? 4.0 : (r.order == 1 ? 1.5 : 1.0)) *
+                       (r.dtype == 1 ? 0.3 : 1.0);
+    it.work = per * (double)r.n;
+    items.push_back(std::move(it));
+  }
+  if (g_tune.longest_first)
+    std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) { return a.work > b.work; });
+  T.count = (int)items.size();
+  T.off_tiles = align16(sizeof(DevReq) * T.count);
+  T.off_coef = align16(T.off_tiles + sizeof(long long) * (T.count + 1));
+  size_t coef_bytes = 0;
+  for (auto &it : items) coef_bytes += align16(it.coef.size());
+  T.bytes.assign(T.off_coef + coef_bytes, 0);
+  long long tiles = 0;
+  size_t co = 0;
+  for (int i = 0; i < T.count; i++) {
+    items[i].d.coef_off = (long long)co;
+    std::memcpy(T.bytes.data() + sizeof(DevReq) * i, &items[i].d, sizeof(DevReq));
+    std::memcpy(T.bytes.data() + T.off_tiles + sizeof(long long) * i, &tiles, sizeof tiles);
+    std::memcpy(T.bytes.data() + T.off_coef + co, items[i].coef.data(), items[i].coef.size());
+    tiles += items[i].tiles;
+    co += align16(items[i].coef.size());
+  }
+  std::memcpy(T.bytes.data() + T.off_tiles + sizeof(long long) * T.count, &tiles, sizeof tiles);
+  return 0;
+}
+
+cudaError_t prepare_kernel() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  const cudaError_t e =
+      cudaFuncSetAttribute(batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
+cudaError_t launch_table(const unsigned char *dev_table, const Table &T, unsigned long long *cursor,
+                         cudaStream_t st) {
+  if (T.count == 0) return cudaSuccess;
+  cudaError_t e = prepare_kernel();
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = (unsigned)(sms * std::max(1, g_tune.ctas_per_sm));
+  batched_kernel<<<grid, BT_TPB, smem_bytes(), st>>>((const DevReq *)dev_table, T.count,
+                                                     (const long long *)(dev_table + T.off_tiles), cursor,
+                                                     dev_table + T.off_coef);
+  return cudaGetLastError();
+}
+
+struct Plan {
+  unsigned char *dev = nullptr;  // table, then the cursor
+  Table table;
+  size_t cursor_off = 0;
+};
+
+struct Scratch {  // per-device table buffer of matfun_cuda_batched
+  std::mutex mu;
+  unsigned char *dev = nullptr;
+  size_t size = 0;
+  cudaEvent_t last = nullptr;  // completion of the previous launch that used the buffer
+};
+Scratch g_scratch[64];
+
+}  // namespace
+}  // namespace mf
+
+using namespace mf;
+
+extern "C" int matfun_cuda_batched(const mf_request *requests, int count, void *stream) {
+  Table T;
+  if (build_table(requests, count, T) != 0) return -1;
+  if (T.count == 0) return 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -2;
+  Scratch &S = g_scratch[dev];
+  std::lock_guard<std::mutex> lock(S.mu);
+  const cudaStream_t st = (cudaStream_t)stream;
+  const size_t need = align16(T.bytes.size()) + sizeof(unsigned long long);
+  if (S.size < need) {
+    if (S.dev) {
+      if (S.last) cudaEventSynchronize(S.last);
+      cudaFree(S.dev);
+    }
+    S.dev = nullptr;
+    S.size = 0;
+    if (cudaMalloc(&S.dev, need) != cudaSuccess) return -2;
+    S.size = need;
+  }
+  if (!S.last && cudaEventCreateWithFlags(&S.last, cudaEventDisableTiming) != cudaSuccess) return -2;
+  // the previous launch on another stream may still read the buffer: order this upload after it
+  if (cudaStreamWaitEvent(st, S.last, 0) != cudaSuccess) return -2;
+  // (a copy from pageable memory is staged before the call returns, so the host table may go out of scope)
+  cudaError_t e = cudaMemcpyAsync(S.dev, T.bytes.data(), T.bytes.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = launch_table(S.dev, T, (unsigned long long *)(S.dev + align16(T.bytes.size())), st);
+  if (e == cudaSuccess) e = cudaEventRecord(S.last, st);
+  return e == cudaSuccess ? 0 : -2;
+}
+
+extern "C" int matfun_cuda_batched_plan(const mf_request *requests, int count, void **plan) {
+  if (!plan) return -1;
+  *plan = nullptr;
+  Plan *P = new Plan;
+  if (build_table(requests, count, P->table) != 0) {
+    delete P;
+    return -1;
+  }
+  P->cursor_off = align16(P->table.bytes.size());
+  if (cudaMalloc(&P->dev, P->cursor_off + sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemcpy(P->dev, P->table.bytes.data(), P->table.bytes.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (P->dev) cudaFree(P->dev);
+    delete P;
+    return -2;
+  }
+  *plan = P;
+  return 0;
+}
+
+extern "C" int matfun_cuda_batched_run(void *plan, void *stream) {
+  Plan *P = (Plan *)plan;
+  if (!P) return -1;
+  const cudaError_t e = launch_table(P->dev, P->table, (unsigned long long *)(P->dev + P->cursor_off),
+                                     (cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : -2;
+}
+
+extern "C" int matfun_cuda_batched_free(void *plan) {
+  Plan *P = (Plan *)plan;
+  if (!P) return 0;
+  const cudaError_t e = P->dev ? cudaFree(P->dev) : cudaSuccess;
+  delete P;
+  return e == cudaSuccess ? 0 : -2;
+}
+
+extern "C" int matfun_cuda_batched_tune(int ctas_per_sm, int longest_first) {
+  if (ctas_per_sm < 1 || ctas_per_sm > 8 || (longest_first != 0 && longest_first != 1)) return -1;
+  g_tune.ctas_per_sm = ctas_per_sm;
+  g_tune.longest_first = longest_first;
+  return 0;
+}

@@ -53,15 +53,12 @@ MF_D unsigned short hmap_entry(int w) {
   return (unsigned short)(sym3(x1, y1, z1) | (sym3(x2, y2, z2) << 8));
 }
 
+// one tile: matrices base .. base + cnt - 1 by a CTA of GMF_TPB threads (the standalone kernel and the batched
+// persistent kernel run the same code)
 template <int KIND, int ORDER>
-__global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const double *__restrict__ A, double *__restrict__ F,
-                                                      double *__restrict__ J, double *__restrict__ H,
-                                                      const GmfCoef C) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  GmfSmem &S = *reinterpret_cast<GmfSmem *>(smem_raw);
+MF_D void gmf_tile(int64_t base, int cnt, const double *__restrict__ A, double *__restrict__ F,
+                   double *__restrict__ J, double *__restrict__ H, const GmfCoef &C, GmfSmem &S) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t base = (int64_t)blockIdx.x * GMF_TPB;
-  const int cnt = (int)min((int64_t)GMF_TPB, n - base);
 
   for (int e = tid; e < cnt * 9; e += GMF_TPB) S.x[e] = A[base * 9 + e];
   if (ORDER >= 2) {  // index tables of phase B
@@ -207,6 +204,16 @@ __global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const double *_
       __syncwarp();
     }
   }
+}
+
+template <int KIND, int ORDER>
+__global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const double *__restrict__ A, double *__restrict__ F,
+                                                      double *__restrict__ J, double *__restrict__ H,
+                                                      const GmfCoef C) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  GmfSmem &S = *reinterpret_cast<GmfSmem *>(smem_raw);
+  const int64_t base = (int64_t)blockIdx.x * GMF_TPB;
+  gmf_tile<KIND, ORDER>(base, (int)min((int64_t)GMF_TPB, n - base), A, F, J, H, C, S);
 }
 
 template <int KIND, int ORDER>

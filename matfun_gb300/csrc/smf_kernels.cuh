@@ -15,7 +15,7 @@
 
 namespace mf {
 
-constexpr int SMF_TPB = 64;
+constexpr int SMF_TPB = 64;  // matrices per CTA of the standalone kernel
 
 // index of the product vector of the Cartesian pair (k, l) (Voigt order 00 11 22 01 02 12)
 MF_D constexpr int pidx(int k, int l) { return k == l ? k : k + l + 2; }
@@ -33,19 +33,25 @@ MF_D double mulpow2(double x, int k) {
 MF_D constexpr int midx(int m) { return m % 4 == 0 ? m / 4 : (m == 1 || m == 3 ? 3 : (m == 2 || m == 6 ? 4 : 5)); }
 MF_D constexpr int mwt_log2(int m) { return m % 4 == 0 ? 0 : -1; }
 
-template <int KIND, int ORDER, bool MAT>
-__global__ void __launch_bounds__(SMF_TPB) smf_kernel(int64_t n, const double *__restrict__ x,
-                                                      double *__restrict__ F, double *__restrict__ J,
-                                                      double *__restrict__ H, const SmfCoef C,
-                                                      int *__restrict__ asym) {
+// shared memory of one tile of TPB matrices
+template <int ORDER, bool MAT, int TPB>
+struct SmfTileSmem {
+  static constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6;
+  double sX[TPB * NIN];
+  double sF[TPB * NF];
+  double sK[ORDER >= 1 ? TPB * 21 : 1];
+  double sG[ORDER >= 2 ? TPB * 56 : 1];
+};
+
+// one tile: matrices base .. base + cnt - 1 by a CTA of TPB threads (the standalone kernel and the batched
+// persistent kernel run the same code)
+template <int KIND, int ORDER, bool MAT, int SMF_TPB>
+MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *__restrict__ F,
+                   double *__restrict__ J, double *__restrict__ H, const SmfCoef &C, int *__restrict__ asym,
+                   SmfTileSmem<ORDER, MAT, SMF_TPB> &TS) {
   constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6, NJ = NF * NF, NH = NJ * NF;
-  __shared__ double sX[SMF_TPB * NIN];
-  __shared__ double sF[SMF_TPB * NF];
-  __shared__ double sK[ORDER >= 1 ? SMF_TPB * 21 : 1];
-  __shared__ double sG[ORDER >= 2 ? SMF_TPB * 56 : 1];
+  double *sX = TS.sX, *sF = TS.sF, *sK = TS.sK, *sG = TS.sG;
   const int tid = threadIdx.x;
-  const int64_t base = (int64_t)blockIdx.x * SMF_TPB;
-  const int cnt = (int)min((int64_t)SMF_TPB, n - base);
 
   for (int e = tid; e < cnt * NIN; e += SMF_TPB) sX[e] = x[base * NIN + e];  // coalesced input
   __syncthreads();
@@ -258,6 +264,16 @@ __global__ void __launch_bounds__(SMF_TPB) smf_kernel(int64_t n, const double *_
         if (tid + SMF_TPB * k < NH) o[tid + SMF_TPB * k] = mulpow2(s[hidx[k]], hexp[k]);
     }
   }
+}
+
+template <int KIND, int ORDER, bool MAT>
+__global__ void __launch_bounds__(SMF_TPB) smf_kernel(int64_t n, const double *__restrict__ x,
+                                                      double *__restrict__ F, double *__restrict__ J,
+                                                      double *__restrict__ H, const SmfCoef C,
+                                                      int *__restrict__ asym) {
+  __shared__ SmfTileSmem<ORDER, MAT, SMF_TPB> TS;
+  const int64_t base = (int64_t)blockIdx.x * SMF_TPB;
+  smf_tile<KIND, ORDER, MAT, SMF_TPB>(base, (int)min((int64_t)SMF_TPB, n - base), x, F, J, H, C, asym, TS);
 }
 
 template <int KIND, bool MAT>

@@ -129,20 +129,24 @@ MF_D float dd2_same_f(double l, float fl, float Dll, const SmfCoefF &C) {
   return out;
 }
 
-constexpr int SMFX_TPB = 64;
+constexpr int SMFX_TPB = 64;  // matrices per CTA of the standalone kernel
 
-template <int KIND, int ORDER, bool MAT>
-__global__ void __launch_bounds__(SMFX_TPB) smf_mixed_kernel(int64_t n, const float *__restrict__ x,
-                                                             float *__restrict__ F, float *__restrict__ J,
-                                                             float *__restrict__ H, const SmfCoefF C) {
+template <int ORDER, bool MAT, int TPB>
+struct SmfxTileSmem {
+  static constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6;
+  float sX[TPB * NIN];
+  float sF[TPB * NF];
+  float sK[ORDER >= 1 ? TPB * 21 : 1];
+  float sG[ORDER >= 2 ? TPB * 56 : 1];
+};
+
+template <int KIND, int ORDER, bool MAT, int SMFX_TPB>
+MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, float *__restrict__ F,
+                         float *__restrict__ J, float *__restrict__ H, const SmfCoefF &C,
+                         SmfxTileSmem<ORDER, MAT, SMFX_TPB> &TS) {
   constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6, NJ = NF * NF, NH = NJ * NF;
-  __shared__ float sX[SMFX_TPB * NIN];
-  __shared__ float sF[SMFX_TPB * NF];
-  __shared__ float sK[ORDER >= 1 ? SMFX_TPB * 21 : 1];
-  __shared__ float sG[ORDER >= 2 ? SMFX_TPB * 56 : 1];
+  float *sX = TS.sX, *sF = TS.sF, *sK = TS.sK, *sG = TS.sG;
   const int tid = threadIdx.x;
-  const int64_t base = (int64_t)blockIdx.x * SMFX_TPB;
-  const int cnt = (int)min((int64_t)SMFX_TPB, n - base);
   for (int e = tid; e < cnt * NIN; e += SMFX_TPB) sX[e] = x[base * NIN + e];
   __syncthreads();
   if (tid < cnt) {
@@ -351,6 +355,15 @@ __global__ void __launch_bounds__(SMFX_TPB) smf_mixed_kernel(int64_t n, const fl
         if (tid + SMFX_TPB * k < NH) o[tid + SMFX_TPB * k] = mulpow2f(s[hidx[k]], hexp[k]);
     }
   }
+}
+
+template <int KIND, int ORDER, bool MAT>
+__global__ void __launch_bounds__(SMFX_TPB) smf_mixed_kernel(int64_t n, const float *__restrict__ x,
+                                                             float *__restrict__ F, float *__restrict__ J,
+                                                             float *__restrict__ H, const SmfCoefF C) {
+  __shared__ SmfxTileSmem<ORDER, MAT, SMFX_TPB> TS;
+  const int64_t base = (int64_t)blockIdx.x * SMFX_TPB;
+  smf_mixed_tile<KIND, ORDER, MAT, SMFX_TPB>(base, (int)min((int64_t)SMFX_TPB, n - base), x, F, J, H, C, TS);
 }
 
 inline void smf_coef_f(int kind, double al, SmfCoefF &C) {
