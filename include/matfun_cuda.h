@@ -91,6 +91,17 @@ int matfun_cuda_batched(const mf_request *requests, int count, void *stream);
 int matfun_cuda_batched_plan(const mf_request *requests, int count, void **plan);
 int matfun_cuda_batched_run(void *plan, void *stream);
 int matfun_cuda_batched_free(void *plan);
+/* No counterpart in the reference.  matfun_cuda_batched without any device allocation, for callers that cannot call
+ * cudaMalloc (a framework that owns all device memory through its own allocator, a plugin that is only handed device
+ * arrays): the request table and the tile cursor go into one fixed 256 KiB array of device memory that belongs to the
+ * library image (present on every GPU that uses the library, until the process exits) instead of a buffer allocated
+ * on first use.  The first call on a device looks up that array's device address (cudaGetSymbolAddress) with the
+ * device current; make that first call before capturing a stream.  All calls share the array and it keeps the last
+ * call's table: calls whose launches overlap on the GPU (different streams, no ordering between them) race and give
+ * wrong results.  Returns 0, -1 (an invalid request), -2 (CUDA error), -4 (the table -- 72 bytes per request plus its
+ * coefficients, about 2.5 KB for gmf and 0.3 KB for smf -- does not fit the 256 KiB). */
+int matfun_cuda_batched_noalloc(const mf_request *requests, int count, void *stream);
+
 /* Tuning of the persistent launch (set by the autotuner, matfun_gb300/autotune.py): CTAs per SM (1..8) and whether
  * requests are laid out longest first (1) or as given (0).  Returns 0 or -1. */
 int matfun_cuda_batched_tune(int ctas_per_sm, int longest_first);

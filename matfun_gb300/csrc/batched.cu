@@ -298,3 +298,42 @@ extern "C" int matfun_cuda_batched_tune(int ctas_per_sm, int longest_first) {
   g_tune.longest_first = longest_first;
   return 0;
 }
+
+// ------------------------------------------------------------------------------------------------ no allocation
+// matfun_cuda_batched_noalloc: the same batched launch for callers that must not allocate device memory -- code that
+// runs inside a host framework which owns every device allocation (its own caching allocator or memory pool), or a
+// plugin that is only handed device arrays.  matfun_cuda_batched caches a table buffer it allocates with cudaMalloc;
+// this entry point instead writes the request table and the tile cursor into one fixed array of device memory that
+// is part of the library image (NOALLOC_BYTES, loaded with the library on every GPU that uses it and held until the
+// process exits).  It calls no cudaMalloc, cudaFree or other device-allocating routine.
+namespace {
+constexpr size_t NOALLOC_BYTES = 256 * 1024;  // cursor (16 bytes) + request table: ~100 gmf or ~700 smf requests
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_addr[64] = {};  // device address of g_noalloc_scratch, per device (set up on first use)
+}  // namespace
+
+extern "C" int matfun_cuda_batched_noalloc(const mf_request *requests, int count, void *stream) {
+  Table T;
+  if (build_table(requests, count, T) != 0) return -1;
+  if (T.count == 0) return 0;
+  if (16 + T.bytes.size() > NOALLOC_BYTES) return -4;  // the table does not fit the fixed scratch array
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -2;
+  unsigned char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {  // first call on this device: the device address of the array, with it current
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return -2;
+      g_noalloc_addr[dev] = (unsigned char *)p;
+    }
+    base = g_noalloc_addr[dev];
+  }
+  const cudaStream_t st = (cudaStream_t)stream;
+  // the cursor (first 16 bytes) is cleared by launch_table; the table follows it
+  cudaError_t e = cudaMemcpyAsync(base + 16, T.bytes.data(), T.bytes.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = launch_table(base + 16, T, (unsigned long long *)base, st);
+  return e == cudaSuccess ? 0 : -2;
+}
