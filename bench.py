@@ -265,14 +265,14 @@ def adjoint_vs_materialised(lib, args, dev):
         def mat_vjp():
             for lo in range(0, n, ch):
                 ev(kind, alpha, ch, A[lo:].data_ptr(), Fm.data_ptr(), Jm.data_ptr(), None, None)
-                torch.einsum("nab,nabcd->ncd", W[lo:lo + ch], Jm.view(ch, 3, 3, 3, 3), out=Abar[lo:lo + ch])
+                Abar[lo:lo + ch] = torch.einsum("nab,nabcd->ncd", W[lo:lo + ch], Jm.view(ch, 3, 3, 3, 3))
 
         def mat_hvp():
             for lo in range(0, n, ch):
                 ev(kind, alpha, ch, A[lo:].data_ptr(), Fm.data_ptr(), Jm.data_ptr(), Hm.data_ptr(), None)
                 HV = torch.einsum("nabcdef,ncd->nabef", Hm.view(ch, 3, 3, 3, 3, 3, 3), V[lo:lo + ch])
-                torch.einsum("nab,nabef->nef", W[lo:lo + ch], HV, out=HWV[lo:lo + ch])
-                torch.einsum("nabcd,ncd->nab", Jm.view(ch, 3, 3, 3, 3), V[lo:lo + ch], out=JV[lo:lo + ch])
+                HWV[lo:lo + ch] = torch.einsum("nab,nabef->nef", W[lo:lo + ch], HV)
+                JV[lo:lo + ch] = torch.einsum("nabcd,ncd->nab", Jm.view(ch, 3, 3, 3, 3), V[lo:lo + ch])
 
         t_mvjp, t_mhvp = timeit(mat_vjp, 1), timeit(mat_hvp, 1)
         res[f"{fam}_{'log' if kind == 1 else 'pow0.3'}"] = {
@@ -282,6 +282,73 @@ def adjoint_vs_materialised(lib, args, dev):
             "vjp_speedup": t_mvjp / t_vjp, "hvp_speedup": t_mhvp / t_hvp,
             "bytes_per_matrix": {"vjp": 216, "hvp": 288}}
     return res
+
+
+def batched_c3(lib, args, dev):
+    """C3: 64 requests, sizes log-uniform in [1e3, 1e6] rescaled to ~8e6 matrices in total, each with a random kind,
+    order in {0, 1, 2}, family in {smf Voigt, smf matrix, gmf} and precision (FP32 for smf only), inputs from the C0 /
+    C1 generators: one autotuned persistent launch replayed from a CUDA graph, against the 64 single-entry launches"""
+    import torch
+
+    from matfun_gb300 import autotune, batched
+    from matfun_gb300 import workloads as w
+    rng = np.random.default_rng(3)
+    sizes = 10.0 ** rng.uniform(3.0, 6.0, 64)
+    sizes = np.maximum(1000, (sizes * args.c3_total / sizes.sum()).astype(np.int64))
+    pool_s = w.c0_smf_spd(int(sizes.max()), seed=7, as_voigt=False)
+    pool_g = w.c1_gmf_groups(int(sizes.max()), seed=8)
+    reqs = []
+    for i, n in enumerate(sizes):
+        fam = ["smf_voigt", "smf", "gmf"][rng.integers(3)]
+        kind = ["exp", "log", "sqrt", "pow"][rng.integers(4)]
+        order = int(rng.integers(3))
+        f32 = fam != "gmf" and rng.uniform() < 0.5
+        src = pool_g[:n] if fam == "gmf" else pool_s[:n]
+        if fam == "smf_voigt":
+            src = w.voigt(src)
+        t = torch.from_numpy(np.ascontiguousarray(src)).to(dev)
+        reqs.append(batched.request(fam, kind, t.float() if f32 else t, order=order,
+                                    alpha=float(rng.uniform(0.1, 0.9)) if kind == "pow" else None))
+    total = int(sum(r.n for r in reqs))
+    choice, tune_ms = autotune.tune(reqs, reps=1, save=False)
+    plan = batched.Plan(reqs)
+    st = torch.cuda.Stream(dev)
+    st.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(st):
+        plan.run()
+    torch.cuda.current_stream(dev).wait_stream(st)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        plan.run()
+    fns = {(0, 0): lib.smf_cuda_eval, (1, 0): lib.smf_cuda_eval_matrix, (2, 0): lib.gmf_cuda_eval,
+           (0, 1): lib.smf_cuda_eval_f32, (1, 1): lib.smf_cuda_eval_matrix_f32}
+    p = lambda t: None if t is None else t.data_ptr()
+
+    def singles():
+        for r in reqs:
+            c = r.c
+            fns[(c.family, c.dtype)](c.kind, c.alpha, c.n, r.x.data_ptr(), p(r.F), p(r.J), p(r.H), None)
+
+    def timeit(f, reps):
+        f()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            f()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_graph = timeit(g.replay, args.c3_steps)
+    t_single = timeit(singles, args.c3_steps)
+    return {"workload": "64 requests, sizes log-uniform [1e3,1e6], mixed family/kind/order/precision (C3)",
+            "matrices": total, "requests": len(reqs),
+            "batched_graph_matrices_per_s": total / (t_graph * 1e-3), "batched_ms": t_graph,
+            "single_launches_matrices_per_s": total / (t_single * 1e-3), "single_ms": t_single,
+            "speedup": t_single / t_graph, "autotuned": choice,
+            "autotune_ms": {k: round(v, 3) for k, v in tune_ms.items()}}
 
 
 def run_ours(args, rank, world, local):
@@ -384,6 +451,8 @@ def run_ours(args, rank, world, local):
         out["mixed"] = mixed_vs_fp64(lib, args, dev, hbm)
     if rank == 0 and not args.no_adjoint:
         out["adjoint"] = adjoint_vs_materialised(lib, args, dev)
+    if rank == 0 and not args.no_batched:
+        out["batched"] = batched_c3(lib, args, dev)
     if rank == 0 and not args.no_cpu:
         Xs = np.ascontiguousarray(X[np.concatenate([np.arange(g * n // 4, g * n // 4 + args.cpu_sample // 4)
                                                     for g in range(4)])])
@@ -408,6 +477,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--c3-total", type=int, default=8_000_000)
+    ap.add_argument("--c3-steps", type=int, default=3)
     ap.add_argument("--adj-n", type=int, default=1 << 22)
     ap.add_argument("--mixed-n", type=int, default=1 << 24)
     ap.add_argument("--mixed-steps", type=int, default=5)
