@@ -41,92 +41,193 @@ MF_D float fun_f(float x, float al) {
   return KIND == SQRT ? sqrtf(x) : powf(x, al);
 }
 
-// f[a, b] in FP32 from FP64 eigenvalues (their difference and sum taken in FP64) -- smf_kernel.hpp:84-115
+// Divided differences on eigenvalues sorted ascending, in FP32.  The eigenvalue differences are taken in FP64 and
+// rounded once (dab = b - a >= 0 and friends), so the near-coalescent branches see the same relative precision as
+// the FP64 kernel; with the order known, the choice of difference formula and of the cluster midpoint of the FP64
+// kernel becomes static.
+// f[a, b], a <= b, dab = b - a -- smf_kernel.hpp:84-115
 template <int KIND>
-MF_D float dd1_f(double a, double b, float fa, float fb, const SmfCoefF &C) {
-  if (KIND == EXP) {
-    const float d = (float)fabs(a - b);
-    return self(a > b, fa, fb) * self(d > 0.f, -expm1f(-d) / d, 1.f);
-  }
+MF_D float dd1s_f(float a, float b, float dab, float fa, float fb, const SmfCoefF &C) {
+  if (KIND == EXP) return fb * self(dab > 0.f, -expm1f(-dab) / dab, 1.f);
   if (KIND == LOG) {
-    const float s = (float)(0.5 * (a + b)), z = (float)(a - b) / (float)(a + b), az = fabsf(z), z2 = z * z;
+    float s = 0.5f * (a + b), z = dab / (a + b), az = fabsf(z), z2 = z * z;
     if (az < 1e-3f) return (1.f + z2 / 3.f + z2 * z2 / 5.f + z2 * z2 * z2 / 7.f) / s;
-    if (az >= 0.5f) return (logf((float)a) - logf((float)b)) / (float)(a - b);
+    if (az >= 0.5f) return (logf(b) - logf(a)) / dab;
     return atanhf(z) / z / s;
   }
-  a = sel(a > 0, a, 0.0);
-  b = sel(b > 0, b, 0.0);
-  if (KIND == SQRT) return 1.f / (sqrtf((float)a) + sqrtf((float)b));
-  const double sd = 0.5 * (a + b);
-  const float s = (float)sd, ss = self(s > 0.f, s, 1.f);
-  const float z = (float)(a - b) / (2.f * ss), az = fabsf(z);
-  const bool zero = az == 0.f, near = !zero & (az < 0.5f);
-  if (!zero & !near) return (fa - fb) / (float)(a - b);
-  const float g = zero ? C.al : (expm1f(C.al * log1pf(z)) - expm1f(C.al * log1pf(-z))) / (2.f * z);
+  if (KIND == SQRT) return 1.f / (sqrtf(a) + sqrtf(b));
+  float s = 0.5f * (a + b), ss = self(s > 0.f, s, 1.f);
+  float z = dab / (2.f * ss), az = fabsf(z);
+  bool zero = az == 0.f, near = !zero & (az < 0.5f);
+  if (!zero & !near) return (fb - fa) / dab;
+  float g = zero ? C.al : (expm1f(C.al * log1pf(z)) - expm1f(C.al * log1pf(-z))) / (2.f * z);
   return (s > 0.f ? powf(ss, C.alm1) : C.zp1) * g;
 }
 
 template <int KIND>
-MF_D float deriv_f(double x, float fx, const SmfCoefF &C) {
+MF_D float deriv_f(float x, float fx, const SmfCoefF &C) {
   if (KIND == EXP) return fx;
-  if (KIND == LOG) return 1.f / (float)x;
-  const float xf = self(x > 0, (float)x, 0.f);
+  if (KIND == LOG) return 1.f / x;
+  float xf = self(x > 0.f, x, 0.f);
   if (KIND == SQRT) return 1.f / (2.f * sqrtf(xf));
   return xf > 0.f ? C.al * powf(xf, C.alm1) : C.al * C.zp1;
 }
 
-// f[li, lj, lk] in FP32; the ordering and the differences of the FP64 eigenvalues in FP64 -- smf_kernel.hpp:148-192
+// f[li, lj, lk] for li <= lj <= lk; dji = lj - li, dkj = lk - lj, dki = lk - li -- smf_kernel.hpp:148-192 (the widest
+// difference is the denominator, the middle eigenvalue the cluster centre)
 template <int KIND>
-MF_D float dd2_f(double li, double lj, double lk, float fi, float fj, float fk, float Dij, float Dik, float Djk,
-                 const SmfCoefF &C) {
-  if (KIND == POW || KIND == SQRT) {
-    li = sel(li > 0, li, 0.0); lj = sel(lj > 0, lj, 0.0); lk = sel(lk > 0, lk, 0.0);
-  }
-  const double dA = lk - li, dB = lj - li, dC = lk - lj;
-  const float aA = fabsf((float)dA), aB = fabsf((float)dB), aC = fabsf((float)dC);
-  const bool useA = (aA >= aB) & (aA >= aC), useB = !useA & (aB >= aC);
-  const float num = self(useA, Djk - Dij, self(useB, Djk - Dik, Dik - Dij));
-  const float den = (float)sel(useA, dA, sel(useB, dB, dC));
-  const double mn = sel(li < lj, li, lj), mx = sel(li < lj, lj, li);
-  const double lo = sel(mn < lk, mn, lk), hi = sel(mx > lk, mx, lk), t = sel(mx < lk, mx, lk), mid = sel(mn > t, mn, t);
-  const float u0 = (float)(lo - mid), w0 = (float)(hi - mid), midf = (float)mid;
+MF_D float dd2s_f(float lj, float lk, float fj, float Dij, float Djk, float dji, float dkj, float dki,
+                  const SmfCoefF &C) {
   bool cluster;
-  if (KIND == EXP) cluster = (w0 - u0) <= 1.f;
-  else cluster = (midf > 0.f) & (-u0 <= C.tau * midf) & (w0 <= C.tau * midf);
+  if (KIND == EXP) cluster = (dkj + dji) <= 1.f;
+  else cluster = (lj > 0.f) & (dji <= C.tau * lj) & (dkj <= C.tau * lj);
   float out;
   if (cluster) {
-    const float fm = self(mid == li, fi, self(mid == lj, fj, fk));
     float u, w, scale;
     if (KIND == EXP) {
-      u = u0; w = w0; scale = fm;
+      u = -dji; w = dkj; scale = fj;
     } else {
-      u = u0 / midf; w = w0 / midf;
-      scale = (KIND == LOG ? 1.f : fm) / (midf * midf);
+      u = -dji / lj; w = dkj / lj;
+      scale = (KIND == LOG ? 1.f : fj) / (lj * lj);
     }
-    float h = 1.f, wk = 1.f, s = C.c2[0];
+    float h = 1.f, wk = 1.f, sm = C.c2[0];
 #pragma unroll
     for (int k = 1; k < DD2_TERMS; k++) {
       wk = wk * w;
       h = fmaf(u, h, wk);
-      s = fmaf(C.c2[k], h, s);
+      sm = fmaf(C.c2[k], h, sm);
     }
-    out = scale * s;
+    out = scale * sm;
   } else {
-    out = num / self(den != 0.f, den, 1.f);
+    out = (Djk - Dij) / self(dki != 0.f, dki, 1.f);
   }
-  if (KIND == POW || KIND == SQRT) out = self(hi > 0, out, C.z2);
+  if (KIND == POW || KIND == SQRT) out = self(lk > 0.f, out, C.z2);
   return out;
 }
 
 template <int KIND>
-MF_D float dd2_same_f(double l, float fl, float Dll, const SmfCoefF &C) {
-  if (KIND == POW || KIND == SQRT) l = sel(l > 0, l, 0.0);
-  const float lf = (float)l;
+MF_D float dd2_same_f(float lf, float fl, float Dll, const SmfCoefF &C) {
   bool cluster = KIND == EXP ? true : (lf > 0.f);
   float out = KIND == EXP ? self(cluster, fl * C.c2[0], Dll - Dll)
                           : self(cluster, ((KIND == LOG ? 1.f : fl) / (lf * lf)) * C.c2[0], Dll - Dll);
   if (KIND == POW || KIND == SQRT) out = self(lf > 0.f, out, C.z2);
   return out;
+}
+
+// |x| of a double as an ordered integer key (max of magnitudes on the integer pipe)
+MF_D long long absbits(double x) { return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll; }
+MF_D long long kmax(long long a, long long b) { return a > b ? a : b; }
+
+// 2^-e for a power of two 2^e of normal range (exponent arithmetic, no division)
+MF_D double pow2inv(double p) {
+  long long e = (__double_as_longlong(p) >> 52) & 0x7FF;
+  return __longlong_as_double((2046ll - e) << 52);
+}
+
+MF_D float nrm3(float &x, float &y, float &z) {
+  float n = __fsqrt_rn(x * x + y * y + z * z), i = __fdiv_rn(1.f, n);
+  x *= i; y *= i; z *= i;
+  return n;
+}
+
+// The eigensystem of the mixed path.  FP32: the cubic's trigonometric root (on the deviator normalised to max 1, where
+// the root of the separated eigenvalue is insensitive to rounding of r), its eigenvector (largest cross product of
+// two rows of G - root I), the orthonormal complement and the 2x2 Jacobi rotation.  FP64: the deviator and the
+// Rayleigh quotients of the FP32 vectors in the deviator shifted by minus half the root (the centre of the remaining
+// pair), so that the pair's block is of the size of its own gap: the rotation angle is then accurate relative to the
+// gap, and the quotients, divided by the vectors' FP64 squared norms (1 - e + e^2 with e = |x|^2 - 1), give the
+// eigenvalues to ~1e-14 relative to |A| (an FP32 vector error d moves a quotient by O(d^2)).  Eigenvalues and the
+// deviator's eigenvalues (xd, for log near the mean) are in the units of the input.
+struct SmfEigM {
+  double lam[3], xd[3], m;
+  float V[3][3];
+};
+
+template <int KIND>
+MF_D void smf_eigsys_mixed(const double *v, SmfEigM &E) {
+  constexpr float SQRT6 = 2.4494897f, TWO_PI_3 = 2.0943951f;
+  double m = (v[0] + v[1] + v[2]) * (1.0 / 3.0);
+  double d0 = v[0] - m, d1 = v[1] - m, d2 = v[2] - m;
+  long long k01 = kmax(absbits(d0), absbits(d1)), k23 = kmax(absbits(d2), absbits(v[3]));
+  long long k45 = kmax(absbits(v[4]), absbits(v[5]));
+  double dmax = __longlong_as_double(kmax(kmax(k01, k23), k45));
+  bool bad = !(dmax < 1e300), iso = !(dmax > 0.0) | bad;  // bad: NaN or infinite input (NaN vectors and results)
+  double dsc = sel(iso, 1.0, pow2floor(dmax)), ids = pow2inv(dsc);
+  float g0 = (float)(d0 * ids), g1 = (float)(d1 * ids), g2 = (float)(d2 * ids);
+  float g3 = (float)(v[3] * ids), g4 = (float)(v[4] * ids), g5 = (float)(v[5] * ids);
+  float p = g0 * g0 + g1 * g1 + g2 * g2 + 2.f * (g3 * g3 + g4 * g4 + g5 * g5);
+  float q = g0 * (g1 * g2 - g5 * g5) - g3 * (g3 * g2 - g5 * g4) + g4 * (g3 * g5 - g1 * g4);
+  float pg = self(iso, 1.f, p), qg = self(iso, 0.f, q);
+  float r = 3.f * SQRT6 * qg / (pg * sqrtf(pg));
+  r = self(r > 1.f, 1.f, self(r < -1.f, -1.f, r));
+  float t = sqrtf(2.f * pg / 3.f), ph = acosf(r) / 3.f;
+  float sh = t * cosf(self(r >= 0.f, ph, ph + TWO_PI_3));
+  float m00 = g0 - sh, m11 = g1 - sh, m22 = g2 - sh;
+  float cxv = g3 * g5 - g4 * m11, cyv = g4 * g3 - m00 * g5, czv = m00 * m11 - g3 * g3;
+  float nn = cxv * cxv + cyv * cyv + czv * czv;
+  {
+    float bx = g3 * m22 - g4 * g5, by = g4 * g4 - m00 * m22, bz = m00 * g5 - g3 * g4;
+    float nb = bx * bx + by * by + bz * bz;
+    bool s1 = nb > nn;
+    cxv = self(s1, bx, cxv); cyv = self(s1, by, cyv); czv = self(s1, bz, czv); nn = self(s1, nb, nn);
+    float ex = m11 * m22 - g5 * g5, ey = g5 * g4 - g3 * m22, ez = g3 * g5 - m11 * g4;
+    float ne = ex * ex + ey * ey + ez * ez;
+    bool s2 = ne > nn;
+    cxv = self(s2, ex, cxv); cyv = self(s2, ey, cyv); czv = self(s2, ez, czv); nn = self(s2, ne, nn);
+  }
+  bool ok = (nn > 1e-30f) & !iso;
+  float vx = self(ok, cxv, 1.f), vy = self(ok, cyv, 0.f), vz = self(ok, czv, 0.f);
+  nrm3(vx, vy, vz);
+  float ax = fabsf(vx), ay = fabsf(vy), az = fabsf(vz);
+  bool k1 = ay < ax, k2 = az < self(k1, ay, ax);
+  float ex = self(k1 | k2, 0.f, 1.f), ey = self(k1 & !k2, 1.f, 0.f), ez = self(k2, 1.f, 0.f);
+  float vk = ex * vx + ey * vy + ez * vz;
+  float ux = ex - vk * vx, uy = ey - vk * vy, uz = ez - vk * vz;
+  nrm3(ux, uy, uz);
+  float wx = vy * uz - vz * uy, wy = vz * ux - vx * uz, wz = vx * uy - vy * ux;
+  // FP64: quotients in the shifted deviator Ds = D + s I, s = root * dsc / 2
+  double s = sel(iso, 0.0, (double)sh * dsc * 0.5);
+  double e0 = d0 + s, e1 = d1 + s, e2 = d2 + s, o3 = v[3], o4 = v[4], o5 = v[5];
+  double Vx = vx, Vy = vy, Vz = vz, Ux = ux, Uy = uy, Uz = uz, Wx = wx, Wy = wy, Wz = wz;
+  double Dvx = e0 * Vx + o3 * Vy + o4 * Vz, Dvy = o3 * Vx + e1 * Vy + o5 * Vz, Dvz = o4 * Vx + o5 * Vy + e2 * Vz;
+  double Dux = e0 * Ux + o3 * Uy + o4 * Uz, Duy = o3 * Ux + e1 * Uy + o5 * Uz, Duz = o4 * Ux + o5 * Uy + e2 * Uz;
+  double Dwx = e0 * Wx + o3 * Wy + o4 * Wz, Dwy = o3 * Wx + e1 * Wy + o5 * Wz, Dwz = o4 * Wx + o5 * Wy + e2 * Wz;
+  double qv = Vx * Dvx + Vy * Dvy + Vz * Dvz, nv = Vx * Vx + Vy * Vy + Vz * Vz;
+  double b11 = Ux * Dux + Uy * Duy + Uz * Duz, b12 = Ux * Dwx + Uy * Dwy + Uz * Dwz;
+  double b22 = Wx * Dwx + Wy * Dwy + Wz * Dwz;
+  double uu = Ux * Ux + Uy * Uy + Uz * Uz, uw = Ux * Wx + Uy * Wy + Uz * Wz, ww = Wx * Wx + Wy * Wy + Wz * Wz;
+  // FP32 Jacobi rotation of the pair from the FP64 block (its entries are of the size of the pair's gap)
+  float jx = (float)(b11 - b22), jy = (float)(b12 + b12), jr = sqrtf(jx * jx + jy * jy);
+  bool jz = !(jr > 0.f), jpos = jx >= 0.f;
+  float jrs = self(jz, 1.f, jr);
+  float big = sqrtf((jrs + fabsf(jx)) / (2.f * jrs)), sml = jy / (2.f * jrs * big);
+  float sgn = self(jy >= 0.f, 1.f, -1.f);
+  float cs = self(jz, 1.f, self(jpos, big, sgn * sml)), sn = self(jz, 0.f, self(jpos, sml, sgn * big));
+  double C = cs, S = sn, CC = C * C, SS = S * S, CS2 = 2.0 * (C * S);
+  double n1 = CC * uu + CS2 * uw + SS * ww - 1.0, n2 = SS * uu - CS2 * uw + CC * ww - 1.0, n0 = nv - 1.0;
+  double t0 = qv * (1.0 - n0 + n0 * n0);
+  double t1 = (CC * b11 + CS2 * b12 + SS * b22) * (1.0 - n1 + n1 * n1);
+  double t2 = (SS * b11 - CS2 * b12 + CC * b22) * (1.0 - n2 + n2 * n2);
+  E.xd[0] = t0 - s; E.xd[1] = t1 - s; E.xd[2] = t2 - s;
+  E.lam[0] = m + E.xd[0]; E.lam[1] = m + E.xd[1]; E.lam[2] = m + E.xd[2];
+  E.m = m;
+  float r1x = cs * ux + sn * wx, r1y = cs * uy + sn * wy, r1z = cs * uz + sn * wz;
+  float r2x = cs * wx - sn * ux, r2y = cs * wy - sn * uy, r2z = cs * wz - sn * uz;
+  // one Newton-Schulz step V <- V (3 I - V^T V) / 2 with the Gram matrix in FP64: the FP32 vectors come out
+  // orthonormal to the rounding of their components (an FP32 Gram matrix would leave its own rounding in them)
+  double R1x = r1x, R1y = r1y, R1z = r1z, R2x = r2x, R2y = r2y, R2z = r2z;
+  float e00 = (float)(n0 * 0.5), e11 = (float)((R1x * R1x + R1y * R1y + R1z * R1z - 1.0) * 0.5);
+  float e22 = (float)((R2x * R2x + R2y * R2y + R2z * R2z - 1.0) * 0.5);
+  float e01 = (float)((Vx * R1x + Vy * R1y + Vz * R1z) * 0.5), e02 = (float)((Vx * R2x + Vy * R2y + Vz * R2z) * 0.5);
+  float e12 = (float)((R1x * R2x + R1y * R2y + R1z * R2z) * 0.5);
+  float c0[3] = {vx, vy, vz}, c1[3] = {r1x, r1y, r1z}, c2[3] = {r2x, r2y, r2z};
+  float nanv = __int_as_float(0x7FC00000);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    E.V[i][0] = self(bad, nanv, c0[i] - (c0[i] * e00 + c1[i] * e01 + c2[i] * e02));
+    E.V[i][1] = self(bad, nanv, c1[i] - (c0[i] * e01 + c1[i] * e11 + c2[i] * e12));
+    E.V[i][2] = self(bad, nanv, c2[i] - (c0[i] * e02 + c1[i] * e12 + c2[i] * e22));
+  }
 }
 
 constexpr int SMFX_TPB = 64;  // matrices per CTA of the standalone kernel
@@ -166,21 +267,44 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
 #pragma unroll
       for (int k = 0; k < 6; k++) v[k] = xi[k];
     }
-    SmfEig E;
-    smf_eigsys<KIND>(v, E);
-    float fl[3], V[3][3];
+    SmfEigM E;
+    smf_eigsys_mixed<KIND>(v, E);
+    // sort ascending (FP64 keys), so that every divided difference below has a static ordering
+    double lam[3] = {E.lam[0], E.lam[1], E.lam[2]}, xd[3] = {E.xd[0], E.xd[1], E.xd[2]};
+    float V[3][3];
 #pragma unroll
-    for (int i = 0; i < 3; i++) {
-      fl[i] = fun_f<KIND>((float)E.lam[i], C.al);
+    for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int j = 0; j < 3; j++) V[i][j] = (float)E.V[i][j];
+      for (int j = 0; j < 3; j++) V[i][j] = E.V[i][j];
+#pragma unroll
+    for (int st = 0; st < 3; st++) {
+      const int a = st == 1 ? 1 : 0, b = a + 1;
+      bool sw = lam[b] < lam[a];
+      double la = lam[a], lb = lam[b], xa = xd[a], xb = xd[b];
+      lam[a] = sel(sw, lb, la); lam[b] = sel(sw, la, lb);
+      xd[a] = sel(sw, xb, xa); xd[b] = sel(sw, xa, xb);
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+        float va = V[r][a], vb = V[r][b];
+        V[r][a] = self(sw, vb, va); V[r][b] = self(sw, va, vb);
+      }
     }
+    if (KIND == POW || KIND == SQRT) {  // f, f' and the divided differences of powers see max(lambda, 0)
+#pragma unroll
+      for (int i = 0; i < 3; i++) lam[i] = sel(lam[i] > 0.0, lam[i], 0.0);
+    }
+    // eigenvalues and their differences, rounded to FP32 once
+    float lf[3] = {(float)lam[0], (float)lam[1], (float)lam[2]};
+    float d10 = (float)(lam[1] - lam[0]), d21 = (float)(lam[2] - lam[1]), d20 = (float)(lam[2] - lam[0]);
+    float fl[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) fl[i] = fun_f<KIND>(lf[i], C.al);
     if (KIND == LOG) {
-      const float mf = (float)E.m, lms = logf((float)(E.m * E.sig));
+      float mf = (float)E.m, lms = logf(mf);
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        const float xd = (float)E.xd[i];
-        fl[i] = self(fabsf(xd) <= 0.5f * mf, lms + log1pf(xd / mf), fl[i]);
+        float x = (float)xd[i];
+        fl[i] = self(fabsf(x) <= 0.5f * mf, lms + log1pf(x / mf), fl[i]);
       }
     }
     float Fv[6];
@@ -197,11 +321,11 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
       for (int s = 0; s < 6; s++) sF[tid * 6 + s] = Fv[s];
     }
     if (ORDER >= 1) {
-      const double *lam = E.lam;
-      const float D01 = dd1_f<KIND>(lam[0], lam[1], fl[0], fl[1], C), D02 = dd1_f<KIND>(lam[0], lam[2], fl[0], fl[2], C);
-      const float D12 = dd1_f<KIND>(lam[1], lam[2], fl[1], fl[2], C);
-      const float D00 = deriv_f<KIND>(lam[0], fl[0], C), D11 = deriv_f<KIND>(lam[1], fl[1], C);
-      const float D22 = deriv_f<KIND>(lam[2], fl[2], C);
+      const float D01 = dd1s_f<KIND>(lf[0], lf[1], d10, fl[0], fl[1], C);
+      const float D02 = dd1s_f<KIND>(lf[0], lf[2], d20, fl[0], fl[2], C);
+      const float D12 = dd1s_f<KIND>(lf[1], lf[2], d21, fl[1], fl[2], C);
+      const float D00 = deriv_f<KIND>(lf[0], fl[0], C), D11 = deriv_f<KIND>(lf[1], fl[1], C);
+      const float D22 = deriv_f<KIND>(lf[2], fl[2], C);
       float P[6][3];
 #pragma unroll
       for (int s6 = 0; s6 < 6; s6++)
@@ -242,15 +366,16 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
       }
       if (ORDER >= 2) {
         float D2[3][3][3];
+        const float dd[3][3] = {{0.f, d10, d20}, {0.f, 0.f, d21}, {0.f, 0.f, 0.f}};
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
           for (int j = i; j < 3; j++)
 #pragma unroll
             for (int l = j; l < 3; l++) {
-              const float d = (i == j && j == l) ? dd2_same_f<KIND>(lam[i], fl[i], Dm[i][i], C)
-                                                 : dd2_f<KIND>(lam[i], lam[j], lam[l], fl[i], fl[j], fl[l], Dm[i][j],
-                                                               Dm[i][l], Dm[j][l], C);
+              const float d = (i == j && j == l)
+                                  ? dd2_same_f<KIND>(lf[i], fl[i], Dm[i][i], C)
+                                  : dd2s_f<KIND>(lf[j], lf[l], fl[j], Dm[i][j], Dm[j][l], dd[i][j], dd[j][l], dd[i][l], C);
               D2[i][j][l] = D2[i][l][j] = D2[j][i][l] = D2[j][l][i] = D2[l][i][j] = D2[l][j][i] = d;
             }
         float Tv[56];
