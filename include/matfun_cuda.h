@@ -116,6 +116,25 @@ int smf_cuda_eval_host(int kind, double alpha, int64_t n, const double *v, doubl
 int smf_cuda_eval_matrix_host(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H);
 int gmf_cuda_eval_host(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H);
 
+/* XLA FFI custom-call handlers registered by matfun.jax for the CUDA platform (reference:
+ * cuda/src/matfun_cuda.cu:245-261, bound by name in python/src/matfun/jax.py:66-87 as targets matfun_value,
+ * matfun_value_jac, matfun_value_jac_hess, matfun_matrix_value*, matfun_gen_value*).  Argument: XLA's call frame
+ * (XLA FFI C API 0.1); result: NULL on success, else an XLA error created through the frame's API.  On XLA's stream:
+ * input x (F64, (..., 6) Voigt or (..., 3, 3)), results F, (F, J) or (F, J, H) as F64 buffers, attributes kind
+ * (int64) and alpha (double). */
+void *SmfValueCuda(void *call_frame);
+void *SmfValueJacCuda(void *call_frame);
+void *SmfValueJacHessCuda(void *call_frame);
+void *SmfMatrixValueCuda(void *call_frame);
+void *SmfMatrixValueJacCuda(void *call_frame);
+void *SmfMatrixValueJacHessCuda(void *call_frame);
+void *GmfValueCuda(void *call_frame);
+void *GmfValueJacCuda(void *call_frame);
+void *GmfValueJacHessCuda(void *call_frame);
+
+/* XLA FFI API version the handlers implement, major * 1000 + minor (reference: cuda/src/matfun_cuda.cu:265) */
+int smf_xla_ffi_api_version(void);
+
 /* Diagnostic (no counterpart in the reference): the measured FP64 fused-multiply-add throughput of the current GPU
  * in TFLOP/s, the bound of the FP64 kernels of this library.  Returns 0, or -1 / -2 like the entry points above. */
 int matfun_cuda_fp64_peak(double *tflops);

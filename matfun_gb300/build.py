@@ -123,7 +123,15 @@ def build_oracle():
     return lib
 
 
-def build_reference_oracle(ref="/root/reference"):
+REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root():
+    """the reference source tree, where it is present (the build host; not the GPU hosts)"""
+    return REFERENCE_ROOT if os.path.isdir(os.path.join(REFERENCE_ROOT, "c", "src")) else None
+
+
+def build_reference_oracle(ref=REFERENCE_ROOT):
     """the reference's own CPU library (oracle/_ref/libmatfun_ref.so) and its CUDA kernels as an sm_103a cubin
     (oracle/_ref/matfun_cuda_ref.cubin), only where the reference sources are present"""
     if not os.path.isdir(os.path.join(ref, "c", "src")):

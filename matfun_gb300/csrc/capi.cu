@@ -18,12 +18,11 @@ bool bad_args(int kind, double alpha, int64_t n, const double *x, const double *
 }
 
 int smf_call(int kind, double alpha, int64_t n, const double *x, bool mat, double *F, double *J, double *H,
-             void *stream) {
+             cudaStream_t st, cudaError_t *err) {
   if (bad_args(kind, alpha, n, x, F, J, H)) return -1;
   if (kind != SMF_POW) alpha = kind == SMF_SQRT ? 0.5 : 0.0;
   if (n == 0) return 0;
   if (n > SMF_MAX_N) return -2;
-  const cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;
   switch (kind) {
     case SMF_EXP: e = mf::smf_launch_exp(alpha, n, x, mat, F, J, H, st); break;
@@ -31,36 +30,49 @@ int smf_call(int kind, double alpha, int64_t n, const double *x, bool mat, doubl
     case SMF_SQRT: e = mf::smf_launch_sqrt(alpha, n, x, mat, F, J, H, st); break;
     default: e = mf::smf_launch_pow(alpha, n, x, mat, F, J, H, st); break;
   }
+  if (err) *err = e;
   return e == cudaSuccess ? 0 : -2;
 }
 
-}  // namespace
-
-extern "C" int smf_cuda_eval(int kind, double alpha, int64_t n, const double *v, double *F, double *J, double *H,
-                             void *stream) {
-  return smf_call(kind, alpha, n, v, false, F, J, H, stream);
-}
-
-extern "C" int smf_cuda_eval_matrix(int kind, double alpha, int64_t n, const double *A, double *F, double *J,
-                                    double *H, void *stream) {
-  return smf_call(kind, alpha, n, A, true, F, J, H, stream);
-}
-
-extern "C" int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H,
-                             void *stream) {
+int gmf_call(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H, cudaStream_t st,
+             cudaError_t *err) {
   if (bad_args(kind, alpha, n, A, F, J, H)) return -1;
   if (kind == SMF_SQRT) kind = SMF_POW, alpha = 0.5;
   if (kind != SMF_POW) alpha = 0.0;
   if (n == 0) return 0;
   if (n > GMF_MAX_N) return -2;
-  const cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;
   switch (kind) {
     case SMF_EXP: e = mf::gmf_launch_exp(alpha, n, A, F, J, H, st); break;
     case SMF_LOG: e = mf::gmf_launch_log(alpha, n, A, F, J, H, st); break;
     default: e = mf::gmf_launch_pow(alpha, n, A, F, J, H, st); break;
   }
+  if (err) *err = e;
   return e == cudaSuccess ? 0 : -2;
+}
+
+}  // namespace
+
+int mf::eval_f64(int family, int kind, double alpha, int64_t n, const double *x, double *F, double *J, double *H,
+                 cudaStream_t st, cudaError_t *err) {
+  if (err) *err = cudaSuccess;
+  return family == 2 ? gmf_call(kind, alpha, n, x, F, J, H, st, err)
+                     : smf_call(kind, alpha, n, x, family == 1, F, J, H, st, err);
+}
+
+extern "C" int smf_cuda_eval(int kind, double alpha, int64_t n, const double *v, double *F, double *J, double *H,
+                             void *stream) {
+  return mf::eval_f64(0, kind, alpha, n, v, F, J, H, (cudaStream_t)stream, nullptr);
+}
+
+extern "C" int smf_cuda_eval_matrix(int kind, double alpha, int64_t n, const double *A, double *F, double *J,
+                                    double *H, void *stream) {
+  return mf::eval_f64(1, kind, alpha, n, A, F, J, H, (cudaStream_t)stream, nullptr);
+}
+
+extern "C" int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H,
+                             void *stream) {
+  return mf::eval_f64(2, kind, alpha, n, A, F, J, H, (cudaStream_t)stream, nullptr);
 }
 
 namespace {

@@ -20,7 +20,7 @@ MF_GMF_DECL(exp)
 MF_GMF_DECL(log)
 MF_GMF_DECL(pow)
 #undef MF_GMF_DECL
-// mixed precision (FP32 storage, FP32 bulk arithmetic, FP64 eigensystem), symmetric family
+// mixed precision (FP32 storage, FP32 bulk arithmetic, FP64 deviator and Rayleigh quotients), symmetric family
 #define MF_SMFX_DECL(k)                                                                                            \
   cudaError_t smf_mixed_launch_##k(double al, int64_t n, const float *x, bool mat, float *F, float *J, float *H, \
                                    cudaStream_t st);
@@ -34,4 +34,8 @@ cudaError_t gmf_adjoint_launch(int kind, double al, int64_t n, const double *A, 
                                double *F, double *Abar, double *JV, double *HWV, cudaStream_t st);
 cudaError_t smf_adjoint_launch(int kind, double al, int64_t n, const double *A, const double *W, const double *V,
                                double *F, double *Abar, double *JV, double *HWV, cudaStream_t st);
+// the three FP64 entry points by family (0 smf Voigt, 1 smf matrix, 2 gmf) with the reference's argument checks and
+// return codes (0, -1, -2); *err (optional) receives the CUDA error of a failed launch (capi.cu)
+int eval_f64(int family, int kind, double alpha, int64_t n, const double *x, double *F, double *J, double *H,
+             cudaStream_t st, cudaError_t *err);
 }  // namespace mf
