@@ -176,6 +176,40 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def _mixed_pair(x32, nf, fn32, fn64, steps, dev):
+    """time the FP32 entry point and the FP64 one (log, order 2) on the same values; max relative error of the FP32
+    results against the FP64 ones (max-norm per output array) on a sample of 65536 matrices"""
+    import torch
+    n = x32.shape[0]
+    d32 = x32.to(dev)
+    d64 = d32.double()
+    outs = {}
+    for tag, dt, x, fn in (("f32", torch.float32, d32, fn32), ("f64", torch.float64, d64, fn64)):
+        F = torch.empty((n, nf), dtype=dt, device=dev)
+        J = torch.empty((n, nf ** 2), dtype=dt, device=dev)
+        H = torch.empty((n, nf ** 3), dtype=dt, device=dev)
+        call = lambda: fn(1, 0.0, n, x.data_ptr(), F.data_ptr(), J.data_ptr(), H.data_ptr(), None)
+        for _ in range(2):
+            assert call() == 0
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            call()
+        e1.record()
+        e1.synchronize()
+        outs[tag] = (e0.elapsed_time(e1) / steps, F, J, H)
+        del F, J, H
+    idx = torch.arange(0, n, max(1, n // 65536), device=dev)
+    err = {}
+    for k, name in ((1, "F"), (2, "J"), (3, "H")):
+        a, b = outs["f32"][k][idx].double(), outs["f64"][k][idx]
+        both = torch.isnan(a) & torch.isnan(b)
+        d = torch.where(both, torch.zeros_like(a), (a - b).abs())
+        err[name] = float(d.max() / torch.nan_to_num(b, nan=0.0).abs().max())
+    return outs["f32"][0], outs["f64"][0], err, int(idx.numel())
+
+
 def mixed_vs_fp64(lib, args, dev, hbm):
     """smf log order 2 (Voigt) on the C2 workload (n = 2^24 SPD, condition number log-uniform in [1, 1e6], smallest
     eigenvalue gap log-uniform in [1e-12, 1], stored as FP32): the mixed-precision path (FP32 storage and bulk
@@ -185,38 +219,31 @@ def mixed_vs_fp64(lib, args, dev, hbm):
 
     from matfun_gb300 import workloads as w
     n = args.mixed_n
-    X32 = w.c2_smf_spd(n, seed=2)
-    d32 = torch.from_numpy(X32).to(dev)
-    d64 = d32.double()
-    outs = {}
-    for tag, dt, x, fn in (("f32", torch.float32, d32, lib.smf_cuda_eval_f32), ("f64", torch.float64, d64, lib.smf_cuda_eval)):
-        F = torch.empty((n, 6), dtype=dt, device=dev)
-        J = torch.empty((n, 36), dtype=dt, device=dev)
-        H = torch.empty((n, 216), dtype=dt, device=dev)
-        call = lambda: fn(1, 0.0, n, x.data_ptr(), F.data_ptr(), J.data_ptr(), H.data_ptr(), None)
-        for _ in range(2):
-            assert call() == 0
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(args.mixed_steps):
-            call()
-        e1.record()
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / args.mixed_steps
-        outs[tag] = (ms, F, J, H)
-    idx = torch.arange(0, n, max(1, n // 65536), device=dev)
-    err = {}
-    for k, name in ((1, "F"), (2, "J"), (3, "H")):
-        a, b = outs["f32"][k][idx].double(), outs["f64"][k][idx]
-        err[name] = float((a - b).abs().max() / b.abs().max())
-    ms32, ms64 = outs["f32"][0], outs["f64"][0]
+    x32 = torch.from_numpy(w.c2_smf_spd(n, seed=2))
+    ms32, ms64, err, ns = _mixed_pair(x32, 6, lib.smf_cuda_eval_f32, lib.smf_cuda_eval, args.mixed_steps, dev)
     bytes32 = (6 + 6 + 36 + 216) * 4
     return {"workload": f"smf log order 2, Voigt, n={n} SPD, condition log-uniform [1,1e6], smallest gap "
                         "log-uniform [1e-12,1], FP32 storage (C2)",
             "mixed_matrices_per_s": n / (ms32 * 1e-3), "fp64_matrices_per_s": n / (ms64 * 1e-3),
             "speedup_vs_fp64": ms64 / ms32, "mixed_ms": ms32, "fp64_ms": ms64,
-            "max_rel_err_vs_fp64": err, "err_sample": int(idx.numel()),
+            "max_rel_err_vs_fp64": err, "err_sample": ns,
+            "mixed_hbm_frac": bytes32 * n / (ms32 * 1e-3) / 1e9 / hbm, "bytes_per_matrix_fp32": bytes32}
+
+
+def mixed_gmf_vs_fp64(lib, args, dev, hbm):
+    """gmf log order 2 on the C1 workload (n = 2^20, the four groups), stored as FP32: the mixed-precision gmf path
+    (FP64 spectral analysis and series, FP32 storage and J / H assembly) against the FP64 path on the same values"""
+    import torch
+
+    from matfun_gb300 import workloads as w
+    n = args.gmf_mixed_n
+    x32 = torch.from_numpy(w.c1_gmf_groups(n, seed=1).astype(np.float32).reshape(n, 9))
+    ms32, ms64, err, ns = _mixed_pair(x32, 9, lib.gmf_cuda_eval_f32, lib.gmf_cuda_eval, args.mixed_steps, dev)
+    bytes32 = (9 + 9 + 81 + 729) * 4
+    return {"workload": f"gmf log order 2, n={n} general matrices (C1 groups), FP32 storage",
+            "mixed_matrices_per_s": n / (ms32 * 1e-3), "fp64_matrices_per_s": n / (ms64 * 1e-3),
+            "speedup_vs_fp64": ms64 / ms32, "mixed_ms": ms32, "fp64_ms": ms64,
+            "max_rel_err_vs_fp64": err, "err_sample": ns,
             "mixed_hbm_frac": bytes32 * n / (ms32 * 1e-3) / 1e9 / hbm, "bytes_per_matrix_fp32": bytes32}
 
 
@@ -449,6 +476,7 @@ def run_ours(args, rank, world, local):
     del dA, dF, dJ, dH
     if rank == 0 and not args.no_mixed:
         out["mixed"] = mixed_vs_fp64(lib, args, dev, hbm)
+        out["mixed_gmf"] = mixed_gmf_vs_fp64(lib, args, dev, hbm)
     if rank == 0 and not args.no_adjoint:
         out["adjoint"] = adjoint_vs_materialised(lib, args, dev)
     if rank == 0 and not args.no_batched:
@@ -483,6 +511,7 @@ def main():
     ap.add_argument("--adj-n", type=int, default=1 << 22)
     ap.add_argument("--mixed-n", type=int, default=1 << 24)
     ap.add_argument("--mixed-steps", type=int, default=5)
+    ap.add_argument("--gmf-mixed-n", type=int, default=1 << 20)
     args = ap.parse_args()
     args.alpha = 0.5 if args.kind == "sqrt" else 0.0
     if args.kind == "sqrt":

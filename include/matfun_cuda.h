@@ -46,16 +46,19 @@ int smf_cuda_eval_matrix(int kind, double alpha, int64_t n, const double *A, dou
 /* replaces gmf_cuda_eval, cuda/include/matfun/matfun_cuda.h:22 (cuda/src/matfun_cuda.cu:194-197) */
 int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H, void *stream);
 
-/* Mixed precision (spec extension; no counterpart in the reference): FP32 arrays in and out, the bulk of the
- * arithmetic in FP32, FP64 kept for the eigensystem and for the eigenvalue differences of the near-coalescent
- * divided-difference branches.  Same layouts, kinds and return codes as smf_cuda_eval / smf_cuda_eval_matrix.
- * Max relative error (max-norm per call) against the FP64 results: <= 1e-6 on the tested workloads, stated per kind
- * and order in the design doc. */
+/* Mixed precision (no counterpart in the reference): FP32 arrays in and out, the bulk of the arithmetic in FP32.
+ * smf: FP64 is kept for the deviator, the Rayleigh quotients that give the eigenvalues and the eigenvalue
+ * differences of the near-coalescent divided-difference branches.  gmf: the spectral analysis (closed-form roots,
+ * refinement, branch-cut pair, groups), the confluent series and the residues run in FP64; storage and the J / H
+ * assembly in FP32.  Same layouts, kinds and return codes as smf_cuda_eval / smf_cuda_eval_matrix / gmf_cuda_eval.
+ * Max relative error (max-norm per output array) against the FP64 results on the tested workloads: <= 1e-6 for smf;
+ * gmf: see its tests (stated per kind and order). */
 int smf_cuda_eval_f32(int kind, double alpha, int64_t n, const float *v, float *F, float *J, float *H, void *stream);
 int smf_cuda_eval_matrix_f32(int kind, double alpha, int64_t n, const float *A, float *F, float *J, float *H,
                              void *stream);
+int gmf_cuda_eval_f32(int kind, double alpha, int64_t n, const float *A, float *F, float *J, float *H, void *stream);
 
-/* Adjoints (spec extension; no counterpart in the reference): contractions of J and H with directions, without
+/* Adjoints (no counterpart in the reference): contractions of J and H with directions, without
  * forming J or H.  Matrix layout (n, 3, 3) for every array; W, V device arrays of directions; outputs, each optional:
  *   F    = f(A)
  *   Abar = J^T W    (Abar_cd = sum_ab W_ab dF_ab/dA_cd: the gradient of sum <W, f(A)>)     needs W
@@ -68,13 +71,13 @@ int smf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const d
 int gmf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const double *W, const double *V, double *F,
                      double *Abar, double *JV, double *HWV, void *stream);
 
-/* Batched evaluation (spec extension; no counterpart in the reference): many requests of uneven size and
+/* Batched evaluation (no counterpart in the reference): many requests of uneven size and
  * mixed family / kind / order / precision in ONE launch of a persistent kernel.  A request: */
 typedef struct mf_request {
   int32_t family;  /* 0: smf Voigt (smf_cuda_eval), 1: smf matrix (smf_cuda_eval_matrix), 2: gmf (gmf_cuda_eval) */
   int32_t kind;    /* SMF_EXP, SMF_LOG, SMF_POW, SMF_SQRT */
   int32_t order;   /* 0: F; 1: F, J; 2: F, J, H */
-  int32_t dtype;   /* 0: FP64 arrays; 1: FP32 arrays (the mixed-precision path, smf only) */
+  int32_t dtype;   /* 0: FP64 arrays; 1: FP32 arrays (the mixed-precision paths) */
   double alpha;    /* exponent of SMF_POW */
   int64_t n;       /* matrices */
   const void *x;   /* device input, layouts as above */

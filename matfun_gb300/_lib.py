@@ -27,6 +27,7 @@ SIGNATURES = {
     "gmf_cuda_eval": (ctypes.c_int, _EVAL),
     "smf_cuda_eval_f32": (ctypes.c_int, _EVAL),
     "smf_cuda_eval_matrix_f32": (ctypes.c_int, _EVAL),
+    "gmf_cuda_eval_f32": (ctypes.c_int, _EVAL),
     "smf_cuda_adjoint": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [ctypes.c_void_p] * 8),
     "gmf_cuda_adjoint": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [ctypes.c_void_p] * 8),
     "smf_cuda_eval_host": (ctypes.c_int, _EVAL[:-1]),

@@ -18,7 +18,7 @@ FAMILIES = {"smf_voigt": 0, "smf": 1, "gmf": 2}
 
 class BatchRequest:
     """one request with its device output tensors; family "smf_voigt" (Voigt vectors), "smf" (symmetric matrices)
-    or "gmf"; FP32 input selects the mixed-precision path (smf only)"""
+    or "gmf"; FP32 input selects the mixed-precision path"""
 
     def __init__(self, family, kind, x, order=0, alpha=None):
         if family not in FAMILIES:

@@ -3,8 +3,9 @@
 // The host cuts every request into tiles of 128 matrices and writes a table (requests, their coefficient blocks,
 // the prefix sum of their tile counts) into device memory.  One persistent kernel (grid = SMs x CTAs per SM) then
 // pulls tiles from a global atomic cursor until all are taken; each tile runs the same tile routine as the
-// standalone kernel of its request (smf FP64 / mixed FP32 in either layout, gmf FP64).  There is no waiting between
-// CTAs: a CTA only increments the cursor and stops when it passes the tile count, so no wait can hang.
+// standalone kernel of its request (smf FP64 / mixed FP32 in either layout, gmf FP64 / mixed FP32).  There is no
+// waiting between CTAs: a CTA only increments the cursor and stops when it passes the tile count, so no wait can
+// hang.
 //
 // Two ways to run it:
 //   matfun_cuda_batched(requests, count, stream)          table in a per-device cached buffer, uploaded on `stream`
@@ -38,20 +39,22 @@ namespace {
     case 3: MF_SMF_CALL(pfx, 3, suf) break;                                              \
     default: MF_SMF_CALL(pfx, 2, suf) break;                                             \
   }
-#define MF_GMF_CALL(K)                                                                  \
+#define MF_GMF_CALL(pfx, K)                                                             \
   switch (R.order) {                                                                    \
-    case 2: bt_gmf_##K##_2(base, cnt, R, coef, smem); break;                             \
-    case 1: bt_gmf_##K##_1(base, cnt, R, coef, smem); break;                             \
-    default: bt_gmf_##K##_0(base, cnt, R, coef, smem); break;                            \
+    case 2: pfx##_##K##_2(base, cnt, R, coef, smem); break;                              \
+    case 1: pfx##_##K##_1(base, cnt, R, coef, smem); break;                              \
+    default: pfx##_##K##_0(base, cnt, R, coef, smem); break;                             \
+  }
+#define MF_GMF_KIND(pfx)                \
+  switch (R.kind) {                     \
+    case 0: MF_GMF_CALL(pfx, 0) break;  \
+    case 1: MF_GMF_CALL(pfx, 1) break;  \
+    default: MF_GMF_CALL(pfx, 2) break; \
   }
 
 __device__ void run_tile(const DevReq &R, long long base, int cnt, const unsigned char *coef, unsigned char *smem) {
   if (R.family == 2) {
-    switch (R.kind) {
-      case 0: MF_GMF_CALL(0) break;
-      case 1: MF_GMF_CALL(1) break;
-      default: MF_GMF_CALL(2) break;
-    }
+    if (R.dtype == 0) { MF_GMF_KIND(bt_gmf) } else { MF_GMF_KIND(bt_gmf32) }
   } else if (R.family == 1) {
     if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, m) } else { MF_SMF_KIND(bt_smf32, m) }
   } else {
@@ -125,7 +128,7 @@ int build_table(const mf_request *req, int count, Table &T) {
     int kind = r.kind;
     double al = r.alpha;
     if (r.family < 0 || r.family > 2 || kind < SMF_EXP || kind > SMF_SQRT || r.order < 0 || r.order > 2 ||
-        r.n < 0 || (r.dtype != 0 && r.dtype != 1) || (r.family == 2 && r.dtype != 0) ||
+        r.n < 0 || (r.dtype != 0 && r.dtype != 1) ||
         (kind == SMF_POW && !(al > 0)))
       return -1;
     if (r.n > 0 && (!r.x || !r.F || (r.order >= 1 && !r.J) || (r.order >= 2 && !r.H))) return -1;
@@ -155,7 +158,7 @@ int build_table(const mf_request *req, int count, Table &T) {
     it.tiles = (r.n + BT_TPB - 1) / BT_TPB;
     // relative work per matrix (measured orders of magnitude): gmf order 2 >> smf order 2 >> first orders
     const double per = (r.family == 2 ? 4.0 : 1.0) * (r.order == 2 ? 4.0 : (r.order == 1 ? 1.5 : 1.0)) *
-                       (r.dtype == 1 ? 0.3 : 1.0);
+                       (r.dtype == 1 ? (r.family == 2 ? 0.8 : 0.3) : 1.0);
     it.work = per * (double)r.n;
     items.push_back(std::move(it));
   }

@@ -24,13 +24,14 @@ template <int ORDER, bool MAT>
 using SmfxS = SmfxTileSmem<ORDER, MAT, BT_TPB>;
 
 #define MF_BT_SIG (long long base, int cnt, const DevReq &R, const unsigned char *coef, unsigned char *smem)
-// smf FP64 / FP32 (kind 0..3, order 0..2, layout V / M) and gmf FP64 (kind 0..2, order 0..2)
+// smf FP64 / FP32 (kind 0..3, order 0..2, layout V / M) and gmf FP64 / FP32 (kind 0..2, order 0..2)
 #define MF_BT_DECL(name) extern __device__ __noinline__ void name MF_BT_SIG;
 #define MF_BT_SMF(pfx, K, O) MF_BT_DECL(pfx##_##K##_##O##_v) MF_BT_DECL(pfx##_##K##_##O##_m)
 #define MF_BT_SMF_K(pfx, K) MF_BT_SMF(pfx, K, 0) MF_BT_SMF(pfx, K, 1) MF_BT_SMF(pfx, K, 2)
 MF_BT_SMF_K(bt_smf64, 0) MF_BT_SMF_K(bt_smf64, 1) MF_BT_SMF_K(bt_smf64, 2) MF_BT_SMF_K(bt_smf64, 3)
 MF_BT_SMF_K(bt_smf32, 0) MF_BT_SMF_K(bt_smf32, 1) MF_BT_SMF_K(bt_smf32, 2) MF_BT_SMF_K(bt_smf32, 3)
-#define MF_BT_GMF_K(K) MF_BT_DECL(bt_gmf_##K##_0) MF_BT_DECL(bt_gmf_##K##_1) MF_BT_DECL(bt_gmf_##K##_2)
-MF_BT_GMF_K(0) MF_BT_GMF_K(1) MF_BT_GMF_K(2)
+#define MF_BT_GMF_K(pfx, K) MF_BT_DECL(pfx##_##K##_0) MF_BT_DECL(pfx##_##K##_1) MF_BT_DECL(pfx##_##K##_2)
+MF_BT_GMF_K(bt_gmf, 0) MF_BT_GMF_K(bt_gmf, 1) MF_BT_GMF_K(bt_gmf, 2)
+MF_BT_GMF_K(bt_gmf32, 0) MF_BT_GMF_K(bt_gmf32, 1) MF_BT_GMF_K(bt_gmf32, 2)
 
 }  // namespace mf

@@ -105,6 +105,24 @@ extern "C" int smf_cuda_eval_matrix_f32(int kind, double alpha, int64_t n, const
   return smf_call_f32(kind, alpha, n, A, true, F, J, H, stream);
 }
 
+extern "C" int gmf_cuda_eval_f32(int kind, double alpha, int64_t n, const float *A, float *F, float *J, float *H,
+                                 void *stream) {
+  if (kind < SMF_EXP || kind > SMF_SQRT || n < 0 || (H && !J) || (kind == SMF_POW && !(alpha > 0))) return -1;
+  if (n > 0 && (!A || !F)) return -1;
+  if (kind == SMF_SQRT) kind = SMF_POW, alpha = 0.5;
+  if (kind != SMF_POW) alpha = 0.0;
+  if (n == 0) return 0;
+  if (n > GMF_MAX_N) return -2;
+  const cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  switch (kind) {
+    case SMF_EXP: e = mf::gmf_mixed_launch_exp(alpha, n, A, F, J, H, st); break;
+    case SMF_LOG: e = mf::gmf_mixed_launch_log(alpha, n, A, F, J, H, st); break;
+    default: e = mf::gmf_mixed_launch_pow(alpha, n, A, F, J, H, st); break;
+  }
+  return e == cudaSuccess ? 0 : -2;
+}
+
 namespace {
 int adjoint_call(bool general, int kind, double alpha, int64_t n, const double *A, const double *W, const double *V,
                  double *F, double *Abar, double *JV, double *HWV, void *stream) {

@@ -1,5 +1,6 @@
 // gmf_kernels.cuh -- general family (gmf_cuda_eval): F, J, H of f(A) for general real 3x3 matrices, FP64, matrix
-// layout.  Replaces gmf_eval_kernel of the reference (cuda/src/matfun_cuda.cu:144-190).
+// layout.  Replaces gmf_eval_kernel of the reference (cuda/src/matfun_cuda.cu:144-190).  The same tile with float
+// storage is the mixed-precision form (gmf_cuda_eval_f32): phase A in FP64, phase B and the arrays in FP32.
 //
 // One CTA = 128 matrices (four warps).
 // Phase A: one thread per matrix computes the record of gmf_device.cuh -- F, the real basis r_1, r_2 (r_0 = I) and
@@ -54,13 +55,15 @@ MF_D unsigned short hmap_entry(int w) {
 }
 
 // one tile: matrices base .. base + cnt - 1 by a CTA of GMF_TPB threads (the standalone kernel and the batched
-// persistent kernel run the same code)
-template <int KIND, int ORDER>
-MF_D void gmf_tile(int64_t base, int cnt, const double *__restrict__ A, double *__restrict__ F,
-                   double *__restrict__ J, double *__restrict__ H, const GmfCoef &C, GmfSmem &S) {
+// persistent kernel run the same code).  T is the type of the arrays in HBM and of phase B: double for the FP64
+// path; float for the mixed-precision path, where phase A (spectral analysis, series, residues: the FP64 steps of
+// the method) stays in FP64 and its record -- with the scale factors folded in, in FP64 -- is rounded to FP32 once.
+template <int KIND, int ORDER, typename T = double>
+MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict__ F, T *__restrict__ J,
+                   T *__restrict__ H, const GmfCoef &C, GmfSmem &S) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  for (int e = tid; e < cnt * 9; e += GMF_TPB) S.x[e] = A[base * 9 + e];
+  for (int e = tid; e < cnt * 9; e += GMF_TPB) S.x[e] = (double)A[base * 9 + e];
   if (ORDER >= 2) {  // index tables of phase B
     for (int w = tid; w < 729; w += GMF_TPB) S.hmap[w] = hmap_entry(w);
     for (int t = tid; t < 165; t += GMF_TPB) {
@@ -112,130 +115,128 @@ MF_D void gmf_tile(int64_t base, int cnt, const double *__restrict__ A, double *
 #pragma unroll
     for (int k = 0; k < 9; k++) S.x[mine * 9 + k] = R.F[k];
     if (ORDER >= 1) {
-      double *rc = S.rec + mine * GMF_REC;
+      // the scale factors sc1 / sc2 are folded into D2' / D3' when finite and nonzero; otherwise each output entry
+      // is multiplied by them (keeping the reference's NaN / Inf); rc[34] / rc[35] hold the factor left to apply
+      T *rc = reinterpret_cast<T *>(S.rec) + mine * GMF_REC;
 #pragma unroll
-      for (int k = 0; k < 9; k++) { rc[k] = R.r1[k]; rc[9 + k] = R.r2[k]; }
+      for (int k = 0; k < 9; k++) { rc[k] = (T)R.r1[k]; rc[9 + k] = (T)R.r2[k]; }
+      const bool f1 = isfinite(R.sc1) & (R.sc1 != 0.0);
+      const double s1 = sel(f1, R.sc1, 1.0);
 #pragma unroll
-      for (int k = 0; k < 6; k++) rc[18 + k] = R.D2[k];
+      for (int k = 0; k < 6; k++) rc[18 + k] = (T)(R.D2[k] * s1);
+      rc[34] = (T)sel(f1, 1.0, R.sc1);
       if (ORDER >= 2) {
+        const bool f2 = isfinite(R.sc2) & (R.sc2 != 0.0);
+        const double s2 = sel(f2, R.sc2, 1.0);
 #pragma unroll
-        for (int k = 0; k < 10; k++) rc[24 + k] = R.D3[k];
-        rc[35] = R.sc2;
+        for (int k = 0; k < 10; k++) rc[24 + k] = (T)(R.D3[k] * s2);
+        rc[35] = (T)sel(f2, 1.0, R.sc2);
       }
-      rc[34] = R.sc1;
     }
   }
   __syncthreads();
-  for (int e = tid; e < cnt * 9; e += GMF_TPB) F[base * 9 + e] = S.x[e];
+  for (int e = tid; e < cnt * 9; e += GMF_TPB) F[base * 9 + e] = (T)S.x[e];
   if (ORDER < 1) return;
 
   // ---- phase B: the warp's 32 matrices one after the other
-  double *wk = S.work[warp];
+  T *wk = reinterpret_cast<T *>(S.work[warp]);
   const int m0 = warp * 32, m1 = min(cnt, m0 + 32);  // (phase B keeps the input order)
   for (int mi = m0; mi < m1; mi++) {
-    const double *rc = S.rec + mi * GMF_REC;
-    const double *r1 = rc, *r2 = rc + 9;
-    // J: fold sc1 into D2' when finite and nonzero (else multiply each entry, keeping the reference's NaN / Inf)
+    const T *rc = reinterpret_cast<const T *>(S.rec) + mi * GMF_REC;
+    const T *r1 = rc, *r2 = rc + 9;
     {
-      const double sc1 = rc[34];
-      const bool fold = isfinite(sc1) & (sc1 != 0.0);
-      const double s = sel(fold, sc1, 1.0);
+      const T sc1 = rc[34];
       if (lane < 27) {  // Y2[y][m] = sum_n D2'_mn r_n[y]
         const int y = lane / 3, m = lane % 3;
         const int i0 = m == 0 ? 0 : (m == 1 ? 3 : 4), i1 = m == 0 ? 3 : (m == 1 ? 1 : 5), i2 = m == 0 ? 4 : (m == 1 ? 5 : 2);
-        const double d0 = rc[18 + i0] * s, d1 = rc[18 + i1] * s, d2 = rc[18 + i2] * s;
-        wk[lane] = (y % 4 == 0 ? d0 : 0.0) + d1 * r1[y] + d2 * r2[y];
+        const T d0 = rc[18 + i0], d1 = rc[18 + i1], d2 = rc[18 + i2];
+        wk[lane] = (y % 4 == 0 ? d0 : T(0)) + d1 * r1[y] + d2 * r2[y];
       }
       __syncwarp();
       for (int t = lane; t < 45; t += 32) {  // T4[x, y] = sum_m r_m[x] Y2[y][m], x <= y
         int y = 0;
         while (sym2(0, y + 1) <= t) y++;
         const int x = t - sym2(0, y);
-        const double *yv = wk + 3 * y;
-        wk[54 + t] = (x % 4 == 0 ? yv[0] : 0.0) + r1[x] * yv[1] + r2[x] * yv[2];
+        const T *yv = wk + 3 * y;
+        wk[54 + t] = (x % 4 == 0 ? yv[0] : T(0)) + r1[x] * yv[1] + r2[x] * yv[2];
       }
       __syncwarp();
-      double *o = J + (base + mi) * 81;
+      T *o = J + (base + mi) * 81;
       for (int w = lane; w < 81; w += 32) {
         const int a = w / 27, b = (w / 9) % 3, c = (w / 3) % 3, d = w % 3;
         const int p1 = 3 * a + c, p2 = 3 * d + b;
-        const double v = wk[54 + sym2(min(p1, p2), max(p1, p2))];
-        o[w] = fold ? v : v * sc1;
+        o[w] = wk[54 + sym2(min(p1, p2), max(p1, p2))] * sc1;
       }
       __syncwarp();
     }
     if (ORDER < 2) continue;
     {
-      const double sc2 = rc[35];
-      const bool fold = isfinite(sc2) & (sc2 != 0.0);
-      const double s = sel(fold, sc2, 1.0);
-      const double *d3 = rc + 24;
-      double *Zs = wk, *Ys = wk + 54, *T6 = wk + 54 + 135;
+      const T sc2 = rc[35];
+      const T *d3 = rc + 24;
+      T *Zs = wk, *Ys = wk + 54, *T6 = wk + 54 + 135;
       for (int t = lane; t < 54; t += 32) {  // Z[z][mn] = sum_p D3'_mnp r_p[z]  (mn: 00 01 02 11 12 22)
         const int z = t / 6, mn = t % 6;
         const int mm = mn < 3 ? 0 : (mn < 5 ? 1 : 2), nn = mn < 3 ? mn : (mn < 5 ? mn - 2 : 2);
         const int i0 = sym3(0, mm, nn);
         const int i1 = nn <= 1 ? sym3(mm, nn, 1) : (mm <= 1 ? sym3(mm, 1, nn) : sym3(1, mm, nn));
         const int i2 = sym3(mm, nn, 2);
-        Zs[t] = (z % 4 == 0 ? d3[i0] * s : 0.0) + (d3[i1] * s) * r1[z] + (d3[i2] * s) * r2[z];
+        Zs[t] = (z % 4 == 0 ? d3[i0] : T(0)) + d3[i1] * r1[z] + d3[i2] * r2[z];
       }
       __syncwarp();
       for (int t = lane; t < 135; t += 32) {  // Y[y, z][m] = sum_n Z[z][m, n] r_n[y]
         const unsigned short e = S.ymap[t];
         const int y = e & 15, z = (e >> 4) & 15, m = e >> 8;
-        const double *zz = Zs + 6 * z;
+        const T *zz = Zs + 6 * z;
         const int k0 = m == 0 ? 0 : (m == 1 ? 1 : 2), k1 = m == 0 ? 1 : (m == 1 ? 3 : 4), k2 = m == 0 ? 2 : (m == 1 ? 4 : 5);
-        Ys[t] = (y % 4 == 0 ? zz[k0] : 0.0) + zz[k1] * r1[y] + zz[k2] * r2[y];
+        Ys[t] = (y % 4 == 0 ? zz[k0] : T(0)) + zz[k1] * r1[y] + zz[k2] * r2[y];
       }
       __syncwarp();
       for (int t = lane; t < 165; t += 32) {  // T6[x, y, z] = sum_m r_m[x] Y[y, z][m]
         const unsigned short e = S.t6map[t];
         const int x = e & 15, y = (e >> 4) & 15, z = e >> 8;
-        const double *yv = Ys + 3 * sym2(y, z);
-        T6[t] = (x % 4 == 0 ? yv[0] : 0.0) + r1[x] * yv[1] + r2[x] * yv[2];
+        const T *yv = Ys + 3 * sym2(y, z);
+        T6[t] = (x % 4 == 0 ? yv[0] : T(0)) + r1[x] * yv[1] + r2[x] * yv[2];
       }
       __syncwarp();
-      double *o = H + (base + mi) * 729;
+      T *o = H + (base + mi) * 729;
       for (int w = lane; w < 729; w += 32) {
         const unsigned short e = S.hmap[w];
-        const double v = T6[e & 255] + T6[e >> 8];
-        o[w] = fold ? v : v * sc2;
+        o[w] = (T6[e & 255] + T6[e >> 8]) * sc2;
       }
       __syncwarp();
     }
   }
 }
 
-template <int KIND, int ORDER>
-__global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const double *__restrict__ A, double *__restrict__ F,
-                                                      double *__restrict__ J, double *__restrict__ H,
-                                                      const GmfCoef C) {
+template <int KIND, int ORDER, typename T>
+__global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const T *__restrict__ A, T *__restrict__ F,
+                                                      T *__restrict__ J, T *__restrict__ H, const GmfCoef C) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GmfSmem &S = *reinterpret_cast<GmfSmem *>(smem_raw);
   const int64_t base = (int64_t)blockIdx.x * GMF_TPB;
-  gmf_tile<KIND, ORDER>(base, (int)min((int64_t)GMF_TPB, n - base), A, F, J, H, C, S);
+  gmf_tile<KIND, ORDER, T>(base, (int)min((int64_t)GMF_TPB, n - base), A, F, J, H, C, S);
 }
 
-template <int KIND, int ORDER>
-cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const double *A, double *F, double *J,
-                           double *H, const GmfCoef &C) {
+template <int KIND, int ORDER, typename T>
+cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const T *A, T *F, T *J, T *H,
+                           const GmfCoef &C) {
   static bool attr = false;  // once per instantiation (idempotent; a racing second call sets the same value)
   if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(gmf_kernel<KIND, ORDER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)sizeof(GmfSmem));
+    const cudaError_t e = cudaFuncSetAttribute(gmf_kernel<KIND, ORDER, T>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GmfSmem));
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  gmf_kernel<KIND, ORDER><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C);
+  gmf_kernel<KIND, ORDER, T><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C);
   return cudaGetLastError();
 }
 
-template <int KIND>
-cudaError_t gmf_launch_kind(int order, cudaStream_t st, unsigned blocks, int64_t n, const double *A, double *F,
-                            double *J, double *H, const GmfCoef &C) {
-  if (order == 2) return gmf_launch_one<KIND, 2>(st, blocks, n, A, F, J, H, C);
-  if (order == 1) return gmf_launch_one<KIND, 1>(st, blocks, n, A, F, J, H, C);
-  return gmf_launch_one<KIND, 0>(st, blocks, n, A, F, J, H, C);
+template <int KIND, typename T>
+cudaError_t gmf_launch_kind(int order, cudaStream_t st, unsigned blocks, int64_t n, const T *A, T *F, T *J, T *H,
+                            const GmfCoef &C) {
+  if (order == 2) return gmf_launch_one<KIND, 2, T>(st, blocks, n, A, F, J, H, C);
+  if (order == 1) return gmf_launch_one<KIND, 1, T>(st, blocks, n, A, F, J, H, C);
+  return gmf_launch_one<KIND, 0, T>(st, blocks, n, A, F, J, H, C);
 }
 
 // host: launch constants (series coefficients gmf_kernel.hpp:48-53; the binomial factors of the term bound by the
@@ -260,14 +261,14 @@ inline void gmf_coef(int kind, double al, int order, GmfCoef &C) {
   }
 }
 
-// one kind (instantiated in gmf_<kind>.cu so that the kinds compile in parallel)
-template <int KIND>
-cudaError_t gmf_launch_t(double al, int64_t n, const double *A, double *F, double *J, double *H, cudaStream_t st) {
+// one kind (instantiated in gmf_<kind>.cu and gmf_mixed_<kind>.cu so that they compile in parallel)
+template <int KIND, typename T = double>
+cudaError_t gmf_launch_t(double al, int64_t n, const T *A, T *F, T *J, T *H, cudaStream_t st) {
   const int order = H ? 2 : (J ? 1 : 0);
   GmfCoef C;
   gmf_coef(KIND, al, order, C);
   const unsigned blocks = (unsigned)((n + GMF_TPB - 1) / GMF_TPB);
-  return gmf_launch_kind<KIND>(order, st, blocks, n, A, F, J, H, C);
+  return gmf_launch_kind<KIND, T>(order, st, blocks, n, A, F, J, H, C);
 }
 
 }  // namespace mf

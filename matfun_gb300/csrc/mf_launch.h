@@ -29,6 +29,13 @@ MF_SMFX_DECL(log)
 MF_SMFX_DECL(sqrt)
 MF_SMFX_DECL(pow)
 #undef MF_SMFX_DECL
+// mixed precision, general family: FP32 storage and J / H assembly, FP64 spectral analysis and series
+#define MF_GMFX_DECL(k) \
+  cudaError_t gmf_mixed_launch_##k(double al, int64_t n, const float *A, float *F, float *J, float *H, cudaStream_t st);
+MF_GMFX_DECL(exp)
+MF_GMFX_DECL(log)
+MF_GMFX_DECL(pow)
+#undef MF_GMFX_DECL
 // adjoints (matrix layout): any of F, Abar = J^T W, JV = J V, HWV = W . H . V; kind normalised as above
 cudaError_t gmf_adjoint_launch(int kind, double al, int64_t n, const double *A, const double *W, const double *V,
                                double *F, double *Abar, double *JV, double *HWV, cudaStream_t st);

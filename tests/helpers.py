@@ -33,7 +33,7 @@ def header_functions(path):
     """names of the functions an include/*.h declares"""
     src = open(path).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*([a-z_][a-z_0-9]*)\s*\(", src, flags=re.M)
+    return re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*([A-Za-z_][A-Za-z_0-9]*)\s*\(", src, flags=re.M)
 
 
 def voigt_to_matrix(v):

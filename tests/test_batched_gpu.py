@@ -26,7 +26,7 @@ def mixed_requests(seed, count=40, nmax=3000):
         fam = ["smf_voigt", "smf", "gmf"][i % 3]
         kind = ["exp", "log", "sqrt", "pow"][rng.integers(4)]
         order = int(rng.integers(3))
-        f32 = fam != "gmf" and rng.uniform() < 0.4
+        f32 = rng.uniform() < 0.4
         n = int(rng.integers(1, nmax))
         if fam == "gmf":
             x = w.c1_gmf_groups(max(n, 4), seed=seed + i)[:n]
@@ -54,7 +54,8 @@ def single(r):
     lib = matfun_gb300.load()
     c = r.c
     fn = {(0, 0): lib.smf_cuda_eval, (1, 0): lib.smf_cuda_eval_matrix, (2, 0): lib.gmf_cuda_eval,
-          (0, 1): lib.smf_cuda_eval_f32, (1, 1): lib.smf_cuda_eval_matrix_f32}[(c.family, c.dtype)]
+          (0, 1): lib.smf_cuda_eval_f32, (1, 1): lib.smf_cuda_eval_matrix_f32,
+          (2, 1): lib.gmf_cuda_eval_f32}[(c.family, c.dtype)]
     outs = [torch.empty_like(t) if t is not None else None for t in (r.F, r.J, r.H)]
     p = lambda t: None if t is None else t.data_ptr()
     assert fn(c.kind, c.alpha, c.n, r.x.data_ptr(), *map(p, outs), None) == 0
@@ -119,8 +120,9 @@ def test_invalid_requests_rejected():
     bad.c.J = None  # order 1 without J
     arr = batched._array([bad])
     assert lib.matfun_cuda_batched(ctypes.cast(arr, ctypes.c_void_p), 1, None) == -1
-    f32gmf = batched.request("gmf", "log", torch.eye(3, device="cuda")[None], order=0)
-    assert lib.matfun_cuda_batched(ctypes.cast(batched._array([f32gmf]), ctypes.c_void_p), 1, None) == -1
+    f32bad = batched.request("gmf", "log", torch.eye(3, device="cuda")[None], order=0)
+    f32bad.c.dtype = 2  # neither FP64 nor FP32
+    assert lib.matfun_cuda_batched(ctypes.cast(batched._array([f32bad]), ctypes.c_void_p), 1, None) == -1
     assert lib.matfun_cuda_batched(None, 0, None) == 0
     assert lib.matfun_cuda_batched_tune(0, 1) == -1 and lib.matfun_cuda_batched_tune(2, 1) == 0
 

@@ -1,7 +1,7 @@
-"""The mixed-precision symmetric path (smf_cuda_eval_f32 / smf_cuda_eval_matrix_f32: FP32 storage and bulk
-arithmetic, FP64 eigensystem) against the FP64 oracle evaluated on the same FP32 input values.  Error measure:
-max |x - ref| / max |ref| over each call's output array (F, J, H separately); the bound is 1e-6 (the north-star
-target for the mixed form) unless a kind's own conditioning is stated below."""
+"""The mixed-precision paths (smf_cuda_eval_f32 / smf_cuda_eval_matrix_f32 / gmf_cuda_eval_f32: FP32 storage, FP32
+bulk arithmetic, FP64 only where FP32 would lose the result) against the FP64 oracle evaluated on the same FP32
+input values.  Error measure: max |x - ref| / max |ref| over each call's output array (F, J, H separately); the
+bound is 1e-6 (the target of the mixed form) unless a kind's own conditioning is stated below."""
 import numpy as np
 import pytest
 
@@ -73,3 +73,38 @@ def test_smf_mixed_c0_and_golden_inputs():
     sel = (g["kind"] == 1) & (np.abs(g["x"]).max(axis=1) < 1e30) & (np.abs(g["x"]).max(axis=1) > 1e-30)
     errs, _, _ = errors(False, 1, 0.0, g["x"][sel].astype(np.float32), 2)
     assert max(errs) <= 1e-5
+
+
+# ---- general family (gmf_cuda_eval_f32): FP64 spectral analysis and series, FP32 storage and J / H assembly
+GMF_KINDS = [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3")]
+GMF_TOL = 1e-6
+
+
+def gmf_errors(kind, alpha, X32, order):
+    import torch
+
+    import matfun_gb300
+    lib = matfun_gb300.load()
+    n = len(X32)
+    dX = torch.from_numpy(np.ascontiguousarray(X32.reshape(n, 9))).cuda()
+    out = [torch.full((n, 9 ** (k + 1)), 7.0, dtype=torch.float32, device="cuda") for k in range(order + 1)]
+    p = [t.data_ptr() for t in out] + [None] * (2 - order)
+    assert lib.gmf_cuda_eval_f32(kind, alpha, n, dX.data_ptr(), *p, None) == 0
+    torch.cuda.synchronize()
+    got = [t.cpu().numpy().astype(np.float64) for t in out]
+    ref = ol.call(ol.oracle(), "gmf_eval", kind, alpha, X32.astype(np.float64).reshape(n, 9), order, 9)
+    return [maxrel(g, r) for g, r in zip(got, ref[1:order + 2])], got, ref
+
+
+@pytest.mark.parametrize("kind,alpha,name", GMF_KINDS)
+@pytest.mark.parametrize("order", [0, 1, 2])
+def test_gmf_mixed_c1(kind, alpha, name, order):
+    """the four C1 groups (real eigenvalues, rotations, shears, near-confluent shears), rounded to FP32"""
+    from matfun_gb300 import workloads as w
+    X = w.c1_gmf_groups(16000, seed=5 + order).astype(np.float32)
+    errs, got, ref = gmf_errors(kind, alpha, X, order)
+    print(f"mixed gmf {name} order {order}: max rel F {errs[0]:.2e}" +
+          "".join(f" {n} {e:.2e}" for n, e in zip("JH", errs[1:])))
+    for g, r in zip(got, ref[1:]):
+        assert np.array_equal(np.isnan(g), np.isnan(r))
+    assert max(errs) <= GMF_TOL

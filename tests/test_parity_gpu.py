@@ -125,7 +125,7 @@ def test_batch_tails(n):
 
 def test_configs_sampled():
     """the benchmark workloads (smf SPD with repeated eigenvalues; gmf real / rotation / shear / near-confluent
-    groups) on a sample, every kind of the benchmark spec's metric"""
+    groups) on a sample, every kind of the benchmark metric"""
     from matfun_gb300 import workloads as w
     V = w.c0_smf_spd(8192, seed=0)
     _cmp("smf_eval", 1, 0.0, V, 2, 6)
