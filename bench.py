@@ -302,11 +302,37 @@ def adjoint_vs_materialised(lib, args, dev):
                 JV[lo:lo + ch] = torch.einsum("nabcd,ncd->nab", Jm.view(ch, 3, 3, 3, 3), V[lo:lo + ch])
 
         t_mvjp, t_mhvp = timeit(mat_vjp, 1), timeit(mat_hvp, 1)
+        del Fm, Jm, Hm
+        # FP32: the mixed-precision adjoint kernels on the same values rounded to FP32
+        A32, W32, V32 = A.float(), W.float(), V.float()
+        Ab32, JV32, HWV32 = torch.empty_like(A32), torch.empty_like(A32), torch.empty_like(A32)
+        fn32 = lib.smf_cuda_adjoint_f32 if fam == "smf" else lib.gmf_cuda_adjoint_f32
+        vjp32 = lambda: fn32(kind, alpha, n, A32.data_ptr(), W32.data_ptr(), None, None, Ab32.data_ptr(), None, None,
+                             None)
+        hvp32 = lambda: fn32(kind, alpha, n, A32.data_ptr(), W32.data_ptr(), V32.data_ptr(), None, None,
+                             JV32.data_ptr(), HWV32.data_ptr(), None)
+        t_vjp32, t_hvp32 = timeit(vjp32), timeit(hvp32)
+        # errors of the FP32 results against the FP64 adjoints on the FP32-rounded values (a sample)
+        m = min(n, 1 << 16)
+        ref = {k: torch.empty((m, 3, 3), dtype=torch.float64, device=dev) for k in ("Abar", "JV", "HWV")}
+        A64s, W64s, V64s = A32[:m].double(), W32[:m].double(), V32[:m].double()  # kept alive over the launch
+        assert fn(kind, alpha, m, A64s.data_ptr(), W64s.data_ptr(), V64s.data_ptr(), None, ref["Abar"].data_ptr(),
+                  ref["JV"].data_ptr(), ref["HWV"].data_ptr(), None) == 0
+        assert vjp32() == 0
+        torch.cuda.synchronize()
+        err = {}
+        for k, got in (("Abar", Ab32), ("JV", JV32), ("HWV", HWV32)):
+            a, b = got[:m].double(), ref[k]
+            ok = ~(torch.isnan(a) & torch.isnan(b))
+            err[k] = float((a - b)[ok].abs().max() / b[ok].abs().max())
         res[f"{fam}_{'log' if kind == 1 else 'pow0.3'}"] = {
             "n": n, "vjp_matrices_per_s": n / (t_vjp * 1e-3), "hvp_matrices_per_s": n / (t_hvp * 1e-3),
             "materialised_vjp_matrices_per_s": n / (t_mvjp * 1e-3),
             "materialised_hvp_matrices_per_s": n / (t_mhvp * 1e-3),
             "vjp_speedup": t_mvjp / t_vjp, "hvp_speedup": t_mhvp / t_hvp,
+            "f32": {"vjp_matrices_per_s": n / (t_vjp32 * 1e-3), "hvp_matrices_per_s": n / (t_hvp32 * 1e-3),
+                    "vjp_speedup_vs_fp64_adjoint": t_vjp / t_vjp32, "hvp_speedup_vs_fp64_adjoint": t_hvp / t_hvp32,
+                    "max_rel_err_vs_fp64": err, "err_sample": m},
             "bytes_per_matrix": {"vjp": 216, "hvp": 288}}
     return res
 

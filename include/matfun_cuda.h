@@ -70,6 +70,12 @@ int smf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const d
                      double *Abar, double *JV, double *HWV, void *stream);
 int gmf_cuda_adjoint(int kind, double alpha, int64_t n, const double *A, const double *W, const double *V, double *F,
                      double *Abar, double *JV, double *HWV, void *stream);
+/* The adjoints in mixed precision: FP32 arrays; gmf from its FP64 record rounded once, smf from the eigensystem and
+ * divided differences of smf_cuda_eval_f32; contractions in FP32.  Same arguments and return codes. */
+int smf_cuda_adjoint_f32(int kind, double alpha, int64_t n, const float *A, const float *W, const float *V, float *F,
+                         float *Abar, float *JV, float *HWV, void *stream);
+int gmf_cuda_adjoint_f32(int kind, double alpha, int64_t n, const float *A, const float *W, const float *V, float *F,
+                         float *Abar, float *JV, float *HWV, void *stream);
 
 /* Batched evaluation (no counterpart in the reference): many requests of uneven size and
  * mixed family / kind / order / precision in ONE launch of a persistent kernel.  A request: */

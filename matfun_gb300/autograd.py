@@ -6,7 +6,8 @@
     (V * g).sum().backward()                           # W . H . V and J V    (no H formed)
 
 The backward is itself a Function whose backward runs the Hessian contraction, so first and second derivatives
-(double backward, Hessian-vector products) never materialise J or H; a third derivative raises.  smf treats A as
+(double backward, Hessian-vector products) never materialise J or H; a third derivative raises.  float32 inputs run
+the mixed-precision adjoint kernels (FP32 arrays and contractions).  smf treats A as
 symmetric (derivatives of A -> f((A + A^T)/2), as the reference's smf_eval_matrix).  Functional forms: `adjoint`.
 """
 import torch
@@ -14,14 +15,17 @@ import torch
 from ._lib import KINDS, load
 
 
-def _fn(fam):
+def _fn(fam, f32):
     lib = load()
+    if f32:
+        return lib.gmf_cuda_adjoint_f32 if fam == "gmf" else lib.smf_cuda_adjoint_f32
     return lib.gmf_cuda_adjoint if fam == "gmf" else lib.smf_cuda_adjoint
 
 
 def adjoint(fam, kind, A, W=None, V=None, alpha=None, want=("F",)):
     """one launch of the adjoint kernel: returns a dict with the requested subset of
-    F = f(A), Abar = J^T W, JV = J V, HWV = W . H . V (matrix layout, shapes of A)"""
+    F = f(A), Abar = J^T W, JV = J V, HWV = W . H . V (matrix layout, shapes of A).  float32 A runs the
+    mixed-precision kernels (FP32 arrays); any other dtype runs in float64."""
     if fam not in ("smf", "gmf"):
         raise ValueError("fam must be 'smf' or 'gmf'")
     if kind not in KINDS:
@@ -32,16 +36,18 @@ def adjoint(fam, kind, A, W=None, V=None, alpha=None, want=("F",)):
         raise ValueError(f"expected matrices (..., 3, 3), got shape {tuple(A.shape)}")
     if not A.is_cuda:
         raise TypeError("expected CUDA tensors")
-    A = A.detach().to(torch.float64).contiguous()
-    W = None if W is None else W.detach().to(torch.float64).expand_as(A).contiguous()
-    V = None if V is None else V.detach().to(torch.float64).expand_as(A).contiguous()
+    f32 = A.dtype == torch.float32
+    dt = torch.float32 if f32 else torch.float64
+    A = A.detach().to(dt).contiguous()
+    W = None if W is None else W.detach().to(dt).expand_as(A).contiguous()
+    V = None if V is None else V.detach().to(dt).expand_as(A).contiguous()
     out = {k: torch.empty_like(A) for k in want}
     p = lambda t: None if t is None else t.data_ptr()
     n = A.numel() // 9
     stream = torch.cuda.current_stream(A.device).cuda_stream
     with torch.cuda.device(A.device):
-        r = _fn(fam)(KINDS[kind], float(alpha or 0.0), n, p(A), p(W), p(V), p(out.get("F")), p(out.get("Abar")),
-                     p(out.get("JV")), p(out.get("HWV")), stream)
+        r = _fn(fam, f32)(KINDS[kind], float(alpha or 0.0), n, p(A), p(W), p(V), p(out.get("F")),
+                          p(out.get("Abar")), p(out.get("JV")), p(out.get("HWV")), stream)
     if r != 0:
         raise RuntimeError(f"matfun_gb300: adjoint kernel returned {r}")
     return out

@@ -12,26 +12,34 @@
 // Wt = U^T sym(W) U, Vt = U^T sym(V) U:
 //   Abar = U (D o Wt) U^T,   JV = U (D o Vt) U^T,   HWV = U (Q + Q^T) U^T,  Q_xy = sum_z D2_xyz Wt_xz Vt_yz
 // (Daleckii-Krein and its second-order form; the first-order map is self-adjoint on symmetric directions).
+//
+// Mixed precision (FP32 arrays, T = float): gmf keeps its FP64 record (spectral analysis, series, residues), folds the
+// scale factors into it in FP64 and rounds it to FP32 once for the contractions; smf takes the eigensystem and the
+// divided differences of the mixed smf kernel (smf_mixed.cuh) and contracts in FP32.
 #pragma once
 #include "gmf_kernels.cuh"
 #include "smf_kernels.cuh"
+#include "smf_mixed.cuh"
 
 namespace mf {
 
-MF_D void mm3(const double *X, const double *Y, double *Z) {  // Z = X Y
+template <typename T>
+MF_D void mm3(const T *X, const T *Y, T *Z) {  // Z = X Y
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) Z[3 * i + j] = X[3 * i] * Y[j] + X[3 * i + 1] * Y[3 + j] + X[3 * i + 2] * Y[6 + j];
 }
-MF_D void mmT3(const double *X, const double *Y, double *Z) {  // Z = X Y^T
+template <typename T>
+MF_D void mmT3(const T *X, const T *Y, T *Z) {  // Z = X Y^T
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++)
       Z[3 * i + j] = X[3 * i] * Y[3 * j] + X[3 * i + 1] * Y[3 * j + 1] + X[3 * i + 2] * Y[3 * j + 2];
 }
-MF_D void mTm3(const double *X, const double *Y, double *Z) {  // Z = X^T Y
+template <typename T>
+MF_D void mTm3(const T *X, const T *Y, T *Z) {  // Z = X^T Y
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -39,7 +47,8 @@ MF_D void mTm3(const double *X, const double *Y, double *Z) {  // Z = X^T Y
 }
 
 // the output factor of a record, applied last as in the reference (NaN for a matrix outside the domain)
-MF_D double scale_out(double v, double sc) { return v * sc; }
+template <typename T>
+MF_D T scale_out(T v, T sc) { return v * sc; }
 
 enum { ADJ_F = 1, ADJ_VJP = 2, ADJ_JVP = 4, ADJ_HVP = 8 };
 
@@ -54,12 +63,12 @@ struct GadjSmem {
   int perm[GADJ_TPB];
 };
 
-template <int KIND, int ORDER>
-__global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const double *__restrict__ A,
-                                                               const double *__restrict__ W,
-                                                               const double *__restrict__ V, double *__restrict__ F,
-                                                               double *__restrict__ Abar, double *__restrict__ JV,
-                                                               double *__restrict__ HWV, const GmfCoef C) {
+template <int KIND, int ORDER, typename T>
+__global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const T *__restrict__ A,
+                                                               const T *__restrict__ W, const T *__restrict__ V,
+                                                               T *__restrict__ F, T *__restrict__ Abar,
+                                                               T *__restrict__ JV, T *__restrict__ HWV,
+                                                               const GmfCoef C) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GadjSmem &S = *reinterpret_cast<GadjSmem *>(smem_raw);
   const int tid = threadIdx.x;
@@ -97,23 +106,34 @@ __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const 
   if (mine < cnt) {
     GmfRec R;
     gmf_finish<KIND, ORDER>(S.state[mine], C, R);
-    double r[3][9];
+    // FP32: fold the scale factors into D2', D3' in FP64 when finite and nonzero, then round the record once
+    constexpr bool MIXED = sizeof(T) == 4;
+    const double rsc2 = ORDER >= 2 ? R.sc2 : 1.0;
+    const bool f1 = MIXED & isfinite(R.sc1) & (R.sc1 != 0.0), f2 = MIXED & isfinite(rsc2) & (rsc2 != 0.0);
+    const double s1 = sel(f1, R.sc1, 1.0), s2 = sel(f2, rsc2, 1.0);
+    const T sc1 = (T)sel(f1, 1.0, R.sc1), sc2 = (T)sel(f2, 1.0, rsc2);
+    T r[3][9];
 #pragma unroll
     for (int k = 0; k < 9; k++) {
-      r[0][k] = k % 4 == 0 ? 1.0 : 0.0;
-      r[1][k] = R.r1[k];
-      r[2][k] = R.r2[k];
+      r[0][k] = k % 4 == 0 ? T(1) : T(0);
+      r[1][k] = (T)R.r1[k];
+      r[2][k] = (T)R.r2[k];
     }
-    const double D2m[3][3] = {{R.D2[0], R.D2[3], R.D2[4]}, {R.D2[3], R.D2[1], R.D2[5]}, {R.D2[4], R.D2[5], R.D2[2]}};
+    T D2s[6], D3s[10];
+#pragma unroll
+    for (int k = 0; k < 6; k++) D2s[k] = (T)(R.D2[k] * s1);
+#pragma unroll
+    for (int k = 0; k < 10; k++) D3s[k] = ORDER >= 2 ? (T)(R.D3[k] * s2) : T(0);
+    const T D2m[3][3] = {{D2s[0], D2s[3], D2s[4]}, {D2s[3], D2s[1], D2s[5]}, {D2s[4], D2s[5], D2s[2]}};
     if (F) {
 #pragma unroll
       for (int k = 0; k < 9; k++) S.out[0][mine * 9 + k] = R.F[k];
     }
     const double *w = S.w + mine * 9, *v = S.v + mine * 9;
-    double Wl[9], Vl[9];
+    T Wl[9], Vl[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) { Wl[k] = W ? w[k] : 0.0; Vl[k] = V ? v[k] : 0.0; }
-    double Gw[3][9];  // W r_n^T
+    for (int k = 0; k < 9; k++) { Wl[k] = W ? (T)w[k] : T(0); Vl[k] = V ? (T)v[k] : T(0); }
+    T Gw[3][9];  // W r_n^T
     if (Abar || HWV) {
 #pragma unroll
       for (int k = 0; k < 9; k++) Gw[0][k] = Wl[k];
@@ -121,27 +141,27 @@ __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const 
       mmT3(Wl, r[2], Gw[2]);
     }
     if (Abar) {  // sc1 sum_m r_m^T (sum_n D2'_mn W r_n^T)
-      double acc[9];
+      T acc[9];
 #pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] = 0.0;
+      for (int k = 0; k < 9; k++) acc[k] = T(0);
 #pragma unroll
       for (int mm = 0; mm < 3; mm++) {
-        double Hm[9], T[9];
+        T Hm[9], Tm[9];
 #pragma unroll
         for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gw[0][k] + D2m[mm][1] * Gw[1][k] + D2m[mm][2] * Gw[2][k];
         if (mm == 0) {
 #pragma unroll
           for (int k = 0; k < 9; k++) acc[k] += Hm[k];
         } else {
-          mTm3(r[mm], Hm, T);
+          mTm3(r[mm], Hm, Tm);
 #pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += T[k];
+          for (int k = 0; k < 9; k++) acc[k] += Tm[k];
         }
       }
 #pragma unroll
-      for (int k = 0; k < 9; k++) S.out[1][mine * 9 + k] = scale_out(acc[k], R.sc1);
+      for (int k = 0; k < 9; k++) S.out[1][mine * 9 + k] = scale_out(acc[k], sc1);
     }
-    double Gv[3][9];  // V r_n
+    T Gv[3][9];  // V r_n
     if (JV || HWV) {
 #pragma unroll
       for (int k = 0; k < 9; k++) Gv[0][k] = Vl[k];
@@ -149,38 +169,38 @@ __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const 
       mm3(Vl, r[2], Gv[2]);
     }
     if (JV) {  // sc1 sum_m r_m (sum_n D2'_mn V r_n)
-      double acc[9];
+      T acc[9];
 #pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] = 0.0;
+      for (int k = 0; k < 9; k++) acc[k] = T(0);
 #pragma unroll
       for (int mm = 0; mm < 3; mm++) {
-        double Hm[9], T[9];
+        T Hm[9], Tm[9];
 #pragma unroll
         for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gv[0][k] + D2m[mm][1] * Gv[1][k] + D2m[mm][2] * Gv[2][k];
         if (mm == 0) {
 #pragma unroll
           for (int k = 0; k < 9; k++) acc[k] += Hm[k];
         } else {
-          mm3(r[mm], Hm, T);
+          mm3(r[mm], Hm, Tm);
 #pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += T[k];
+          for (int k = 0; k < 9; k++) acc[k] += Tm[k];
         }
       }
 #pragma unroll
-      for (int k = 0; k < 9; k++) S.out[2][mine * 9 + k] = scale_out(acc[k], R.sc1);
+      for (int k = 0; k < 9; k++) S.out[2][mine * 9 + k] = scale_out(acc[k], sc1);
     }
     if (ORDER >= 2 && HWV) {
       // M_mn = r_m V r_n ; X_p = sum_mn D3'_mnp M_mn ; HWV = sc2 sum_p (X_p^T W r_p^T + r_p^T W X_p^T)
-      double X[3][9];
+      T X[3][9];
 #pragma unroll
       for (int p = 0; p < 3; p++)
 #pragma unroll
-        for (int k = 0; k < 9; k++) X[p][k] = 0.0;
+        for (int k = 0; k < 9; k++) X[p][k] = T(0);
 #pragma unroll
       for (int mm = 0; mm < 3; mm++)
 #pragma unroll
         for (int nn = 0; nn < 3; nn++) {
-          double M[9];
+          T M[9];
           if (mm == 0) {
 #pragma unroll
             for (int k = 0; k < 9; k++) M[k] = Gv[nn][k];
@@ -191,17 +211,17 @@ __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const 
           for (int p = 0; p < 3; p++) {
             int i0 = mm, i1 = nn, i2 = p;
             sort3(i0, i1, i2);
-            const double d = R.D3[sym3(i0, i1, i2)];
+            const T d = D3s[sym3(i0, i1, i2)];
 #pragma unroll
             for (int k = 0; k < 9; k++) X[p][k] += d * M[k];
           }
         }
-      double acc[9];
+      T acc[9];
 #pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] = 0.0;
+      for (int k = 0; k < 9; k++) acc[k] = T(0);
 #pragma unroll
       for (int p = 0; p < 3; p++) {
-        double T1[9], T2[9], T3[9];
+        T T1[9], T2[9], T3[9];
         mTm3(X[p], Gw[p], T1);  // X_p^T (W r_p^T)
         mmT3(Wl, X[p], T2);     // W X_p^T
         if (p == 0) {
@@ -214,19 +234,85 @@ __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const 
         for (int k = 0; k < 9; k++) acc[k] += T1[k] + T3[k];
       }
 #pragma unroll
-      for (int k = 0; k < 9; k++) S.out[3][mine * 9 + k] = scale_out(acc[k], R.sc2);
+      for (int k = 0; k < 9; k++) S.out[3][mine * 9 + k] = scale_out(acc[k], sc2);
     }
   }
   __syncthreads();
-  double *dst[4] = {F, Abar, JV, HWV};
+  T *dst[4] = {F, Abar, JV, HWV};
 #pragma unroll
   for (int q = 0; q < 4; q++) {
     if (!dst[q]) continue;
-    for (int e = tid; e < cnt * 9; e += GADJ_TPB) dst[q][base * 9 + e] = S.out[q][e];
+    for (int e = tid; e < cnt * 9; e += GADJ_TPB) dst[q][base * 9 + e] = (T)S.out[q][e];
   }
 }
 
 // ------------------------------------------------------------------------------------------------ symmetric
+// the contractions in the eigenbasis: Wt = U^T sym(W) U, Vt = U^T sym(V) U; Abar = U (D o Wt) U^T,
+// JV = U (D o Vt) U^T, HWV = U (Q + Q^T) U^T with Q_xy = sum_z D2_xyz Wt_xz Vt_yz (outputs may be null)
+template <typename T, int ORDER>
+MF_D void smf_adj_apply(const T (&U)[3][3], const T (&Dm)[3][3], const T (&D2)[3][3][3], const T *w, const T *v,
+                        T *oAbar, T *oJV, T *oHWV) {
+  T Wt[3][3], Vt[3][3];
+  auto rotate = [&](const T *Xg, T Xt[3][3]) {
+    T Xs[3][3], Tm[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) Xs[i][j] = T(0.5) * (Xg[3 * i + j] + Xg[3 * j + i]);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) Tm[i][b] = Xs[i][0] * U[0][b] + Xs[i][1] * U[1][b] + Xs[i][2] * U[2][b];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) Xt[a][b] = U[0][a] * Tm[0][b] + U[1][a] * Tm[1][b] + U[2][a] * Tm[2][b];
+  };
+  auto back = [&](T Y[3][3], T *out) {  // out = U Y U^T
+    T Tm[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) Tm[i][b] = U[i][0] * Y[0][b] + U[i][1] * Y[1][b] + U[i][2] * Y[2][b];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) out[3 * i + j] = Tm[i][0] * U[j][0] + Tm[i][1] * U[j][1] + Tm[i][2] * U[j][2];
+  };
+  if (oAbar || oHWV) rotate(w, Wt);
+  if (oJV || oHWV) rotate(v, Vt);
+  if (oAbar) {
+    T Y[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) Y[a][b] = Dm[a][b] * Wt[a][b];
+    back(Y, oAbar);
+  }
+  if (oJV) {
+    T Y[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) Y[a][b] = Dm[a][b] * Vt[a][b];
+    back(Y, oJV);
+  }
+  if (ORDER >= 2 && oHWV) {
+    T Q[3][3], Y[3][3];
+#pragma unroll
+    for (int x = 0; x < 3; x++)
+#pragma unroll
+      for (int y = 0; y < 3; y++)
+        Q[x][y] = D2[x][y][0] * Wt[x][0] * Vt[y][0] + D2[x][y][1] * Wt[x][1] * Vt[y][1] +
+                  D2[x][y][2] * Wt[x][2] * Vt[y][2];
+#pragma unroll
+    for (int x = 0; x < 3; x++)
+#pragma unroll
+      for (int y = 0; y < 3; y++) Y[x][y] = Q[x][y] + Q[y][x];
+    back(Y, oHWV);
+  }
+}
+
 constexpr int SADJ_TPB = 64;
 
 template <int KIND, int ORDER>
@@ -275,54 +361,8 @@ __global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel(int64_t n, const 
       const double Dm[3][3] = {{smf_deriv<KIND>(lam[0], fl[0], C), D01, D02},
                                {D01, smf_deriv<KIND>(lam[1], fl[1], C), D12},
                                {D02, D12, smf_deriv<KIND>(lam[2], fl[2], C)}};
-      // Xt = U^T sym(X) U for X = W, V
-      double Wt[3][3], Vt[3][3];
-      auto rotate = [&](const double *Xg, double Xt[3][3]) {
-        double Xs[3][3], T[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-          for (int j = 0; j < 3; j++) Xs[i][j] = 0.5 * (Xg[3 * i + j] + Xg[3 * j + i]);
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-          for (int b = 0; b < 3; b++) T[i][b] = Xs[i][0] * U[0][b] + Xs[i][1] * U[1][b] + Xs[i][2] * U[2][b];
-#pragma unroll
-        for (int a = 0; a < 3; a++)
-#pragma unroll
-          for (int b = 0; b < 3; b++) Xt[a][b] = U[0][a] * T[0][b] + U[1][a] * T[1][b] + U[2][a] * T[2][b];
-      };
-      auto back = [&](double Y[3][3], double *out) {  // out = U Y U^T
-        double T[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-          for (int b = 0; b < 3; b++) T[i][b] = U[i][0] * Y[0][b] + U[i][1] * Y[1][b] + U[i][2] * Y[2][b];
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-          for (int j = 0; j < 3; j++) out[3 * i + j] = T[i][0] * U[j][0] + T[i][1] * U[j][1] + T[i][2] * U[j][2];
-      };
-      if (Abar || HWV) rotate(sw + tid * 9, Wt);
-      if (JV || HWV) rotate(sv + tid * 9, Vt);
-      if (Abar) {
-        double Y[3][3];
-#pragma unroll
-        for (int a = 0; a < 3; a++)
-#pragma unroll
-          for (int b = 0; b < 3; b++) Y[a][b] = Dm[a][b] * Wt[a][b];
-        back(Y, so[1] + tid * 9);
-      }
-      if (JV) {
-        double Y[3][3];
-#pragma unroll
-        for (int a = 0; a < 3; a++)
-#pragma unroll
-          for (int b = 0; b < 3; b++) Y[a][b] = Dm[a][b] * Vt[a][b];
-        back(Y, so[2] + tid * 9);
-      }
+      double D2[3][3][3];
       if (ORDER >= 2 && HWV) {
-        double D2[3][3][3];
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -334,19 +374,9 @@ __global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel(int64_t n, const 
                                                                   Dm[i][j], Dm[i][l], Dm[j][l], C);
               D2[i][j][l] = D2[i][l][j] = D2[j][i][l] = D2[j][l][i] = D2[l][i][j] = D2[l][j][i] = d;
             }
-        double Q[3][3], Y[3][3];
-#pragma unroll
-        for (int x = 0; x < 3; x++)
-#pragma unroll
-          for (int y = 0; y < 3; y++)
-            Q[x][y] = D2[x][y][0] * Wt[x][0] * Vt[y][0] + D2[x][y][1] * Wt[x][1] * Vt[y][1] +
-                      D2[x][y][2] * Wt[x][2] * Vt[y][2];
-#pragma unroll
-        for (int x = 0; x < 3; x++)
-#pragma unroll
-          for (int y = 0; y < 3; y++) Y[x][y] = Q[x][y] + Q[y][x];
-        back(Y, so[3] + tid * 9);
       }
+      smf_adj_apply<double, ORDER>(U, Dm, D2, sw + tid * 9, sv + tid * 9, Abar ? so[1] + tid * 9 : nullptr,
+                                   JV ? so[2] + tid * 9 : nullptr, HWV ? so[3] + tid * 9 : nullptr);
     }
   }
   __syncthreads();
@@ -358,30 +388,77 @@ __global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel(int64_t n, const 
   }
 }
 
-// ------------------------------------------------------------------------------------------------ launchers
+// mixed precision: FP32 arrays, the eigensystem and divided differences of smf_mixed.cuh, FP32 contractions
 template <int KIND, int ORDER>
-cudaError_t gmf_adjoint_one(unsigned blocks, int64_t n, const double *A, const double *W, const double *V, double *F,
-                            double *Abar, double *JV, double *HWV, const GmfCoef &C, cudaStream_t st) {
+__global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel_f32(int64_t n, const float *__restrict__ A,
+                                                                   const float *__restrict__ W,
+                                                                   const float *__restrict__ V, float *__restrict__ F,
+                                                                   float *__restrict__ Abar, float *__restrict__ JV,
+                                                                   float *__restrict__ HWV, const SmfCoefF C) {
+  __shared__ float sx[SADJ_TPB * 9], sw[SADJ_TPB * 9], sv[SADJ_TPB * 9], so[4][SADJ_TPB * 9];
+  const int tid = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * SADJ_TPB;
+  const int cnt = (int)min((int64_t)SADJ_TPB, n - base);
+  for (int e = tid; e < cnt * 9; e += SADJ_TPB) {
+    sx[e] = A[base * 9 + e];
+    if (W) sw[e] = W[base * 9 + e];
+    if (V) sv[e] = V[base * 9 + e];
+  }
+  __syncthreads();
+  if (tid < cnt) {
+    double v6[6];
+    sym_voigt_f(sx + tid * 9, v6);
+    SmfSpecF Sp;
+    smf_spectrum_f<KIND>(v6, C, Sp);
+    if (F) {
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+          so[0][tid * 9 + 3 * a + b] = Sp.V[a][0] * Sp.fl[0] * Sp.V[b][0] + Sp.V[a][1] * Sp.fl[1] * Sp.V[b][1] +
+                                       Sp.V[a][2] * Sp.fl[2] * Sp.V[b][2];
+    }
+    if (Abar || JV || HWV) {
+      float Dm[3][3], D2[3][3][3];
+      smf_dm_f<KIND>(Sp, C, Dm);
+      if (ORDER >= 2 && HWV) smf_d2_f<KIND>(Sp, Dm, C, D2);
+      smf_adj_apply<float, ORDER>(Sp.V, Dm, D2, sw + tid * 9, sv + tid * 9, Abar ? so[1] + tid * 9 : nullptr,
+                                  JV ? so[2] + tid * 9 : nullptr, HWV ? so[3] + tid * 9 : nullptr);
+    }
+  }
+  __syncthreads();
+  float *dst[4] = {F, Abar, JV, HWV};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (!dst[q]) continue;
+    for (int e = tid; e < cnt * 9; e += SADJ_TPB) dst[q][base * 9 + e] = so[q][e];
+  }
+}
+
+// ------------------------------------------------------------------------------------------------ launchers
+template <int KIND, int ORDER, typename T>
+cudaError_t gmf_adjoint_one(unsigned blocks, int64_t n, const T *A, const T *W, const T *V, T *F, T *Abar, T *JV,
+                            T *HWV, const GmfCoef &C, cudaStream_t st) {
   static bool attr = false;  // per instantiation (idempotent)
   if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(gmf_adjoint_kernel<KIND, ORDER>,
+    const cudaError_t e = cudaFuncSetAttribute(gmf_adjoint_kernel<KIND, ORDER, T>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GadjSmem));
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  gmf_adjoint_kernel<KIND, ORDER><<<blocks, GADJ_TPB, sizeof(GadjSmem), st>>>(n, A, W, V, F, Abar, JV, HWV, C);
+  gmf_adjoint_kernel<KIND, ORDER, T><<<blocks, GADJ_TPB, sizeof(GadjSmem), st>>>(n, A, W, V, F, Abar, JV, HWV, C);
   return cudaGetLastError();
 }
 
-template <int KIND>
-cudaError_t gmf_adjoint_t(double al, int64_t n, const double *A, const double *W, const double *V, double *F,
-                          double *Abar, double *JV, double *HWV, cudaStream_t st) {
+template <int KIND, typename T = double>
+cudaError_t gmf_adjoint_t(double al, int64_t n, const T *A, const T *W, const T *V, T *F, T *Abar, T *JV, T *HWV,
+                          cudaStream_t st) {
   const int order = HWV ? 2 : 1;
   GmfCoef C;
   gmf_coef(KIND, al, order, C);
   const unsigned blocks = (unsigned)((n + GADJ_TPB - 1) / GADJ_TPB);
-  return order == 2 ? gmf_adjoint_one<KIND, 2>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st)
-                    : gmf_adjoint_one<KIND, 1>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st);
+  return order == 2 ? gmf_adjoint_one<KIND, 2, T>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st)
+                    : gmf_adjoint_one<KIND, 1, T>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st);
 }
 
 template <int KIND>
@@ -392,6 +469,17 @@ cudaError_t smf_adjoint_t(double al, int64_t n, const double *A, const double *W
   const unsigned blocks = (unsigned)((n + SADJ_TPB - 1) / SADJ_TPB);
   if (HWV) smf_adjoint_kernel<KIND, 2><<<blocks, SADJ_TPB, 0, st>>>(n, A, W, V, F, Abar, JV, HWV, C);
   else smf_adjoint_kernel<KIND, 1><<<blocks, SADJ_TPB, 0, st>>>(n, A, W, V, F, Abar, JV, HWV, C);
+  return cudaGetLastError();
+}
+
+template <int KIND>
+cudaError_t smf_adjoint_f32_t(double al, int64_t n, const float *A, const float *W, const float *V, float *F,
+                              float *Abar, float *JV, float *HWV, cudaStream_t st) {
+  SmfCoefF C;
+  smf_coef_f(KIND, al, C);
+  const unsigned blocks = (unsigned)((n + SADJ_TPB - 1) / SADJ_TPB);
+  if (HWV) smf_adjoint_kernel_f32<KIND, 2><<<blocks, SADJ_TPB, 0, st>>>(n, A, W, V, F, Abar, JV, HWV, C);
+  else smf_adjoint_kernel_f32<KIND, 1><<<blocks, SADJ_TPB, 0, st>>>(n, A, W, V, F, Abar, JV, HWV, C);
   return cudaGetLastError();
 }
 

@@ -124,8 +124,20 @@ extern "C" int gmf_cuda_eval_f32(int kind, double alpha, int64_t n, const float 
 }
 
 namespace {
-int adjoint_call(bool general, int kind, double alpha, int64_t n, const double *A, const double *W, const double *V,
-                 double *F, double *Abar, double *JV, double *HWV, void *stream) {
+cudaError_t adjoint_launch(bool general, int kind, double al, int64_t n, const double *A, const double *W,
+                           const double *V, double *F, double *Abar, double *JV, double *HWV, cudaStream_t st) {
+  return general ? mf::gmf_adjoint_launch(kind, al, n, A, W, V, F, Abar, JV, HWV, st)
+                 : mf::smf_adjoint_launch(kind, al, n, A, W, V, F, Abar, JV, HWV, st);
+}
+cudaError_t adjoint_launch(bool general, int kind, double al, int64_t n, const float *A, const float *W,
+                           const float *V, float *F, float *Abar, float *JV, float *HWV, cudaStream_t st) {
+  return general ? mf::gmf_adjoint_launch_f32(kind, al, n, A, W, V, F, Abar, JV, HWV, st)
+                 : mf::smf_adjoint_launch_f32(kind, al, n, A, W, V, F, Abar, JV, HWV, st);
+}
+
+template <typename T>
+int adjoint_call(bool general, int kind, double alpha, int64_t n, const T *A, const T *W, const T *V, T *F, T *Abar,
+                 T *JV, T *HWV, void *stream) {
   if (kind < SMF_EXP || kind > SMF_SQRT || n < 0 || (kind == SMF_POW && !(alpha > 0))) return -1;
   if ((Abar && !W) || (JV && !V) || (HWV && !(W && V))) return -1;
   if (n > 0 && !A) return -1;
@@ -133,8 +145,7 @@ int adjoint_call(bool general, int kind, double alpha, int64_t n, const double *
   if (kind != SMF_POW) alpha = kind == SMF_SQRT ? 0.5 : 0.0;
   if (n == 0 || !(F || Abar || JV || HWV)) return 0;
   if (n > SMF_MAX_N) return -2;
-  const cudaError_t e = general ? mf::gmf_adjoint_launch(kind, alpha, n, A, W, V, F, Abar, JV, HWV, (cudaStream_t)stream)
-                                : mf::smf_adjoint_launch(kind, alpha, n, A, W, V, F, Abar, JV, HWV, (cudaStream_t)stream);
+  const cudaError_t e = adjoint_launch(general, kind, alpha, n, A, W, V, F, Abar, JV, HWV, (cudaStream_t)stream);
   return e == cudaSuccess ? 0 : -2;
 }
 }  // namespace
@@ -150,3 +161,13 @@ extern "C" int smf_cuda_adjoint(int kind, double alpha, int64_t n, const double 
 }
 
 extern "C" const char *matfun_cuda_version(void) { return "matfun-gb300 0.1.0 (sm_103a)"; }
+
+extern "C" int gmf_cuda_adjoint_f32(int kind, double alpha, int64_t n, const float *A, const float *W, const float *V,
+                                    float *F, float *Abar, float *JV, float *HWV, void *stream) {
+  return adjoint_call(true, kind, alpha, n, A, W, V, F, Abar, JV, HWV, stream);
+}
+
+extern "C" int smf_cuda_adjoint_f32(int kind, double alpha, int64_t n, const float *A, const float *W, const float *V,
+                                    float *F, float *Abar, float *JV, float *HWV, void *stream) {
+  return adjoint_call(false, kind, alpha, n, A, W, V, F, Abar, JV, HWV, stream);
+}

@@ -41,6 +41,11 @@ cudaError_t gmf_adjoint_launch(int kind, double al, int64_t n, const double *A, 
                                double *F, double *Abar, double *JV, double *HWV, cudaStream_t st);
 cudaError_t smf_adjoint_launch(int kind, double al, int64_t n, const double *A, const double *W, const double *V,
                                double *F, double *Abar, double *JV, double *HWV, cudaStream_t st);
+// the same in mixed precision (FP32 arrays)
+cudaError_t gmf_adjoint_launch_f32(int kind, double al, int64_t n, const float *A, const float *W, const float *V,
+                                   float *F, float *Abar, float *JV, float *HWV, cudaStream_t st);
+cudaError_t smf_adjoint_launch_f32(int kind, double al, int64_t n, const float *A, const float *W, const float *V,
+                                   float *F, float *Abar, float *JV, float *HWV, cudaStream_t st);
 // the three FP64 entry points by family (0 smf Voigt, 1 smf matrix, 2 gmf) with the reference's argument checks and
 // return codes (0, -1, -2); *err (optional) receives the CUDA error of a failed launch (capi.cu)
 int eval_f64(int family, int kind, double alpha, int64_t n, const double *x, double *F, double *J, double *H,

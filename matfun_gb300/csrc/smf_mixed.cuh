@@ -230,6 +230,97 @@ MF_D void smf_eigsys_mixed(const double *v, SmfEigM &E) {
   }
 }
 
+// symmetric part of an FP32 3x3 matrix as Voigt values in FP64; all NaN if |a_ij - a_ji| > 1e-8 max |a_kl|
+// (smf_kernel.hpp:408-421), checked in FP64 on the FP32 values
+MF_D void sym_voigt_f(const float *xi, double *v) {
+  double a9[9], mx = 0.0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) { a9[k] = xi[k]; mx = sel(fabs(a9[k]) > mx, fabs(a9[k]), mx); }
+  const double tol = 1e-8 * mx;
+  bool sym = !(fabs(a9[1] - a9[3]) > tol) & !(fabs(a9[2] - a9[6]) > tol) & !(fabs(a9[5] - a9[7]) > tol);
+  v[0] = a9[0]; v[1] = a9[4]; v[2] = a9[8];
+  v[3] = 0.5 * (a9[1] + a9[3]); v[4] = 0.5 * (a9[2] + a9[6]); v[5] = 0.5 * (a9[5] + a9[7]);
+#pragma unroll
+  for (int k = 0; k < 6; k++) v[k] = sel(sym, v[k], __longlong_as_double(0x7FF8000000000000ll));
+}
+
+// the spectrum of the mixed path, eigenvalues sorted ascending: FP32 eigenvectors V (columns), eigenvalues lf,
+// their differences taken in FP64 and rounded once (d10 = l1 - l0, d21, d20), and f(lambda) (log near the mean
+// through log1p of the deviator's eigenvalue, smf_kernel.hpp:283-290); powers see max(lambda, 0)
+struct SmfSpecF {
+  float lf[3], fl[3], V[3][3], d10, d21, d20;
+};
+
+template <int KIND>
+MF_D void smf_spectrum_f(const double *v, const SmfCoefF &C, SmfSpecF &Sp) {
+  SmfEigM E;
+  smf_eigsys_mixed<KIND>(v, E);
+  double lam[3] = {E.lam[0], E.lam[1], E.lam[2]}, xd[3] = {E.xd[0], E.xd[1], E.xd[2]};
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) Sp.V[i][j] = E.V[i][j];
+#pragma unroll
+  for (int st = 0; st < 3; st++) {  // sort ascending (FP64 keys): a static order for every divided difference
+    const int a = st == 1 ? 1 : 0, b = a + 1;
+    bool sw = lam[b] < lam[a];
+    double la = lam[a], lb = lam[b], xa = xd[a], xb = xd[b];
+    lam[a] = sel(sw, lb, la); lam[b] = sel(sw, la, lb);
+    xd[a] = sel(sw, xb, xa); xd[b] = sel(sw, xa, xb);
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      float va = Sp.V[r][a], vb = Sp.V[r][b];
+      Sp.V[r][a] = self(sw, vb, va); Sp.V[r][b] = self(sw, va, vb);
+    }
+  }
+  if (KIND == POW || KIND == SQRT) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) lam[i] = sel(lam[i] > 0.0, lam[i], 0.0);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) Sp.lf[i] = (float)lam[i];
+  Sp.d10 = (float)(lam[1] - lam[0]); Sp.d21 = (float)(lam[2] - lam[1]); Sp.d20 = (float)(lam[2] - lam[0]);
+#pragma unroll
+  for (int i = 0; i < 3; i++) Sp.fl[i] = fun_f<KIND>(Sp.lf[i], C.al);
+  if (KIND == LOG) {
+    float mf = (float)E.m, lms = logf(mf);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      float x = (float)xd[i];
+      Sp.fl[i] = self(fabsf(x) <= 0.5f * mf, lms + log1pf(x / mf), Sp.fl[i]);
+    }
+  }
+}
+
+// first divided differences D_ij = f[l_i, l_j] (D_ii = f'(l_i)) in FP32
+template <int KIND>
+MF_D void smf_dm_f(const SmfSpecF &Sp, const SmfCoefF &C, float Dm[3][3]) {
+  const float D01 = dd1s_f<KIND>(Sp.lf[0], Sp.lf[1], Sp.d10, Sp.fl[0], Sp.fl[1], C);
+  const float D02 = dd1s_f<KIND>(Sp.lf[0], Sp.lf[2], Sp.d20, Sp.fl[0], Sp.fl[2], C);
+  const float D12 = dd1s_f<KIND>(Sp.lf[1], Sp.lf[2], Sp.d21, Sp.fl[1], Sp.fl[2], C);
+  Dm[0][0] = deriv_f<KIND>(Sp.lf[0], Sp.fl[0], C); Dm[1][1] = deriv_f<KIND>(Sp.lf[1], Sp.fl[1], C);
+  Dm[2][2] = deriv_f<KIND>(Sp.lf[2], Sp.fl[2], C);
+  Dm[0][1] = Dm[1][0] = D01; Dm[0][2] = Dm[2][0] = D02; Dm[1][2] = Dm[2][1] = D12;
+}
+
+// second divided differences D2_ijl = f[l_i, l_j, l_l] (symmetric) in FP32
+template <int KIND>
+MF_D void smf_d2_f(const SmfSpecF &Sp, const float Dm[3][3], const SmfCoefF &C, float D2[3][3][3]) {
+  const float dd[3][3] = {{0.f, Sp.d10, Sp.d20}, {0.f, 0.f, Sp.d21}, {0.f, 0.f, 0.f}};
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++)
+#pragma unroll
+      for (int l = j; l < 3; l++) {
+        const float d = (i == j && j == l)
+                            ? dd2_same_f<KIND>(Sp.lf[i], Sp.fl[i], Dm[i][i], C)
+                            : dd2s_f<KIND>(Sp.lf[j], Sp.lf[l], Sp.fl[j], Dm[i][j], Dm[j][l], dd[i][j], dd[j][l],
+                                           dd[i][l], C);
+        D2[i][j][l] = D2[i][l][j] = D2[j][i][l] = D2[j][l][i] = D2[l][i][j] = D2[l][j][i] = d;
+      }
+}
+
 constexpr int SMFX_TPB = 64;  // matrices per CTA of the standalone kernel
 
 template <int ORDER, bool MAT, int TPB>
@@ -253,60 +344,16 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
   if (tid < cnt) {
     double v[6];
     const float *xi = sX + tid * NIN;
-    if (MAT) {  // symmetric part; NaN if |a_ij - a_ji| > 1e-8 max|a| (checked in FP64 on the FP32 values)
-      double a9[9], mx = 0.0;
-#pragma unroll
-      for (int k = 0; k < 9; k++) { a9[k] = xi[k]; mx = sel(fabs(a9[k]) > mx, fabs(a9[k]), mx); }
-      const double tol = 1e-8 * mx;
-      bool sym = !(fabs(a9[1] - a9[3]) > tol) & !(fabs(a9[2] - a9[6]) > tol) & !(fabs(a9[5] - a9[7]) > tol);
-      v[0] = a9[0]; v[1] = a9[4]; v[2] = a9[8];
-      v[3] = 0.5 * (a9[1] + a9[3]); v[4] = 0.5 * (a9[2] + a9[6]); v[5] = 0.5 * (a9[5] + a9[7]);
-#pragma unroll
-      for (int k = 0; k < 6; k++) v[k] = sel(sym, v[k], __longlong_as_double(0x7FF8000000000000ll));
+    if (MAT) {
+      sym_voigt_f(xi, v);
     } else {
 #pragma unroll
       for (int k = 0; k < 6; k++) v[k] = xi[k];
     }
-    SmfEigM E;
-    smf_eigsys_mixed<KIND>(v, E);
-    // sort ascending (FP64 keys), so that every divided difference below has a static ordering
-    double lam[3] = {E.lam[0], E.lam[1], E.lam[2]}, xd[3] = {E.xd[0], E.xd[1], E.xd[2]};
-    float V[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) V[i][j] = E.V[i][j];
-#pragma unroll
-    for (int st = 0; st < 3; st++) {
-      const int a = st == 1 ? 1 : 0, b = a + 1;
-      bool sw = lam[b] < lam[a];
-      double la = lam[a], lb = lam[b], xa = xd[a], xb = xd[b];
-      lam[a] = sel(sw, lb, la); lam[b] = sel(sw, la, lb);
-      xd[a] = sel(sw, xb, xa); xd[b] = sel(sw, xa, xb);
-#pragma unroll
-      for (int r = 0; r < 3; r++) {
-        float va = V[r][a], vb = V[r][b];
-        V[r][a] = self(sw, vb, va); V[r][b] = self(sw, va, vb);
-      }
-    }
-    if (KIND == POW || KIND == SQRT) {  // f, f' and the divided differences of powers see max(lambda, 0)
-#pragma unroll
-      for (int i = 0; i < 3; i++) lam[i] = sel(lam[i] > 0.0, lam[i], 0.0);
-    }
-    // eigenvalues and their differences, rounded to FP32 once
-    float lf[3] = {(float)lam[0], (float)lam[1], (float)lam[2]};
-    float d10 = (float)(lam[1] - lam[0]), d21 = (float)(lam[2] - lam[1]), d20 = (float)(lam[2] - lam[0]);
-    float fl[3];
-#pragma unroll
-    for (int i = 0; i < 3; i++) fl[i] = fun_f<KIND>(lf[i], C.al);
-    if (KIND == LOG) {
-      float mf = (float)E.m, lms = logf(mf);
-#pragma unroll
-      for (int i = 0; i < 3; i++) {
-        float x = (float)xd[i];
-        fl[i] = self(fabsf(x) <= 0.5f * mf, lms + log1pf(x / mf), fl[i]);
-      }
-    }
+    SmfSpecF Sp;
+    smf_spectrum_f<KIND>(v, C, Sp);
+    const float(&V)[3][3] = Sp.V;
+    const float *fl = Sp.fl;
     float Fv[6];
 #pragma unroll
     for (int s = 0; s < 6; s++) {
@@ -321,17 +368,13 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
       for (int s = 0; s < 6; s++) sF[tid * 6 + s] = Fv[s];
     }
     if (ORDER >= 1) {
-      const float D01 = dd1s_f<KIND>(lf[0], lf[1], d10, fl[0], fl[1], C);
-      const float D02 = dd1s_f<KIND>(lf[0], lf[2], d20, fl[0], fl[2], C);
-      const float D12 = dd1s_f<KIND>(lf[1], lf[2], d21, fl[1], fl[2], C);
-      const float D00 = deriv_f<KIND>(lf[0], fl[0], C), D11 = deriv_f<KIND>(lf[1], fl[1], C);
-      const float D22 = deriv_f<KIND>(lf[2], fl[2], C);
+      float Dm[3][3];
+      smf_dm_f<KIND>(Sp, C, Dm);
       float P[6][3];
 #pragma unroll
       for (int s6 = 0; s6 < 6; s6++)
 #pragma unroll
         for (int a = 0; a < 3; a++) P[s6][a] = V[vk_(s6)][a] * V[vl_(s6)][a];
-      const float Dm[3][3] = {{D00, D01, D02}, {D01, D11, D12}, {D02, D12, D22}};
       {
         float Bv[21];
 #pragma unroll
@@ -366,18 +409,7 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
       }
       if (ORDER >= 2) {
         float D2[3][3][3];
-        const float dd[3][3] = {{0.f, d10, d20}, {0.f, 0.f, d21}, {0.f, 0.f, 0.f}};
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-          for (int j = i; j < 3; j++)
-#pragma unroll
-            for (int l = j; l < 3; l++) {
-              const float d = (i == j && j == l)
-                                  ? dd2_same_f<KIND>(lf[i], fl[i], Dm[i][i], C)
-                                  : dd2s_f<KIND>(lf[j], lf[l], fl[j], Dm[i][j], Dm[j][l], dd[i][j], dd[j][l], dd[i][l], C);
-              D2[i][j][l] = D2[i][l][j] = D2[j][i][l] = D2[j][l][i] = D2[l][i][j] = D2[l][j][i] = d;
-            }
+        smf_d2_f<KIND>(Sp, Dm, C, D2);
         float Tv[56];
 #pragma unroll
         for (int g = 0; g < 6; g++) {

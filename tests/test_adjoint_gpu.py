@@ -105,3 +105,53 @@ def test_third_derivative_refused_and_domain_nan():
     (h,) = torch.autograd.grad(g.sum(), B, create_graph=True)
     with pytest.raises(RuntimeError):
         torch.autograd.grad(h.sum(), B)
+
+
+@pytest.mark.parametrize("fam,kind,alpha", CASES)
+def test_adjoint_f32_against_fp64(fam, kind, alpha):
+    """the mixed-precision adjoints (smf_cuda_adjoint_f32 / gmf_cuda_adjoint_f32) against the FP64 adjoints on the
+    same FP32 values: max |x - ref| / max |ref| per output <= 1e-6, identical NaN positions; smf on the C2 workload
+    (condition numbers to 1e6, gaps to 1e-12), gmf on the C1 groups"""
+    import torch
+
+    from matfun_gb300 import workloads as w
+    from matfun_gb300.autograd import adjoint
+    n = 16000
+    A = (w.c1_gmf_groups(n, seed=11) if fam == "gmf" else w.c2_smf_spd(n, seed=11, as_voigt=False)).astype(np.float32)
+    rng = np.random.default_rng(12)
+    W = rng.standard_normal((n, 3, 3)).astype(np.float32)
+    V = rng.standard_normal((n, 3, 3)).astype(np.float32)
+    want = ("F", "Abar", "JV", "HWV")
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    r32 = adjoint(fam, kind, t(A), W=t(W), V=t(V), alpha=alpha, want=want)
+    r64 = adjoint(fam, kind, t(A).double(), W=t(W).double(), V=t(V).double(), alpha=alpha, want=want)
+    errs = {}
+    for k in want:
+        assert r32[k].dtype == torch.float32 and r64[k].dtype == torch.float64
+        got, ref = r32[k].double().cpu().numpy(), r64[k].cpu().numpy()
+        assert np.array_equal(np.isnan(got), np.isnan(ref)), k
+        errs[k] = maxrel(got, ref)
+    print(f"adjoint f32 {fam} {kind} {alpha}: " + " ".join(f"{k} {e:.2e}" for k, e in errs.items()))
+    assert max(errs.values()) <= 1e-6, errs
+
+
+def test_autograd_f32_gradient_and_hvp():
+    """float32 tensors run the FP32 adjoint kernels through autograd: gradient and Hessian-vector product close to the
+    float64 ones"""
+    import torch
+
+    from matfun_gb300 import autograd as ag
+    from matfun_gb300 import workloads as w
+    A = torch.from_numpy(w.c0_smf_spd(512, seed=4, as_voigt=False).astype(np.float32)).cuda()
+    Wd = torch.randn(512, 3, 3, device="cuda", generator=torch.Generator("cuda").manual_seed(1))
+    Vd = torch.randn(512, 3, 3, device="cuda", generator=torch.Generator("cuda").manual_seed(2))
+    out = {}
+    for dt in (torch.float32, torch.float64):
+        X = A.to(dt).requires_grad_(True)
+        L = (Wd.to(dt) * ag.smf("log", X)).sum()
+        g, = torch.autograd.grad(L, X, create_graph=True)
+        hv, = torch.autograd.grad((g * Vd.to(dt)).sum(), X)
+        out[dt] = (g.detach(), hv)
+        assert g.dtype == dt and hv.dtype == dt
+    for a, b in zip(out[torch.float32], out[torch.float64]):
+        assert float((a.double() - b).abs().max() / b.abs().max()) <= 1e-6
