@@ -24,15 +24,6 @@ struct SmfCoefF {
 
 MF_D float self(bool m, float a, float b) { return m ? a : b; }
 
-// x * 2^k for k in [-3, 1], exact for normal floats (exponent arithmetic), a multiplication otherwise
-MF_D float mulpow2f(float x, int k) {
-  if (k == 0) return x;
-  const int b = __float_as_int(x);
-  const int e = (b >> 23) & 0xFF;
-  if (e > 3 && e < 0xFE) return __int_as_float(b + (k << 23));
-  return x * __int_as_float((127 + k) << 23);
-}
-
 template <int KIND>
 MF_D float fun_f(float x, float al) {
   if (KIND == EXP) return expf(x);
@@ -462,7 +453,8 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
   for (int e = tid; e < cnt * NF; e += SMFX_TPB) F[base * NF + e] = sF[e];
   if (ORDER >= 1) {
     constexpr int KJ = (NJ + SMFX_TPB - 1) / SMFX_TPB;
-    int jidx[KJ], jexp[KJ];
+    int jidx[KJ];
+    float jw[KJ];  // layout weight 2^ex (an FP32 multiplication by a power of two is exact)
 #pragma unroll
     for (int k = 0; k < KJ; k++) {
       const int w = min(tid + SMFX_TPB * k, NJ - 1);
@@ -475,19 +467,20 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
         ex = I >= 3 ? -1 : 0;
       }
       jidx[k] = sym2(min(I, p), max(I, p));
-      jexp[k] = ex;
+      jw[k] = __int_as_float((127 + ex) << 23);
     }
     for (int mi = 0; mi < cnt; mi++) {
       float *o = J + (base + mi) * NJ;
       const float *s = sK + mi * 21;
 #pragma unroll
       for (int k = 0; k < KJ; k++)
-        if (tid + SMFX_TPB * k < NJ) o[tid + SMFX_TPB * k] = mulpow2f(s[jidx[k]], jexp[k]);
+        if (tid + SMFX_TPB * k < NJ) o[tid + SMFX_TPB * k] = s[jidx[k]] * jw[k];
     }
   }
   if (ORDER >= 2) {
     constexpr int KH = (NH + SMFX_TPB - 1) / SMFX_TPB;
-    int hidx[KH], hexp[KH];
+    int hidx[KH];
+    float hw[KH];
 #pragma unroll
     for (int k = 0; k < KH; k++) {
       const int w = min(tid + SMFX_TPB * k, NH - 1);
@@ -502,14 +495,14 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
       }
       sort3(I, p, q);
       hidx[k] = sym3(I, p, q);
-      hexp[k] = ex;
+      hw[k] = __int_as_float((127 + ex) << 23);
     }
     for (int mi = 0; mi < cnt; mi++) {
       float *o = H + (base + mi) * NH;
       const float *s = sG + mi * 56;
 #pragma unroll
       for (int k = 0; k < KH; k++)
-        if (tid + SMFX_TPB * k < NH) o[tid + SMFX_TPB * k] = mulpow2f(s[hidx[k]], hexp[k]);
+        if (tid + SMFX_TPB * k < NH) o[tid + SMFX_TPB * k] = s[hidx[k]] * hw[k];
     }
   }
 }
