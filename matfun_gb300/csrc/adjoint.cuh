@@ -406,10 +406,10 @@ __global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel_f32(int64_t n, co
   }
   __syncthreads();
   if (tid < cnt) {
-    double v6[6];
-    sym_voigt_f(sx + tid * 9, v6);
+    SmfInF in;
+    sym_in_f(sx + tid * 9, in);
     SmfSpecF Sp;
-    smf_spectrum_f<KIND>(v6, C, Sp);
+    smf_spectrum_f<KIND, true>(in, C, Sp);
     if (F) {
 #pragma unroll
       for (int a = 0; a < 3; a++)

@@ -1,0 +1,73 @@
+// ffloat.cuh -- float-float arithmetic on the FP32 pipe: a value x = hi + lo with |lo| <= ulp(hi) / 2 (about 48
+// significant bits, relative 2^-48 ~ 3.6e-15), built on the error-free transformations
+//   two_sum  (Knuth, TAOCP vol. 2, 4.2.2):       a + b = s + e exactly, s = fl(a + b)
+//   two_prod (with a fused multiply-add):        a * b = p + e exactly, p = fl(a * b)
+// and the compensated dot product Dot2 of Ogita, Rump and Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput.
+// 26 (2005)), whose result is as accurate as if computed in twice the working precision and then rounded.
+// On GB300 an FP64 instruction costs about 80 FP32 instruction slots, so a handful of these FP32 operations replaces
+// one FP64 operation at a fraction of its cost.  The code relies on IEEE FP32 semantics without reassociation (no
+// fast-math); products that must stay exact are written with fmaf explicitly.
+#pragma once
+#include "mf_common.cuh"
+
+namespace mf {
+
+struct ffl {
+  float hi, lo;
+};
+
+MF_D ffl two_sum(float a, float b) {
+  float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+MF_D ffl fast_two_sum(float a, float b) {  // |a| >= |b| (or a == 0)
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+MF_D ffl two_prod(float a, float b) {
+  float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+MF_D ffl ff_add(ffl x, ffl y) {  // accurate under cancellation of the high parts
+  ffl s = two_sum(x.hi, y.hi), t = two_sum(x.lo, y.lo);
+  s.lo += t.hi;
+  s = fast_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return fast_two_sum(s.hi, s.lo);
+}
+MF_D ffl ff_neg(ffl x) { return {-x.hi, -x.lo}; }
+MF_D ffl ff_sub(ffl x, ffl y) { return ff_add(x, ff_neg(y)); }
+MF_D ffl ff_mul_f(ffl x, float b) {
+  ffl p = two_prod(x.hi, b);
+  p.lo = fmaf(x.lo, b, p.lo);
+  return fast_two_sum(p.hi, p.lo);
+}
+MF_D ffl ff_mul(ffl x, ffl y) {
+  ffl p = two_prod(x.hi, y.hi);
+  p.lo = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, p.lo));
+  return fast_two_sum(p.hi, p.lo);
+}
+MF_D ffl ff_from(float a) { return {a, 0.f}; }
+
+// running compensated sum (Sum2 / Dot2 of Ogita-Rump-Oishi): S + E, every term added through two_sum
+struct ffacc {
+  float s, e;
+};
+MF_D void acc_add(ffacc &A, float t) {
+  ffl r = two_sum(A.s, t);
+  A.s = r.hi;
+  A.e += r.lo;
+}
+MF_D void acc_prod(ffacc &A, float a, float b) {  // += a * b (exact product)
+  ffl p = two_prod(a, b);
+  acc_add(A, p.hi);
+  A.e += p.lo;
+}
+MF_D void acc_ffprod(ffacc &A, ffl a, float b) {  // += a * b for a float-float a
+  ffl p = two_prod(a.hi, b);
+  acc_add(A, p.hi);
+  A.e = fmaf(a.lo, b, A.e + p.lo);
+}
+MF_D ffl acc_ff(const ffacc &A) { return two_sum(A.s, A.e); }
+
+}  // namespace mf

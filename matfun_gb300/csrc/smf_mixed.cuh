@@ -1,16 +1,17 @@
 // smf_mixed.cuh -- mixed-precision symmetric family: FP32 input and output, FP32 for the bulk of the arithmetic.
 //
-// FP64 is kept only where FP32 would lose the result:
-//   * the eigensystem (deviator, the cubic's trigonometric root, cross-product eigenvector, Jacobi rotation, Rayleigh
-//     quotients): with condition numbers up to 1e6 and eigenvalue gaps down to 1e-12 an FP32 eigensolve loses the
-//     small eigenvalues and the near-degenerate pairs entirely;
+// Beyond FP32 precision (float-float, ffloat.cuh, on the FP32 pipe) only where FP32 would lose the result:
+//   * the Rayleigh quotients that give the eigenvalues and the Gram matrix of the eigenvectors: with condition
+//     numbers up to 1e6 and eigenvalue gaps down to 1e-12 FP32 quotients lose the small eigenvalues and the
+//     near-degenerate pairs entirely;
 //   * the differences of eigenvalues that feed the near-coalescent branches of the divided differences (z, u, w and
-//     the denominators of the difference formulas), taken from the FP64 eigenvalues before rounding to FP32.
+//     the denominators of the difference formulas), taken from the float-float eigenvalues before rounding to FP32.
 // f(lambda), the first and second divided differences (stable forms, cluster series), the product vectors and the
-// J / H forms of smf_kernels.cuh run in FP32.  The FP64 share per matrix drops from ~2.5k to ~0.4k operations, so
-// on GB300 (FP64 at 1/74 of FP32) the kernel moves towards the HBM roofline, and FP32 storage halves the bytes.
+// J / H forms of smf_kernels.cuh run in FP32.  The kernel executes no FP64 instruction (the FP64 kernel: ~2.5k per
+// matrix, at 1/74 of the FP32 rate on GB300), so it moves towards the HBM roofline, and FP32 storage halves the bytes.
 // Accuracy against the FP64 oracle is stated per kind and order in the tests (<= 1e-6 relative, max-norm).
 #pragma once
+#include "ffloat.cuh"
 #include "smf_kernels.cuh"
 
 namespace mf {
@@ -105,47 +106,133 @@ MF_D float dd2_same_f(float lf, float fl, float Dll, const SmfCoefF &C) {
   return out;
 }
 
-// |x| of a double as an ordered integer key (max of magnitudes on the integer pipe)
-MF_D long long absbits(double x) { return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll; }
-MF_D long long kmax(long long a, long long b) { return a > b ? a : b; }
-
-// 2^-e for a power of two 2^e of normal range (exponent arithmetic, no division)
-MF_D double pow2inv(double p) {
-  long long e = (__double_as_longlong(p) >> 52) & 0x7FF;
-  return __longlong_as_double((2046ll - e) << 52);
-}
-
 MF_D float nrm3(float &x, float &y, float &z) {
   float n = __fsqrt_rn(x * x + y * y + z * z), i = __fdiv_rn(1.f, n);
   x *= i; y *= i; z *= i;
   return n;
 }
 
-// The eigensystem of the mixed path.  FP32: the cubic's trigonometric root (on the deviator normalised to max 1, where
-// the root of the separated eigenvalue is insensitive to rounding of r), its eigenvector (largest cross product of
-// two rows of G - root I), the orthonormal complement and the 2x2 Jacobi rotation.  FP64: the deviator and the
-// Rayleigh quotients of the FP32 vectors in the deviator shifted by minus half the root (the centre of the remaining
-// pair), so that the pair's block is of the size of its own gap: the rotation angle is then accurate relative to the
-// gap, and the quotients, divided by the vectors' FP64 squared norms (1 - e + e^2 with e = |x|^2 - 1), give the
-// eigenvalues to ~1e-14 relative to |A| (an FP32 vector error d moves a quotient by O(d^2)).  Eigenvalues and the
-// deviator's eigenvalues (xd, for log near the mean) are in the units of the input.
-struct SmfEigM {
-  double lam[3], xd[3], m;
+// The symmetric input of the mixed path: FP32 diagonal, float-float off-diagonal (the exact average of a_ij and a_ji
+// for the matrix layout; LO = false for Voigt input, whose off-diagonal entries are FP32 values)
+struct SmfInF {
+  float d[3];
+  ffl o[3];  // (0,1), (0,2), (1,2)
+};
+
+// x^T A x with the diagonal shifted by a float-float (A - mu I), compensated (Dot2) to float-float accuracy
+template <bool LO>
+MF_D ffl quad_ff(const ffl *dg, const ffl *o, float x0, float x1, float x2) {
+  const float x[3] = {x0, x1, x2};
+  ffacc A = {0.f, 0.f};
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    ffl p = two_prod(x[i], x[i]);
+    ffl t = two_prod(dg[i].hi, p.hi);
+    acc_add(A, t.hi);
+    A.e += fmaf(dg[i].hi, p.lo, fmaf(dg[i].lo, p.hi, t.lo));
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int i = k == 2 ? 1 : 0, j = k == 0 ? 1 : 2;
+    ffl p = two_prod(2.f * x[i], x[j]);
+    ffl t = two_prod(o[k].hi, p.hi);
+    acc_add(A, t.hi);
+    A.e += LO ? fmaf(o[k].hi, p.lo, fmaf(o[k].lo, p.hi, t.lo)) : fmaf(o[k].hi, p.lo, t.lo);
+  }
+  return acc_ff(A);
+}
+
+// x^T A y (A as above)
+template <bool LO>
+MF_D ffl bil_ff(const ffl *dg, const ffl *o, const float *x, const float *y) {
+  ffacc A = {0.f, 0.f};
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    ffl p = two_prod(x[i], y[i]);
+    ffl t = two_prod(dg[i].hi, p.hi);
+    acc_add(A, t.hi);
+    A.e += fmaf(dg[i].hi, p.lo, fmaf(dg[i].lo, p.hi, t.lo));
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int i = k == 2 ? 1 : 0, j = k == 0 ? 1 : 2;
+    ffl p1 = two_prod(x[i], y[j]), p2 = two_prod(x[j], y[i]);
+    ffl s = two_sum(p1.hi, p2.hi);
+    float sl = s.lo + (p1.lo + p2.lo);
+    ffl t = two_prod(o[k].hi, s.hi);
+    acc_add(A, t.hi);
+    A.e += LO ? fmaf(o[k].hi, sl, fmaf(o[k].lo, s.hi, t.lo)) : fmaf(o[k].hi, sl, t.lo);
+  }
+  return acc_ff(A);
+}
+
+MF_D ffl dot_ff(const float *x, const float *y) {
+  ffacc A = {0.f, 0.f};
+#pragma unroll
+  for (int i = 0; i < 3; i++) acc_prod(A, x[i], y[i]);
+  return acc_ff(A);
+}
+
+// q / n for n = 1 + e close to 1: q (1 - e + e^2), float-float
+MF_D ffl div_norm(ffl q, ffl n) {
+  float e = (n.hi - 1.f) + n.lo;
+  return ff_mul(q, fast_two_sum(1.f, e * e - e));
+}
+
+// The eigensystem of the mixed path, with no FP64: FP32 for the cubic's trigonometric root (on the deviator normalised
+// to max 1, where the root of the separated eigenvalue is insensitive to rounding of r), its eigenvector (largest
+// cross product of two rows of G - root I), the orthonormal complement and the 2x2 Jacobi rotation; float-float
+// (ffloat.cuh) for the deviator, the Rayleigh quotients of the FP32 vectors and their Gram matrix.  The quotients
+// are taken in A - mu I, mu the centre of the remaining pair, so that the pair's block is of the size of its own gap:
+// the rotation angle is accurate relative to the gap, and the quotients divided by the vectors' squared norms give
+// the eigenvalues to ~1e-14 relative to |A| (an FP32 vector error d moves a quotient by O(d^2)).  One Newton-Schulz
+// step V (3 I - V^T V) / 2 with the float-float Gram matrix leaves the FP32 vectors orthonormal to the rounding of
+// their components.  Input scaled by a power of two; eigenvalues and the deviator's eigenvalues (xd, for log near
+// the mean) in the units of the input.
+struct SmfEigF {
+  ffl lam[3], xd[3];
+  float m;
   float V[3][3];
 };
 
-template <int KIND>
-MF_D void smf_eigsys_mixed(const double *v, SmfEigM &E) {
+template <int KIND, bool LO>
+MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E) {
   constexpr float SQRT6 = 2.4494897f, TWO_PI_3 = 2.0943951f;
-  double m = (v[0] + v[1] + v[2]) * (1.0 / 3.0);
-  double d0 = v[0] - m, d1 = v[1] - m, d2 = v[2] - m;
-  long long k01 = kmax(absbits(d0), absbits(d1)), k23 = kmax(absbits(d2), absbits(v[3]));
-  long long k45 = kmax(absbits(v[4]), absbits(v[5]));
-  double dmax = __longlong_as_double(kmax(kmax(k01, k23), k45));
-  bool bad = !(dmax < 1e300), iso = !(dmax > 0.0) | bad;  // bad: NaN or infinite input (NaN vectors and results)
-  double dsc = sel(iso, 1.0, pow2floor(dmax)), ids = pow2inv(dsc);
-  float g0 = (float)(d0 * ids), g1 = (float)(d1 * ids), g2 = (float)(d2 * ids);
-  float g3 = (float)(v[3] * ids), g4 = (float)(v[4] * ids), g5 = (float)(v[5] * ids);
+  // power-of-two scaling from the largest magnitude (integer compare of the bit patterns: NaN sorts above Inf)
+  int kb = 0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) kb = max(kb, __float_as_int(in.d[i]) & 0x7FFFFFFF);
+#pragma unroll
+  for (int k = 0; k < 3; k++) kb = max(kb, __float_as_int(in.o[k].hi) & 0x7FFFFFFF);
+  const bool bad = kb >= 0x7F800000;  // NaN or infinite input: NaN vectors and results
+  int ex = min(max((kb >> 23) & 0xFF, 1), 253);
+  const float sig = __int_as_float(ex << 23), isig = __int_as_float((254 - ex) << 23);
+  float a[3];
+  ffl o[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) a[i] = in.d[i] * isig;
+#pragma unroll
+  for (int k = 0; k < 3; k++) o[k] = {in.o[k].hi * isig, LO ? in.o[k].lo * isig : 0.f};
+  // mean of the diagonal and deviator, float-float
+  ffl s01 = two_sum(a[0], a[1]), s = two_sum(s01.hi, a[2]);
+  s = fast_two_sum(s.hi, s.lo + s01.lo);
+  float q1 = s.hi / 3.f;
+  float q2 = (fmaf(-q1, 3.f, s.hi) + s.lo) / 3.f;
+  const ffl m = fast_two_sum(q1, q2);
+  float dv[3];  // deviator in FP32 (the input of the trigonometric root only)
+#pragma unroll
+  for (int i = 0; i < 3; i++) dv[i] = a[i] - m.hi;
+  // FP32: normalised deviator, trigonometric root, eigenvector, complement
+  int kd = 0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) kd = max(kd, __float_as_int(dv[i]) & 0x7FFFFFFF);
+#pragma unroll
+  for (int k = 0; k < 3; k++) kd = max(kd, __float_as_int(o[k].hi) & 0x7FFFFFFF);
+  const bool iso = (kd == 0) | bad;
+  const int ed = min(max((kd >> 23) & 0xFF, 1), 253);
+  const float dsc = __int_as_float(ed << 23), ids = __int_as_float((254 - ed) << 23);
+  float g0 = dv[0] * ids, g1 = dv[1] * ids, g2 = dv[2] * ids;
+  float g3 = o[0].hi * ids, g4 = o[1].hi * ids, g5 = o[2].hi * ids;
   float p = g0 * g0 + g1 * g1 + g2 * g2 + 2.f * (g3 * g3 + g4 * g4 + g5 * g5);
   float q = g0 * (g1 * g2 - g5 * g5) - g3 * (g3 * g2 - g5 * g4) + g4 * (g3 * g5 - g1 * g4);
   float pg = self(iso, 1.f, p), qg = self(iso, 0.f, q);
@@ -161,103 +248,121 @@ MF_D void smf_eigsys_mixed(const double *v, SmfEigM &E) {
     float nb = bx * bx + by * by + bz * bz;
     bool s1 = nb > nn;
     cxv = self(s1, bx, cxv); cyv = self(s1, by, cyv); czv = self(s1, bz, czv); nn = self(s1, nb, nn);
-    float ex = m11 * m22 - g5 * g5, ey = g5 * g4 - g3 * m22, ez = g3 * g5 - m11 * g4;
-    float ne = ex * ex + ey * ey + ez * ez;
+    float ex2 = m11 * m22 - g5 * g5, ey2 = g5 * g4 - g3 * m22, ez2 = g3 * g5 - m11 * g4;
+    float ne = ex2 * ex2 + ey2 * ey2 + ez2 * ez2;
     bool s2 = ne > nn;
-    cxv = self(s2, ex, cxv); cyv = self(s2, ey, cyv); czv = self(s2, ez, czv); nn = self(s2, ne, nn);
+    cxv = self(s2, ex2, cxv); cyv = self(s2, ey2, cyv); czv = self(s2, ez2, czv); nn = self(s2, ne, nn);
   }
   bool ok = (nn > 1e-30f) & !iso;
-  float vx = self(ok, cxv, 1.f), vy = self(ok, cyv, 0.f), vz = self(ok, czv, 0.f);
-  nrm3(vx, vy, vz);
-  float ax = fabsf(vx), ay = fabsf(vy), az = fabsf(vz);
+  float v[3] = {self(ok, cxv, 1.f), self(ok, cyv, 0.f), self(ok, czv, 0.f)};
+  nrm3(v[0], v[1], v[2]);
+  float ax = fabsf(v[0]), ay = fabsf(v[1]), az = fabsf(v[2]);
   bool k1 = ay < ax, k2 = az < self(k1, ay, ax);
-  float ex = self(k1 | k2, 0.f, 1.f), ey = self(k1 & !k2, 1.f, 0.f), ez = self(k2, 1.f, 0.f);
-  float vk = ex * vx + ey * vy + ez * vz;
-  float ux = ex - vk * vx, uy = ey - vk * vy, uz = ez - vk * vz;
-  nrm3(ux, uy, uz);
-  float wx = vy * uz - vz * uy, wy = vz * ux - vx * uz, wz = vx * uy - vy * ux;
-  // FP64: quotients in the shifted deviator Ds = D + s I, s = root * dsc / 2
-  double s = sel(iso, 0.0, (double)sh * dsc * 0.5);
-  double e0 = d0 + s, e1 = d1 + s, e2 = d2 + s, o3 = v[3], o4 = v[4], o5 = v[5];
-  double Vx = vx, Vy = vy, Vz = vz, Ux = ux, Uy = uy, Uz = uz, Wx = wx, Wy = wy, Wz = wz;
-  double Dvx = e0 * Vx + o3 * Vy + o4 * Vz, Dvy = o3 * Vx + e1 * Vy + o5 * Vz, Dvz = o4 * Vx + o5 * Vy + e2 * Vz;
-  double Dux = e0 * Ux + o3 * Uy + o4 * Uz, Duy = o3 * Ux + e1 * Uy + o5 * Uz, Duz = o4 * Ux + o5 * Uy + e2 * Uz;
-  double Dwx = e0 * Wx + o3 * Wy + o4 * Wz, Dwy = o3 * Wx + e1 * Wy + o5 * Wz, Dwz = o4 * Wx + o5 * Wy + e2 * Wz;
-  double qv = Vx * Dvx + Vy * Dvy + Vz * Dvz, nv = Vx * Vx + Vy * Vy + Vz * Vz;
-  double b11 = Ux * Dux + Uy * Duy + Uz * Duz, b12 = Ux * Dwx + Uy * Dwy + Uz * Dwz;
-  double b22 = Wx * Dwx + Wy * Dwy + Wz * Dwz;
-  double uu = Ux * Ux + Uy * Uy + Uz * Uz, uw = Ux * Wx + Uy * Wy + Uz * Wz, ww = Wx * Wx + Wy * Wy + Wz * Wz;
-  // FP32 Jacobi rotation of the pair from the FP64 block (its entries are of the size of the pair's gap)
-  float jx = (float)(b11 - b22), jy = (float)(b12 + b12), jr = sqrtf(jx * jx + jy * jy);
+  float ex1 = self(k1 | k2, 0.f, 1.f), ey1 = self(k1 & !k2, 1.f, 0.f), ez1 = self(k2, 1.f, 0.f);
+  float vk = ex1 * v[0] + ey1 * v[1] + ez1 * v[2];
+  float u[3] = {ex1 - vk * v[0], ey1 - vk * v[1], ez1 - vk * v[2]};
+  nrm3(u[0], u[1], u[2]);
+  float w[3] = {v[1] * u[2] - v[2] * u[1], v[2] * u[0] - v[0] * u[2], v[0] * u[1] - v[1] * u[0]};
+  // float-float: quotients in A - mu I, mu = mean - root / 2 (the centre of the remaining pair)
+  const float mu = self(iso, m.hi, m.hi - 0.5f * (sh * dsc));
+  ffl dg[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) dg[i] = two_sum(a[i], -mu);
+  const ffl qv = quad_ff<LO>(dg, o, v[0], v[1], v[2]), nv = dot_ff(v, v);
+  const ffl b11 = quad_ff<LO>(dg, o, u[0], u[1], u[2]), b22 = quad_ff<LO>(dg, o, w[0], w[1], w[2]);
+  const ffl b12 = bil_ff<LO>(dg, o, u, w);
+  // FP32 Jacobi rotation of the pair from the block (its entries are of the size of the pair's gap)
+  ffl jd = ff_sub(b11, b22);
+  float jx = jd.hi + jd.lo, jy = 2.f * (b12.hi + b12.lo), jr = sqrtf(jx * jx + jy * jy);
   bool jz = !(jr > 0.f), jpos = jx >= 0.f;
   float jrs = self(jz, 1.f, jr);
   float big = sqrtf((jrs + fabsf(jx)) / (2.f * jrs)), sml = jy / (2.f * jrs * big);
   float sgn = self(jy >= 0.f, 1.f, -1.f);
   float cs = self(jz, 1.f, self(jpos, big, sgn * sml)), sn = self(jz, 0.f, self(jpos, sml, sgn * big));
-  double C = cs, S = sn, CC = C * C, SS = S * S, CS2 = 2.0 * (C * S);
-  double n1 = CC * uu + CS2 * uw + SS * ww - 1.0, n2 = SS * uu - CS2 * uw + CC * ww - 1.0, n0 = nv - 1.0;
-  double t0 = qv * (1.0 - n0 + n0 * n0);
-  double t1 = (CC * b11 + CS2 * b12 + SS * b22) * (1.0 - n1 + n1 * n1);
-  double t2 = (SS * b11 - CS2 * b12 + CC * b22) * (1.0 - n2 + n2 * n2);
-  E.xd[0] = t0 - s; E.xd[1] = t1 - s; E.xd[2] = t2 - s;
-  E.lam[0] = m + E.xd[0]; E.lam[1] = m + E.xd[1]; E.lam[2] = m + E.xd[2];
-  E.m = m;
-  float r1x = cs * ux + sn * wx, r1y = cs * uy + sn * wy, r1z = cs * uz + sn * wz;
-  float r2x = cs * wx - sn * ux, r2y = cs * wy - sn * uy, r2z = cs * wz - sn * uz;
-  // one Newton-Schulz step V <- V (3 I - V^T V) / 2 with the Gram matrix in FP64: the FP32 vectors come out
-  // orthonormal to the rounding of their components (an FP32 Gram matrix would leave its own rounding in them)
-  double R1x = r1x, R1y = r1y, R1z = r1z, R2x = r2x, R2y = r2y, R2z = r2z;
-  float e00 = (float)(n0 * 0.5), e11 = (float)((R1x * R1x + R1y * R1y + R1z * R1z - 1.0) * 0.5);
-  float e22 = (float)((R2x * R2x + R2y * R2y + R2z * R2z - 1.0) * 0.5);
-  float e01 = (float)((Vx * R1x + Vy * R1y + Vz * R1z) * 0.5), e02 = (float)((Vx * R2x + Vy * R2y + Vz * R2z) * 0.5);
-  float e12 = (float)((R1x * R2x + R1y * R2y + R1z * R2z) * 0.5);
-  float c0[3] = {vx, vy, vz}, c1[3] = {r1x, r1y, r1z}, c2[3] = {r2x, r2y, r2z};
+  float r1[3] = {cs * u[0] + sn * w[0], cs * u[1] + sn * w[1], cs * u[2] + sn * w[2]};
+  float r2[3] = {cs * w[0] - sn * u[0], cs * w[1] - sn * u[1], cs * w[2] - sn * u[2]};
+  const ffl n1 = dot_ff(r1, r1), n2 = dot_ff(r2, r2);
+  const ffl q1f = quad_ff<LO>(dg, o, r1[0], r1[1], r1[2]), q2f = quad_ff<LO>(dg, o, r2[0], r2[1], r2[2]);
+  const ffl th[3] = {div_norm(qv, nv), div_norm(q1f, n1), div_norm(q2f, n2)};
+  const ffl mum = ff_sub(ff_from(mu), m);  // mu - mean
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const ffl lam = ff_add(th[i], ff_from(mu));
+    E.lam[i] = {lam.hi * sig, lam.lo * sig};
+    const ffl xd = ff_add(th[i], mum);
+    E.xd[i] = {xd.hi * sig, xd.lo * sig};
+  }
+  E.m = m.hi * sig;
+  // Newton-Schulz step with the float-float Gram matrix
+  const ffl g01 = dot_ff(v, r1), g02 = dot_ff(v, r2), g12 = dot_ff(r1, r2);
+  float e00 = 0.5f * ((nv.hi - 1.f) + nv.lo), e11 = 0.5f * ((n1.hi - 1.f) + n1.lo);
+  float e22 = 0.5f * ((n2.hi - 1.f) + n2.lo);
+  float e01 = 0.5f * (g01.hi + g01.lo), e02 = 0.5f * (g02.hi + g02.lo), e12 = 0.5f * (g12.hi + g12.lo);
   float nanv = __int_as_float(0x7FC00000);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    E.V[i][0] = self(bad, nanv, c0[i] - (c0[i] * e00 + c1[i] * e01 + c2[i] * e02));
-    E.V[i][1] = self(bad, nanv, c1[i] - (c0[i] * e01 + c1[i] * e11 + c2[i] * e12));
-    E.V[i][2] = self(bad, nanv, c2[i] - (c0[i] * e02 + c1[i] * e12 + c2[i] * e22));
+    E.V[i][0] = self(bad, nanv, v[i] - (v[i] * e00 + r1[i] * e01 + r2[i] * e02));
+    E.V[i][1] = self(bad, nanv, r1[i] - (v[i] * e01 + r1[i] * e11 + r2[i] * e12));
+    E.V[i][2] = self(bad, nanv, r2[i] - (v[i] * e02 + r1[i] * e12 + r2[i] * e22));
+  }
+  if (bad) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) E.lam[i] = E.xd[i] = {nanv, nanv};
   }
 }
 
-// symmetric part of an FP32 3x3 matrix as Voigt values in FP64; all NaN if |a_ij - a_ji| > 1e-8 max |a_kl|
-// (smf_kernel.hpp:408-421), checked in FP64 on the FP32 values
-MF_D void sym_voigt_f(const float *xi, double *v) {
-  double a9[9], mx = 0.0;
+// Voigt input (FP32 values)
+MF_D void voigt_in_f(const float *xi, SmfInF &in) {
 #pragma unroll
-  for (int k = 0; k < 9; k++) { a9[k] = xi[k]; mx = sel(fabs(a9[k]) > mx, fabs(a9[k]), mx); }
-  const double tol = 1e-8 * mx;
-  bool sym = !(fabs(a9[1] - a9[3]) > tol) & !(fabs(a9[2] - a9[6]) > tol) & !(fabs(a9[5] - a9[7]) > tol);
-  v[0] = a9[0]; v[1] = a9[4]; v[2] = a9[8];
-  v[3] = 0.5 * (a9[1] + a9[3]); v[4] = 0.5 * (a9[2] + a9[6]); v[5] = 0.5 * (a9[5] + a9[7]);
+  for (int i = 0; i < 3; i++) in.d[i] = xi[i];
 #pragma unroll
-  for (int k = 0; k < 6; k++) v[k] = sel(sym, v[k], __longlong_as_double(0x7FF8000000000000ll));
+  for (int k = 0; k < 3; k++) in.o[k] = {xi[3 + k], 0.f};
+}
+
+// symmetric part of an FP32 3x3 matrix: the off-diagonal averages exactly as float-float; all NaN if
+// |a_ij - a_ji| > 1e-8 max |a_kl| (smf_kernel.hpp:408-421)
+MF_D void sym_in_f(const float *xi, SmfInF &in) {
+  float mx = 0.f;
+#pragma unroll
+  for (int k = 0; k < 9; k++) mx = fmaxf(mx, fabsf(xi[k]));
+  const float tol = 1e-8f * mx;
+  const bool sym = !(fabsf(xi[1] - xi[3]) > tol) & !(fabsf(xi[2] - xi[6]) > tol) & !(fabsf(xi[5] - xi[7]) > tol);
+  const float nanv = __int_as_float(0x7FC00000);
+  in.d[0] = self(sym, xi[0], nanv); in.d[1] = self(sym, xi[4], nanv); in.d[2] = self(sym, xi[8], nanv);
+  const int ia[3] = {1, 2, 5}, ib[3] = {3, 6, 7};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    ffl t = two_sum(xi[ia[k]], xi[ib[k]]);
+    in.o[k] = {self(sym, 0.5f * t.hi, nanv), self(sym, 0.5f * t.lo, nanv)};
+  }
 }
 
 // the spectrum of the mixed path, eigenvalues sorted ascending: FP32 eigenvectors V (columns), eigenvalues lf,
-// their differences taken in FP64 and rounded once (d10 = l1 - l0, d21, d20), and f(lambda) (log near the mean
-// through log1p of the deviator's eigenvalue, smf_kernel.hpp:283-290); powers see max(lambda, 0)
+// their differences taken in float-float and rounded once (d10 = l1 - l0, d21, d20), and f(lambda) (log near the
+// mean through log1p of the deviator's eigenvalue, smf_kernel.hpp:283-290); powers see max(lambda, 0)
 struct SmfSpecF {
   float lf[3], fl[3], V[3][3], d10, d21, d20;
 };
 
-template <int KIND>
-MF_D void smf_spectrum_f(const double *v, const SmfCoefF &C, SmfSpecF &Sp) {
-  SmfEigM E;
-  smf_eigsys_mixed<KIND>(v, E);
-  double lam[3] = {E.lam[0], E.lam[1], E.lam[2]}, xd[3] = {E.xd[0], E.xd[1], E.xd[2]};
+MF_D bool ff_less(ffl a, ffl b) { return (a.hi < b.hi) | ((a.hi == b.hi) & (a.lo < b.lo)); }
+MF_D ffl ff_sel(bool c, ffl a, ffl b) { return {self(c, a.hi, b.hi), self(c, a.lo, b.lo)}; }
+
+template <int KIND, bool LO>
+MF_D void smf_spectrum_f(const SmfInF &in, const SmfCoefF &C, SmfSpecF &Sp) {
+  SmfEigF E;
+  smf_eigsys_ff<KIND, LO>(in, E);
+  ffl lam[3] = {E.lam[0], E.lam[1], E.lam[2]}, xd[3] = {E.xd[0], E.xd[1], E.xd[2]};
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) Sp.V[i][j] = E.V[i][j];
 #pragma unroll
-  for (int st = 0; st < 3; st++) {  // sort ascending (FP64 keys): a static order for every divided difference
+  for (int st = 0; st < 3; st++) {  // sort ascending: a static order for every divided difference
     const int a = st == 1 ? 1 : 0, b = a + 1;
-    bool sw = lam[b] < lam[a];
-    double la = lam[a], lb = lam[b], xa = xd[a], xb = xd[b];
-    lam[a] = sel(sw, lb, la); lam[b] = sel(sw, la, lb);
-    xd[a] = sel(sw, xb, xa); xd[b] = sel(sw, xa, xb);
+    bool sw = ff_less(lam[b], lam[a]);
+    ffl la = lam[a], lb = lam[b], xa = xd[a], xb = xd[b];
+    lam[a] = ff_sel(sw, lb, la); lam[b] = ff_sel(sw, la, lb);
+    xd[a] = ff_sel(sw, xb, xa); xd[b] = ff_sel(sw, xa, xb);
 #pragma unroll
     for (int r = 0; r < 3; r++) {
       float va = Sp.V[r][a], vb = Sp.V[r][b];
@@ -266,18 +371,19 @@ MF_D void smf_spectrum_f(const double *v, const SmfCoefF &C, SmfSpecF &Sp) {
   }
   if (KIND == POW || KIND == SQRT) {
 #pragma unroll
-    for (int i = 0; i < 3; i++) lam[i] = sel(lam[i] > 0.0, lam[i], 0.0);
+    for (int i = 0; i < 3; i++) lam[i] = ff_sel(ff_less(ffl{0.f, 0.f}, lam[i]), lam[i], ffl{0.f, 0.f});
   }
 #pragma unroll
-  for (int i = 0; i < 3; i++) Sp.lf[i] = (float)lam[i];
-  Sp.d10 = (float)(lam[1] - lam[0]); Sp.d21 = (float)(lam[2] - lam[1]); Sp.d20 = (float)(lam[2] - lam[0]);
+  for (int i = 0; i < 3; i++) Sp.lf[i] = lam[i].hi;
+  ffl t10 = ff_sub(lam[1], lam[0]), t21 = ff_sub(lam[2], lam[1]), t20 = ff_sub(lam[2], lam[0]);
+  Sp.d10 = t10.hi + t10.lo; Sp.d21 = t21.hi + t21.lo; Sp.d20 = t20.hi + t20.lo;
 #pragma unroll
   for (int i = 0; i < 3; i++) Sp.fl[i] = fun_f<KIND>(Sp.lf[i], C.al);
   if (KIND == LOG) {
-    float mf = (float)E.m, lms = logf(mf);
+    float mf = E.m, lms = logf(mf);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      float x = (float)xd[i];
+      float x = xd[i].hi + xd[i].lo;
       Sp.fl[i] = self(fabsf(x) <= 0.5f * mf, lms + log1pf(x / mf), Sp.fl[i]);
     }
   }
@@ -333,16 +439,12 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
   for (int e = tid; e < cnt * NIN; e += SMFX_TPB) sX[e] = x[base * NIN + e];
   __syncthreads();
   if (tid < cnt) {
-    double v[6];
     const float *xi = sX + tid * NIN;
-    if (MAT) {
-      sym_voigt_f(xi, v);
-    } else {
-#pragma unroll
-      for (int k = 0; k < 6; k++) v[k] = xi[k];
-    }
+    SmfInF in;
+    if (MAT) sym_in_f(xi, in);
+    else voigt_in_f(xi, in);
     SmfSpecF Sp;
-    smf_spectrum_f<KIND>(v, C, Sp);
+    smf_spectrum_f<KIND, MAT>(in, C, Sp);
     const float(&V)[3][3] = Sp.V;
     const float *fl = Sp.fl;
     float Fv[6];
