@@ -162,10 +162,13 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
       }
       __syncwarp();
       T *o = J + (base + mi) * 81;
+      const bool one1 = sc1 == T(1);  // folded (the common case): no multiply per entry; uniform in the warp
       for (int w = lane; w < 81; w += 32) {
         const int a = w / 27, b = (w / 9) % 3, c = (w / 3) % 3, d = w % 3;
         const int p1 = 3 * a + c, p2 = 3 * d + b;
-        o[w] = wk[54 + sym2(min(p1, p2), max(p1, p2))] * sc1;
+        const T v = wk[54 + sym2(min(p1, p2), max(p1, p2))];
+        if (one1) o[w] = v;
+        else o[w] = v * sc1;
       }
       __syncwarp();
     }
@@ -199,9 +202,16 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
       }
       __syncwarp();
       T *o = H + (base + mi) * 729;
-      for (int w = lane; w < 729; w += 32) {
-        const unsigned short e = S.hmap[w];
-        o[w] = (T6[e & 255] + T6[e >> 8]) * sc2;
+      if (sc2 == T(1)) {
+        for (int w = lane; w < 729; w += 32) {
+          const unsigned short e = S.hmap[w];
+          o[w] = T6[e & 255] + T6[e >> 8];
+        }
+      } else {
+        for (int w = lane; w < 729; w += 32) {
+          const unsigned short e = S.hmap[w];
+          o[w] = (T6[e & 255] + T6[e >> 8]) * sc2;
+        }
       }
       __syncwarp();
     }

@@ -1,9 +1,11 @@
 // host.cu -- host-buffer entry points: the reference's CPU API (smf_eval, smf_eval_matrix, gmf_eval of
 // c/include/matfun/matfun.h:28-41: host arrays, synchronous, -1 / -3 return codes) evaluated on the current GPU.
 //
-// The batch is cut into chunks; chunk k is copied in, evaluated and copied out on stream k % 2, so that the copies of
-// one chunk overlap the kernel of the next (two copy directions and the SMs busy at once).  With page-locked host
-// buffers the copies run at the link's rate; with pageable buffers the results are the same and the copies slower.
+// Page-locked host arrays (cudaHostAlloc / cudaMallocHost / registered) are mapped into the GPU's address space, and on
+// GB300 the GPU reaches host memory over NVLink-C2C: when every array of a call is page-locked and mapped, the kernels
+// read the inputs and write F, J, H in place, with no device buffer and no copy engine (the stores stream over the
+// link while the SMs compute).  Otherwise (pageable arrays) the batch is cut into chunks; chunk k is copied in,
+// evaluated and copied out on stream k % 2, so that the copies of one chunk overlap the kernel of the next.
 // Device buffers and streams are kept per device; calls on the same device are serialised by a mutex.
 #include <climits>
 #include <cstdint>
@@ -70,6 +72,20 @@ cudaError_t launch(int fam, int kind, double alpha, int64_t n, const double *x, 
   }
 }
 
+// the device address of a page-locked, mapped host array (null for a null pointer); false for anything else
+bool mapped(const void *p, void **dev) {
+  *dev = nullptr;
+  if (!p) return true;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+  *dev = a.devicePointer;
+  return true;
+}
+
 int host_eval(int fam, int kind, double alpha, int64_t n, const double *x, double *F, double *J, double *H) {
   // argument checks and normalisation of c/src/matfun.cc:23-32
   if (kind < SMF_EXP || kind > SMF_SQRT || n < 0 || (H && !J) || (kind == SMF_POW && !(alpha > 0))) return -1;
@@ -83,6 +99,25 @@ int host_eval(int fam, int kind, double alpha, int64_t n, const double *x, doubl
   std::lock_guard<std::mutex> lock(d.mu);
   const int order = H ? 2 : (J ? 1 : 0);
   const int64_t nin = fam == VOIGT ? 6 : 9, nf = nin, nj = J ? nf * nf : 0, nh = H ? nf * nf * nf : 0;
+  void *mx, *mF, *mJ, *mH;
+  if (mapped(x, &mx) & mapped(F, &mF) & mapped(J, &mJ) & mapped(H, &mH)) {
+    // in place over the host link: launches of at most 2^26 matrices on one stream, then one synchronisation
+    if (ensure(d, 0) != cudaSuccess) return -2;
+    cudaStream_t st = d.st[0];
+    cudaError_t e = fam == MATRIX ? cudaMemsetAsync(d.asym, 0, sizeof(int), st) : cudaSuccess;
+    const int64_t step = (int64_t)1 << 26;
+    for (int64_t lo = 0; lo < n && e == cudaSuccess; lo += step) {
+      const int64_t m = n - lo < step ? n - lo : step;
+      e = launch(fam, kind, alpha, m, (const double *)mx + lo * nin, (double *)mF + lo * nf,
+                 J ? (double *)mJ + lo * nj : nullptr, H ? (double *)mH + lo * nh : nullptr, st,
+                 fam == MATRIX ? d.asym : nullptr);
+    }
+    int asym = 0;
+    if (e == cudaSuccess && fam == MATRIX) e = cudaMemcpyAsync(&asym, d.asym, sizeof(int), cudaMemcpyDeviceToHost, st);
+    const cudaError_t es = cudaStreamSynchronize(st);
+    if (e != cudaSuccess || es != cudaSuccess) return -2;
+    return asym ? -3 : 0;
+  }
   const int64_t C = n < chunk_for(order) ? n : chunk_for(order);
   const int64_t per = nin + nf + nj + nh;
   if (ensure(d, (size_t)(2 * C * per)) != cudaSuccess) return -2;

@@ -76,3 +76,33 @@ def test_pinned_buffers_and_names(shim):
     assert r == 0
     o = ol.call(ol.oracle(), "gmf_eval", 0, 0.0, X.numpy(), 2, 9)
     assert maxrel(H.numpy(), o[3]) <= 1e-12 and maxrel(F.numpy(), o[1]) <= 1e-12
+
+
+@pytest.mark.parametrize("fam", ["smf_matrix", "gmf"])
+def test_in_place_path_equals_chunked_copies(shim, fam):
+    """every array page-locked: the kernels read and write host memory in place over the host link; the results are
+    those of the chunked copy path (pageable arrays) bit for bit, and -3 for a non-symmetric matrix as there"""
+    import torch
+
+    import matfun_gb300
+    from matfun_gb300 import workloads as w
+    lib = matfun_gb300.load()
+    n = (1 << 16) + 123
+    if fam == "gmf":
+        A = w.c1_gmf_groups(4 * ((n + 3) // 4), seed=21)[:n].reshape(n, 9)
+        fn, code = lib.gmf_cuda_eval_host, 0
+    else:
+        A = w.c0_smf_spd(n, seed=21, as_voigt=False).reshape(n, 9)
+        A[777, 2] += 0.5  # not symmetric: -3 and NaN results for that matrix
+        fn, code = lib.smf_cuda_eval_matrix_host, -3
+    outs = {}
+    for pinned in (True, False):
+        tens = [torch.from_numpy(np.ascontiguousarray(A))] + [torch.full((n, k), 3.0, dtype=torch.float64)
+                                                               for k in (9, 81, 729)]
+        if pinned:
+            tens = [t.pin_memory() for t in tens]
+        assert fn(1, 0.0, n, *[t.data_ptr() for t in tens]) == code
+        outs[pinned] = [t.numpy() for t in tens[1:]]
+    for a, b in zip(outs[True], outs[False]):
+        assert np.array_equal(np.isnan(a), np.isnan(b))
+        assert np.array_equal(np.nan_to_num(a), np.nan_to_num(b))
