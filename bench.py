@@ -30,7 +30,11 @@ BYTES_PER_MATRIX = {0: 72 + 72, 1: 72 + 72 + 648, 2: 72 + 72 + 648 + 5832}  # FP
 METRIC = "gmf log order-2 matrices/s (FP64)"
 # FP64 floating-point operations per matrix executed by gmf_kernel<KIND, 2> on this workload (2 per DFMA), from the
 # ncu counters smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum (profiles/gmf_kernel_log_o2_c1.md)
-FP64_FLOP_PER_MATRIX = {"log": 2 * 3434 + 1789 + 2176}
+FP64_FLOP_PER_MATRIX = {"log": 2 * 3456 + 1805 + 1283}
+# DRAM bytes per matrix of gmf_kernel<LOG, 2> from one ncu capture at n = 65536 on the same workload (374.2 MB read +
+# written; the last writes of that launch still sit in L2 when the kernel ends, so a full launch moves up to the
+# algorithmic 6624 B per matrix)
+NCU_DRAM_BYTES_PER_MATRIX = 374.2e6 / 65536
 
 
 def peaks():
@@ -485,7 +489,10 @@ def run_ours(args, rank, world, local):
                           "parallelism": f"independent matrices x{world}"},
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                             "frac": achieved / hbm, "peak_source": peak_kind,
-                            "traffic": None,
+                            "traffic": (NCU_DRAM_BYTES_PER_MATRIX * n / 1e9) if args.kind == "log" else None,
+                            "traffic_unit": "GB per launch",
+                            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of gmf_kernel<LOG,2> "
+                                              "at n=65536 (374.2 MB), scaled by n",
                             "note": "algorithmic bytes (72 in + 6552 out per matrix) / event time; the kernel is "
                                     "bound by the FP64 pipe (see fp64), not by HBM"},
                "fp64": {"peak_tflops": fp64_peak.value if fp64_ok else None,

@@ -56,3 +56,49 @@ def test_smf_matches_reference_kernel(kind, alpha, order):
     for a, b in zip(ours, ref):
         assert np.array_equal(np.isnan(a), np.isnan(b))
         assert maxrel(a, b) <= 1e-12
+
+
+def _time(fn, reps):
+    import torch
+    assert fn() == 0
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def test_faster_than_reference_kernels():
+    """the measured speed against the reference's kernels on the same GB300 and buffers (CUDA events, printed per
+    kind and order): gmf at n = 2^20 on the C1 groups, smf log (Voigt) at n = 65536 on the C0 matrices; order 2 of
+    both must be faster than the reference"""
+    import torch
+
+    import matfun_gb300
+    from matfun_gb300 import workloads as w
+    lib, ref = matfun_gb300.load(), ref_gpu.load()
+    n = 1 << 20
+    X = torch.from_numpy(w.c1_gmf_groups(n, seed=1).reshape(n, 9)).cuda()
+    F, J, H = (torch.empty(n, k, dtype=torch.float64, device="cuda") for k in (9, 81, 729))
+    speed = {}
+    for kind, name in ((1, "log"), (0, "exp"), (3, "sqrt")):
+        for order in (0, 1, 2):
+            p = (F.data_ptr(), J.data_ptr() if order else None, H.data_ptr() if order > 1 else None)
+            to = _time(lambda: lib.gmf_cuda_eval(kind, 0.0, n, X.data_ptr(), *p, None), 3)
+            tr = _time(lambda: ref.refgpu_gmf(kind, 0.0, order, n, X.data_ptr(), *p, None), 3)
+            speed[("gmf", name, order)] = tr / to
+            print(f"gmf {name} order {order} n=2^20: ours {to:8.2f} ms, reference kernel {tr:8.2f} ms, {tr / to:.2f}x")
+    del F, J, H
+    m = 65536
+    V = torch.from_numpy(w.c0_smf_spd(m)).cuda()
+    F, J, H = (torch.empty(m, k, dtype=torch.float64, device="cuda") for k in (6, 36, 216))
+    for order in (0, 1, 2):
+        p = (F.data_ptr(), J.data_ptr() if order else None, H.data_ptr() if order > 1 else None)
+        to = _time(lambda: lib.smf_cuda_eval(1, 0.0, m, V.data_ptr(), *p, None), 20)
+        tr = _time(lambda: ref.refgpu_smf(1, 0.0, order, m, V.data_ptr(), *p, None), 20)
+        speed[("smf", "log", order)] = tr / to
+        print(f"smf log Voigt order {order} n=65536: ours {to:7.3f} ms, reference kernel {tr:7.3f} ms, {tr / to:.2f}x")
+    assert speed[("gmf", "log", 2)] > 1.0 and speed[("smf", "log", 2)] > 1.0, speed
