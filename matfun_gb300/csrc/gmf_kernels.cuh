@@ -8,7 +8,7 @@
 //   halves: after the spectral analysis (gmf_classify) the CTA ranks its matrices by class (no group / real series /
 //   complex series) and series length, and the second half (gmf_finish) runs in that order, so that a warp's lanes
 //   take the same branches and run series of similar length (unsorted, half of the lanes idled on average).
-// Phase B: each warp walks its 32 matrices; for one matrix the 32 lanes build, through shared memory,
+// Phase B: each warp walks the 32 matrices it finished; for one matrix the 32 lanes build, through shared memory,
 //   Y2[y][m]      = sum_n D2'_mn r_n[y]                       (27)
 //   T4[x, y]      = sum_m r_m[x] Y2[y][m]                      (symmetric: 45 distinct of 81)
 //   Z[z][m, n]    = sum_p D3'_mnp r_p[z]                       (54)
@@ -107,17 +107,18 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   }
   __syncthreads();
 
-  // ---- phase A, second half, in sorted order; results stored by matrix
+  // ---- phase A, second half, in sorted order: slot tid takes the matrix of rank tid; F goes straight to HBM, the
+  // record stays in shared memory at the slot
   const int mine = S.perm[tid];
   if (mine < cnt) {
     GmfRec R;
     gmf_finish<KIND, ORDER>(S.state[mine], C, R);
 #pragma unroll
-    for (int k = 0; k < 9; k++) S.x[mine * 9 + k] = R.F[k];
+    for (int k = 0; k < 9; k++) F[(base + mine) * 9 + k] = (T)R.F[k];
     if (ORDER >= 1) {
       // the scale factors sc1 / sc2 are folded into D2' / D3' when finite and nonzero; otherwise each output entry
       // is multiplied by them (keeping the reference's NaN / Inf); rc[34] / rc[35] hold the factor left to apply
-      T *rc = reinterpret_cast<T *>(S.rec) + mine * GMF_REC;
+      T *rc = reinterpret_cast<T *>(S.rec) + tid * GMF_REC;
 #pragma unroll
       for (int k = 0; k < 9; k++) { rc[k] = (T)R.r1[k]; rc[9 + k] = (T)R.r2[k]; }
       const bool f1 = isfinite(R.sc1) & (R.sc1 != 0.0);
@@ -134,15 +135,16 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
       }
     }
   }
-  __syncthreads();
-  for (int e = tid; e < cnt * 9; e += GMF_TPB) F[base * 9 + e] = (T)S.x[e];
   if (ORDER < 1) return;
+  __syncwarp();
 
-  // ---- phase B: the warp's 32 matrices one after the other
+  // ---- phase B: each warp assembles the matrices it finished (its 32 slots), so no CTA barrier separates the two
+  // phases: a warp with short series assembles while the others still run theirs
   T *wk = reinterpret_cast<T *>(S.work[warp]);
-  const int m0 = warp * 32, m1 = min(cnt, m0 + 32);  // (phase B keeps the input order)
-  for (int mi = m0; mi < m1; mi++) {
-    const T *rc = reinterpret_cast<const T *>(S.rec) + mi * GMF_REC;
+  for (int sl = warp * 32; sl < warp * 32 + 32; sl++) {
+    const int mi = S.perm[sl];
+    if (mi >= cnt) break;  // the padding slots sort last
+    const T *rc = reinterpret_cast<const T *>(S.rec) + sl * GMF_REC;
     const T *r1 = rc, *r2 = rc + 9;
     {
       const T sc1 = rc[34];
