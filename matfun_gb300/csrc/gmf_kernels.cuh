@@ -16,7 +16,7 @@
 //   T6[x, y, z]   = sum_m r_m[x] Y[y, z][m]                    (symmetric: 165 distinct of 729)
 // (x, y, z = 3a + c index matrix entries) and writes, 32 consecutive doubles per store,
 //   J_abcd   = sc1 T4[ac, db]
-//   H_abcdef = sc2 (T6[ac, de, fb] + T6[ae, fc, db]).
+//   H_abcdef = sc2 (T6[ac, de, fb] + T6[ae, fc, db])   (405 distinct sums: H is symmetric under (cd) <-> (ef)).
 // The reference forms Y (27), Z (81) and Yh (243) per matrix and evaluates each of the 729 H entries with 6
 // multiply-adds in every thread (gmf_kernel.hpp:636-691); the symmetric form needs about a third of the FP64
 // instructions, which bound this kernel on GB300 (FP64 at 1/74 of the FP32 rate).  Spreading one matrix over the
@@ -38,8 +38,10 @@ struct GmfSmem {
   GmfState state[GMF_TPB];        // the first half's results, by matrix
   unsigned key[GMF_TPB];          // sort key of each matrix
   int perm[GMF_TPB];              // processing slot -> matrix
-  double work[GMF_WARPS][54 + 135 + 165]; // per warp: Z, Y, T6 (J: Y2 in Z, T4 in Y)
-  unsigned short hmap[729];       // H entry -> (T6 index of the first term) | (second) << 8
+  double work[GMF_WARPS][165 + 405];  // per warp: T6, then Z and Y, then the 405 distinct H values over Z and Y
+                                      // (J: Y2 at 0, T4 at 54)
+  unsigned short umap[405];       // distinct H value -> (T6 index of the first term) | (second) << 8
+  unsigned short hkey[729];       // H entry -> its distinct value (H is symmetric under (cd) <-> (ef))
   unsigned short t6map[165];      // T6 item -> x | y << 4 | z << 8
   unsigned short ymap[135];       // Y item  -> y | z << 4 | m << 8
 };
@@ -65,7 +67,16 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
 
   for (int e = tid; e < cnt * 9; e += GMF_TPB) S.x[e] = (double)A[base * 9 + e];
   if (ORDER >= 2) {  // index tables of phase B
-    for (int w = tid; w < 729; w += GMF_TPB) S.hmap[w] = hmap_entry(w);
+    for (int t = tid; t < 405; t += GMF_TPB) {  // t = 45 (ab) + sym2(cd, ef), cd <= ef
+      const int p = t % 45;
+      int ef = 0;
+      while (sym2(0, ef + 1) <= p) ef++;
+      S.umap[t] = hmap_entry(81 * (t / 45) + 9 * (p - sym2(0, ef)) + ef);
+    }
+    for (int w = tid; w < 729; w += GMF_TPB) {
+      const int cd = (w / 9) % 9, ef = w % 9;
+      S.hkey[w] = (unsigned short)(45 * (w / 81) + sym2(min(cd, ef), max(cd, ef)));
+    }
     for (int t = tid; t < 165; t += GMF_TPB) {
       int z = 0;
       while (sym3(0, 0, z + 1) <= t) z++;
@@ -178,7 +189,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
     {
       const T sc2 = rc[35];
       const T *d3 = rc + 24;
-      T *Zs = wk, *Ys = wk + 54, *T6 = wk + 54 + 135;
+      T *T6 = wk, *Zs = wk + 165, *Ys = wk + 165 + 54, *U = wk + 165;
       for (int t = lane; t < 54; t += 32) {  // Z[z][mn] = sum_p D3'_mnp r_p[z]  (mn: 00 01 02 11 12 22)
         const int z = t / 6, mn = t % 6;
         const int mm = mn < 3 ? 0 : (mn < 5 ? 1 : 2), nn = mn < 3 ? mn : (mn < 5 ? mn - 2 : 2);
@@ -203,17 +214,17 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
         T6[t] = (x % 4 == 0 ? yv[0] : T(0)) + r1[x] * yv[1] + r2[x] * yv[2];
       }
       __syncwarp();
+      // the 405 distinct H values (Z and Y are no longer needed: U takes their place), then the 729 stores
+      for (int t = lane; t < 405; t += 32) {
+        const unsigned short e = S.umap[t];
+        U[t] = T6[e & 255] + T6[e >> 8];
+      }
+      __syncwarp();
       T *o = H + (base + mi) * 729;
       if (sc2 == T(1)) {
-        for (int w = lane; w < 729; w += 32) {
-          const unsigned short e = S.hmap[w];
-          o[w] = T6[e & 255] + T6[e >> 8];
-        }
+        for (int w = lane; w < 729; w += 32) o[w] = U[S.hkey[w]];
       } else {
-        for (int w = lane; w < 729; w += 32) {
-          const unsigned short e = S.hmap[w];
-          o[w] = (T6[e & 255] + T6[e >> 8]) * sc2;
-        }
+        for (int w = lane; w < 729; w += 32) o[w] = U[S.hkey[w]] * sc2;
       }
       __syncwarp();
     }
