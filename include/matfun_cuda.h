@@ -141,6 +141,20 @@ void *GmfValueCuda(void *call_frame);
 void *GmfValueJacCuda(void *call_frame);
 void *GmfValueJacHessCuda(void *call_frame);
 
+/* Additional XLA FFI handlers (no counterpart in the reference), same call-frame conventions:
+ *   SmfValueF32Cuda, SmfMatrixValueF32Cuda, GmfValueF32Cuda: the FP32 forms (smf_cuda_eval_f32 ...), F32 buffers,
+ *     one to three results (F, J, H), attributes kind, alpha;
+ *   SmfAdjointCuda, GmfAdjointCuda (F64) and SmfAdjointF32Cuda, GmfAdjointF32Cuda (F32): arguments A, W, V
+ *     ((..., 3, 3); W or V with no elements when not given), attributes kind, alpha and outputs (int64 bit mask:
+ *     1 F, 2 J^T W, 4 J V, 8 W.H.V), one result per set bit in that order (smf_cuda_adjoint / gmf_cuda_adjoint). */
+void *SmfValueF32Cuda(void *call_frame);
+void *SmfMatrixValueF32Cuda(void *call_frame);
+void *GmfValueF32Cuda(void *call_frame);
+void *SmfAdjointCuda(void *call_frame);
+void *GmfAdjointCuda(void *call_frame);
+void *SmfAdjointF32Cuda(void *call_frame);
+void *GmfAdjointF32Cuda(void *call_frame);
+
 /* XLA FFI API version the handlers implement, major * 1000 + minor (reference: cuda/src/matfun_cuda.cu:265) */
 int smf_xla_ffi_api_version(void);
 

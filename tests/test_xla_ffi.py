@@ -133,3 +133,32 @@ def test_frame_layout_pinned_to_the_vendored_xla_header():
     r = subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), f"REF={ref}", "ffi-abi"],
                        cwd=ROOT, capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+
+def test_adjoint_frames_checked_before_launch(lib):
+    """the additional adjoint handlers: shapes, directions, the output mask and the result count are checked before
+    anything runs; an empty batch succeeds without a launch"""
+    A = (xf.DT_F64, 16, (4, 3, 3))
+    Z = (xf.DT_F64, 24, (0,))
+    at = xf.adjoint_attrs
+    cases = [
+        ("no outputs", "SmfAdjointCuda", [A, A, Z], at(1, 0.0, 0), [], "outputs"),
+        ("mask beyond 4 bits", "SmfAdjointCuda", [A, A, Z], at(1, 0.0, 16), [A], "outputs"),
+        ("result count", "GmfAdjointCuda", [A, A, Z], at(1, 0.0, 2 | 4), [A], "one result per selected output"),
+        ("W of another shape", "SmfAdjointCuda", [A, (xf.DT_F64, 24, (5, 3, 3)), Z], at(1, 0.0, 2), [A], "shape of A"),
+        ("A not (..., 3, 3)", "GmfAdjointCuda", [(xf.DT_F64, 16, (4, 9)), A, Z], at(1, 0.0, 1), [A], "(..., 3, 3)"),
+        ("J^T W without W", "SmfAdjointCuda", [A, Z, Z], at(1, 0.0, 2), [A], "invalid kind or alpha"),
+        ("F64 buffers to an F32 handler", "GmfAdjointF32Cuda", [A, A, Z], at(1, 0.0, 1), [A], "dtype"),
+        ("two arguments", "SmfAdjointCuda", [A, A], at(1, 0.0, 1), [A], "number of arguments"),
+    ]
+    for label, nm, args, attrs, rets, text in cases:
+        xla = xf.FakeXla()
+        cf, keep = xf.frame3(xla, args, rets, attrs)
+        assert call(lib, nm, cf) is not None, label
+        assert xla.errors[-1][0] == xf.ERR_INVALID_ARGUMENT and text in xla.errors[-1][1], (label, xla.errors[-1])
+    E = (xf.DT_F64, 16, (0, 3, 3))
+    for nm in ("SmfAdjointCuda", "GmfAdjointCuda"):
+        xla = xf.FakeXla()
+        cf, keep = xf.frame3(xla, [E, E, E], [E, E], at(1, 0.0, 1 | 8))
+        assert call(lib, nm, cf) is None and xla.errors == []

@@ -148,6 +148,21 @@ def std_attrs(kind, alpha):
     return {"kind": (ATTR_SCALAR, DT_S64, C.c_int64(kind)), "alpha": (ATTR_SCALAR, DT_F64, C.c_double(alpha))}
 
 
+def frame3(xla, args, rets, attrs):
+    """a call frame with several arguments (the adjoint handlers: A, W, V)"""
+    cf, keep = frame(xla, args[0], rets, attrs)
+    bufs = [_buffer(*a, keep) for a in args]
+    at = (C.c_int32 * len(bufs))(*([ARG_BUFFER] * len(bufs)))
+    ap = (C.c_void_p * len(bufs))(*[C.addressof(b) for b in bufs])
+    keep += [at, ap]
+    cf.args = Args(C.sizeof(Args), None, len(bufs), C.cast(at, C.POINTER(C.c_int32)), C.cast(ap, C.POINTER(C.c_void_p)))
+    return cf, keep
+
+
+def adjoint_attrs(kind, alpha, outputs):
+    return {**std_attrs(kind, alpha), "outputs": (ATTR_SCALAR, DT_S64, C.c_int64(outputs))}
+
+
 HANDLERS = {"voigt": ("SmfValueCuda", "SmfValueJacCuda", "SmfValueJacHessCuda"),
             "matrix": ("SmfMatrixValueCuda", "SmfMatrixValueJacCuda", "SmfMatrixValueJacHessCuda"),
             "general": ("GmfValueCuda", "GmfValueJacCuda", "GmfValueJacHessCuda")}
