@@ -16,6 +16,11 @@
 
 namespace mf {
 
+// terms of the cluster series of the second divided difference in FP32: the offsets are at most tau = 0.25 of the
+// centre (exp: 1 in absolute terms, with factorial coefficients), so term k is below (k + 1) 0.25^k |c2[0]| and the
+// series is truncated below 1e-8 relative after 16 terms (the FP64 form keeps the reference's 30)
+constexpr int DD2_TERMS_F = 16;
+
 struct SmfCoefF {
   float al, alm1;   // exponent and exponent - 1
   float zp1, z2;    // 0^(al - 1), f''(0)/2 for powers
@@ -84,7 +89,7 @@ MF_D float dd2s_f(float lj, float lk, float fj, float Dij, float Djk, float dji,
     }
     float h = 1.f, wk = 1.f, sm = C.c2[0];
 #pragma unroll
-    for (int k = 1; k < DD2_TERMS; k++) {
+    for (int k = 1; k < DD2_TERMS_F; k++) {
       wk = wk * w;
       h = fmaf(u, h, wk);
       sm = fmaf(C.c2[k], h, sm);
