@@ -120,14 +120,26 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x, world):
+def max_over_ranks(x, world, device="cuda"):
+    """the slowest rank's value (the job ends with its last rank); nccl on the GPUs, gloo on CPU tensors"""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(n_per_rank, ms, world):
+    """matrices/s of the whole job: every rank evaluates its own n_per_rank matrices (weak scaling, no collective on
+    the data path), the job takes the slowest rank's time"""
+    return world * n_per_rank / (ms * 1e-3)
+
+
+def rank_seed(rank):
+    """the seed of a rank's matrices: independent replicas of the workload"""
+    return 1 + rank
 
 
 def cpu_rate(kind_code, alpha, X, order, budget_s=10.0):
@@ -416,7 +428,7 @@ def run_ours(args, rank, world, local):
     lib = matfun_gb300.load()
     kind = KINDS[args.kind]
     n = args.n
-    X = w.c1_gmf_groups(n, seed=1 + rank).reshape(n, 9)
+    X = w.c1_gmf_groups(n, seed=rank_seed(rank)).reshape(n, 9)
     dev = torch.device("cuda", local)
     dA = torch.from_numpy(X).to(dev)
     dF = torch.empty((n, 9), dtype=torch.float64, device=dev)
@@ -446,7 +458,7 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / args.steps
     ms = max_over_ranks(ms, world)
-    value = world * n / (ms * 1e-3)
+    value = whole_job_rate(n, ms, world)
 
     # e2e: the host-buffer C ABI (gmf_cuda_eval_host: the reference's gmf_eval signature on host arrays; chunks
     # copied in, evaluated and copied out on two streams) on page-locked host arrays, copies inside the timed region
@@ -468,7 +480,7 @@ def run_ours(args, rank, world, local):
     for _ in range(e2e_steps):
         e2e_step()  # synchronous: returns when the results are in host memory
     e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0) / e2e_steps, world)
-    e2e_value = world * n / (e2e_ms * 1e-3)
+    e2e_value = whole_job_rate(n, e2e_ms, world)
     # result check of the last e2e step against the device result
     assert torch.equal(hH[:4].to(dev), dH[:4]) and torch.equal(hF[-4:].to(dev), dF[-4:])
 
