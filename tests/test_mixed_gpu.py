@@ -108,3 +108,32 @@ def test_gmf_mixed_c1(kind, alpha, name, order):
     for g, r in zip(got, ref[1:]):
         assert np.array_equal(np.isnan(g), np.isnan(r))
     assert max(errs) <= GMF_TOL
+
+
+@pytest.mark.parametrize("scale,order", [(1e-30, 0), (1e30, 0), (2.0 ** -20, 2), (2.0 ** 40, 2)])
+def test_smf_mixed_extreme_scales(scale, order):
+    """the float-float eigensystem scales by a power of two first: matrices of 1e-30 and 1e30 (FP32 range) keep the
+    accuracy of unit-scale ones for F; J and H at scales whose values FP32 storage can hold (H of log grows as
+    lambda^-2: at condition 1e6 and scale 1e-30 it is far beyond FP32)"""
+    from matfun_gb300 import workloads as w
+    X = (w.c2_smf_spd(8000, seed=31).astype(np.float64) * scale).astype(np.float32)
+    for kind, alpha in ((1, 0.0), (3, 0.0), (2, 0.3)):
+        errs, got, ref = errors(False, kind, alpha, X, order)
+        for g, r in zip(got, ref[1:]):
+            assert np.array_equal(np.isnan(g), np.isnan(r))
+        assert max(errs) <= TOL, (kind, errs)
+
+
+def test_smf_mixed_nonfinite_inputs_give_nan():
+    """NaN or infinite input entries: NaN results for that matrix only, the other matrices unaffected"""
+    from matfun_gb300 import workloads as w
+    X = w.c2_smf_spd(256, seed=32)
+    X[3, 0] = np.nan
+    X[7, 4] = np.inf
+    X[9, 2] = -np.inf
+    got = run_f32(False, 1, 0.0, X, 2)
+    for g in got:
+        assert np.isnan(g[[3, 7, 9]]).all()
+        good = np.ones(len(X), bool)
+        good[[3, 7, 9]] = False
+        assert not np.isnan(g[good]).any()
