@@ -256,32 +256,70 @@ struct GmfRec {
   double sc1, sc2;       // output factors of J and H (NaN for a matrix outside the domain)
 };
 
-template <int KIND, int ORDER>
-MF_D void gmf_classify(const double *a, const GmfCoef &C, GmfState &St) {
-  // ---- scaling (exp: none), shift m, deviator S
+// scaling by a power of two (exp: none), shift m, deviator S (gmf_kernel.hpp:262-275)
+template <int KIND>
+MF_D void gmf_scale(const double *a, double &sig, double *As, double &m, double *S) {
   double amax = fabs(a[0]);
 #pragma unroll
   for (int k = 1; k < 9; k++) amax = tmax(amax, fabs(a[k]));
-  double sig = KIND == EXP ? 1.0 : pow2safe(amax), isig = 1.0 / sig;
-  double As[9], S[9];
+  sig = KIND == EXP ? 1.0 : pow2safe(amax);
+  const double isig = 1.0 / sig;
 #pragma unroll
   for (int k = 0; k < 9; k++) As[k] = a[k] * isig;
-  double m = (As[0] + As[4] + As[8]) / 3.0;
+  m = (As[0] + As[4] + As[8]) / 3.0;
 #pragma unroll
   for (int k = 0; k < 9; k++) S[k] = k % 4 == 0 ? As[k] - m : As[k];
-  cx x[3], mu[3];
-  roots3(S, x);
-#pragma unroll
-  for (int i = 0; i < 3; i++) mu[i] = cmk(m + x[i].re, x[i].im);
+}
 
-  // ---- pair refinement (gmf_kernel.hpp:277-304)
+// the pair-refinement test (gmf_kernel.hpp:277-284)
+MF_D bool gmf_pair_check(const double *S, double m, const cx *mu, double &mid, double &Rp) {
   double smax = fabs(S[0]);
 #pragma unroll
   for (int k = 1; k < 9; k++) smax = tmax(smax, fabs(S[k]));
-  double mid = 0.5 * (mu[1].re + mu[2].re), Rp = 0.5 * cabs_s(csub(mu[1], mu[2]));
+  mid = 0.5 * (mu[1].re + mu[2].re);
+  Rp = 0.5 * cabs_s(csub(mu[1], mu[2]));
   bool small = fabs(mid) + Rp <= 0.25 * fabs(mu[0].re);
   bool aniso = (fabs(m) <= smax) & (Rp <= 0.25 * fabs(mid - mu[0].re));
-  bool pc = (mu[0].re != 0) & (small | aniso);
+  return (mu[0].re != 0) & (small | aniso);
+}
+
+// first part of the spectral analysis: the closed-form roots x of the deviator, and a key of the branches the rest
+// takes (complex pair, pair refinement, branch-cut pair), so that a CTA can order its matrices by it before the rest
+template <int KIND>
+MF_D unsigned gmf_roots(const double *a, cx *x) {
+  double sig, As[9], m, S[9];
+  gmf_scale<KIND>(a, sig, As, m, S);
+  roots3(S, x);
+  cx mu[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) mu[i] = cmk(m + x[i].re, x[i].im);
+  double mid, Rp;
+  const bool pc = gmf_pair_check(S, m, mu, mid, Rp);
+  const bool cut = (KIND != EXP) & (mu[1].re + mu[2].re < 0);
+  const bool cplx = (x[0].im != 0) | (x[1].im != 0) | (x[2].im != 0);
+  // geometry bucket (16 levels): the argument of the complex pair, or the spread of three real roots relative to their
+  // mean; neighbours in it take the same groups, Newton steps and series lengths in the rest
+  const int ip = x[1].im != 0 ? 1 : (x[2].im != 0 ? 2 : 0);
+  const cx mp = mu[ip];
+  const float argp = fabsf(atan2f((float)mp.im, (float)mp.re)) * (16.0f / 3.1415927f);
+  const float spread = (float)((tmax(tmax(x[0].re, x[1].re), x[2].re) - tmin(tmin(x[0].re, x[1].re), x[2].re)) /
+                               tmax(fabs(m), 1e-300)) * 8.0f;
+  const unsigned geo = (unsigned)fminf(cplx ? argp : spread, 15.0f);
+  return (cplx ? 128u : 0u) | (pc ? 64u : 0u) | (cut ? 32u : 0u) | geo;
+}
+
+// the rest of the spectral analysis, from the roots x of gmf_roots
+template <int KIND, int ORDER>
+MF_D void gmf_classify_from(const double *a, const cx *xr, const GmfCoef &C, GmfState &St) {
+  double sig, As[9], m, S[9];
+  gmf_scale<KIND>(a, sig, As, m, S);
+  cx x[3], mu[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) { x[i] = xr[i]; mu[i] = cmk(m + x[i].re, x[i].im); }
+
+  // ---- pair refinement (gmf_kernel.hpp:277-304)
+  double mid, Rp;
+  bool pc = gmf_pair_check(S, m, mu, mid, Rp);
   double pcen = 0.0, ps = 0.0;
   bool preal = true;
   if (pc) {
@@ -482,6 +520,13 @@ MF_D void gmf_classify(const double *a, const GmfCoef &C, GmfState &St) {
   St.flags = (ab[0] ? 1 : 0) | (ab[1] ? 2 : 0) | (ab[2] ? 4 : 0) | (inG[0] ? 8 : 0) | (inG[1] ? 16 : 0) |
              (inG[2] ? 32 : 0) | (pk[0] ? 64 : 0) | (pk[1] ? 128 : 0) | (pk[2] ? 256 : 0) | (bad ? 512 : 0) |
              (real ? 1024 : 0);
+}
+
+template <int KIND, int ORDER>
+MF_D void gmf_classify(const double *a, const GmfCoef &C, GmfState &St) {
+  cx x[3];
+  gmf_roots<KIND>(a, x);
+  gmf_classify_from<KIND, ORDER>(a, x, C, St);
 }
 
 // the second half: divided differences (series, residues), real basis, F and the reduced D2', D3'

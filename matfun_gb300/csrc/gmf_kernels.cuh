@@ -4,10 +4,12 @@
 //
 // One CTA = 128 matrices (four warps).
 // Phase A: one thread per matrix computes the record of gmf_device.cuh -- F, the real basis r_1, r_2 (r_0 = I) and
-//   the symmetric reduced divided differences D2' (6), D3' (10) -- into shared memory (36 doubles per matrix), in two
-//   halves: after the spectral analysis (gmf_classify) the CTA ranks its matrices by class (no group / real series /
-//   complex series) and series length, and the second half (gmf_finish) runs in that order, so that a warp's lanes
-//   take the same branches and run series of similar length (unsorted, half of the lanes idled on average).
+//   the symmetric reduced divided differences D2' (6), D3' (10) -- into shared memory (36 doubles per matrix), in three
+//   parts with a CTA-local ordering of the matrices before the second and the third, so that a warp's lanes take the
+//   same branches: the closed-form roots (gmf_roots), ordered by the branches of the spectral analysis that follow
+//   (complex pair, pair refinement, branch-cut pair); the rest of the spectral analysis (gmf_classify_from), ordered
+//   by class (no group / real series / complex series) and series length; then gmf_finish.  Unordered, about half
+//   of the lanes idled.
 // Phase B: each warp walks the 32 matrices it finished; for one matrix the 32 lanes build, through shared memory,
 //   Y2[y][m]      = sum_n D2'_mn r_n[y]                       (27)
 //   T4[x, y]      = sum_m r_m[x] Y2[y][m]                      (symmetric: 45 distinct of 81)
@@ -22,6 +24,8 @@
 // instructions, which bound this kernel on GB300 (FP64 at 1/74 of the FP32 rate).  Spreading one matrix over the
 // warp keeps the shared memory per CTA small (31 KB), so the occupancy is set by the registers of phase A.
 #pragma once
+#include <climits>
+
 #include "gmf_device.cuh"
 #include "mf_launch.h"
 
@@ -42,6 +46,7 @@ struct GmfSmem {
                                       // (J: Y2 at 0, T4 at 54)
   unsigned short umap[405];       // distinct H value -> (T6 index of the first term) | (second) << 8
   unsigned short hkey[729];       // H entry -> its distinct value (H is symmetric under (cd) <-> (ef))
+  long long gidx[GMF_TPB];        // tile position -> matrix index in the arrays
   unsigned short t6map[165];      // T6 item -> x | y << 4 | z << 8
   unsigned short ymap[135];       // Y item  -> y | z << 4 | m << 8
 };
@@ -60,12 +65,18 @@ MF_D unsigned short hmap_entry(int w) {
 // persistent kernel run the same code).  T is the type of the arrays in HBM and of phase B: double for the FP64
 // path; float for the mixed-precision path, where phase A (spectral analysis, series, residues: the FP64 steps of
 // the method) stays in FP64 and its record -- with the scale factors folded in, in FP64 -- is rounded to FP32 once.
+// idx (optional): tile position p holds matrix idx[base + p] of the arrays instead of base + p (the reordered launch).
 template <int KIND, int ORDER, typename T = double>
 MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict__ F, T *__restrict__ J,
-                   T *__restrict__ H, const GmfCoef &C, GmfSmem &S) {
+                   T *__restrict__ H, const GmfCoef &C, GmfSmem &S, const int *__restrict__ idx = nullptr) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  for (int e = tid; e < cnt * 9; e += GMF_TPB) S.x[e] = (double)A[base * 9 + e];
+  for (int e = tid; e < cnt * 9; e += GMF_TPB) {
+    const int p = e / 9;
+    const long long g = idx ? (long long)idx[base + p] : base + p;
+    S.x[e] = (double)A[g * 9 + (e - 9 * p)];
+    if (e == 9 * p) S.gidx[p] = g;
+  }
   if (ORDER >= 2) {  // index tables of phase B
     for (int t = tid; t < 405; t += GMF_TPB) {  // t = 45 (ab) + sym2(cd, ef), cd <= ef
       const int p = t % 45;
@@ -93,18 +104,18 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   }
   __syncthreads();
 
-  // ---- phase A, first half: spectral analysis of matrix tid, and its sort key
+  // ---- phase A, first part: the closed-form roots of matrix tid and the key of the branches the spectral analysis
+  // takes next (complex pair, pair refinement, branch-cut pair); the roots wait in the matrix's state slot
   unsigned key = 0xFFFFFFFFu;
   if (tid < cnt) {
     double a[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) a[k] = S.x[tid * 9 + k];
-    GmfState St;
-    gmf_classify<KIND, ORDER>(a, C, St);
-    S.state[tid] = St;
-    // class (no group < real series < complex series), longer series first, then the group's node pattern
-    const unsigned cls = St.K == 0 ? 0u : ((St.flags & 1024) ? 1u : 2u);
-    key = (cls << 16) | ((unsigned)(255 - St.K) << 6) | (unsigned)((St.flags >> 3) & 63);
+    cx x[3];
+    key = gmf_roots<KIND>(a, x);
+    double *xs = reinterpret_cast<double *>(&S.state[tid]);
+#pragma unroll
+    for (int i = 0; i < 3; i++) { xs[2 * i] = x[i].re; xs[2 * i + 1] = x[i].im; }
   }
   S.key[tid] = key;
   __syncthreads();
@@ -118,14 +129,48 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   }
   __syncthreads();
 
-  // ---- phase A, second half, in sorted order: slot tid takes the matrix of rank tid; F goes straight to HBM, the
-  // record stays in shared memory at the slot
+  // ---- phase A, second part, in that order (the lanes of a warp take the same branches): the rest of the spectral
+  // analysis, and the key of the finish: class (no group < real series < complex series), longer series first, then
+  // the group's node pattern
+  {
+    const int mi = S.perm[tid];
+    unsigned key2 = 0xFFFFFFFFu;
+    if (mi < cnt) {
+      double a[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) a[k] = S.x[mi * 9 + k];
+      const double *xs = reinterpret_cast<const double *>(&S.state[mi]);
+      cx x[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) x[i] = cmk(xs[2 * i], xs[2 * i + 1]);
+      GmfState St;
+      gmf_classify_from<KIND, ORDER>(a, x, C, St);
+      S.state[mi] = St;
+      const unsigned cls = St.K == 0 ? 0u : ((St.flags & 1024) ? 1u : 2u);
+      key2 = (cls << 16) | ((unsigned)(255 - St.K) << 6) | (unsigned)((St.flags >> 3) & 63);
+    }
+    S.key[mi] = key2;  // (every thread finished reading the first keys before the last barrier)
+  }
+  __syncthreads();
+  {
+    key = S.key[tid];
+    int rank = 0;
+    for (int j = 0; j < GMF_TPB; j++) {
+      const unsigned kj = S.key[j];
+      rank += (kj < key) | ((kj == key) & (j < tid));
+    }
+    S.perm[rank] = tid;
+  }
+  __syncthreads();
+
+  // ---- phase A, finish, in the order of the second key: slot tid takes the matrix of rank tid; F goes straight to
+  // HBM, the record stays in shared memory at the slot
   const int mine = S.perm[tid];
   if (mine < cnt) {
     GmfRec R;
     gmf_finish<KIND, ORDER>(S.state[mine], C, R);
 #pragma unroll
-    for (int k = 0; k < 9; k++) F[(base + mine) * 9 + k] = (T)R.F[k];
+    for (int k = 0; k < 9; k++) F[S.gidx[mine] * 9 + k] = (T)R.F[k];
     if (ORDER >= 1) {
       // the scale factors sc1 / sc2 are folded into D2' / D3' when finite and nonzero; otherwise each output entry
       // is multiplied by them (keeping the reference's NaN / Inf); rc[34] / rc[35] hold the factor left to apply
@@ -174,7 +219,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
         wk[54 + t] = (x % 4 == 0 ? yv[0] : T(0)) + r1[x] * yv[1] + r2[x] * yv[2];
       }
       __syncwarp();
-      T *o = J + (base + mi) * 81;
+      T *o = J + S.gidx[mi] * 81;
       const bool one1 = sc1 == T(1);  // folded (the common case): no multiply per entry; uniform in the warp
       for (int w = lane; w < 81; w += 32) {
         const int a = w / 27, b = (w / 9) % 3, c = (w / 3) % 3, d = w % 3;
@@ -220,7 +265,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
         U[t] = T6[e & 255] + T6[e >> 8];
       }
       __syncwarp();
-      T *o = H + (base + mi) * 729;
+      T *o = H + S.gidx[mi] * 729;
       if (sc2 == T(1)) {
         for (int w = lane; w < 729; w += 32) o[w] = U[S.hkey[w]];
       } else {
@@ -233,16 +278,89 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
 
 template <int KIND, int ORDER, typename T>
 __global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const T *__restrict__ A, T *__restrict__ F,
-                                                      T *__restrict__ J, T *__restrict__ H, const GmfCoef C) {
+                                                      T *__restrict__ J, T *__restrict__ H, const GmfCoef C,
+                                                      const int *__restrict__ idx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GmfSmem &S = *reinterpret_cast<GmfSmem *>(smem_raw);
   const int64_t base = (int64_t)blockIdx.x * GMF_TPB;
-  gmf_tile<KIND, ORDER, T>(base, (int)min((int64_t)GMF_TPB, n - base), A, F, J, H, C, S);
+  gmf_tile<KIND, ORDER, T>(base, (int)min((int64_t)GMF_TPB, n - base), A, F, J, H, C, S, idx);
+}
+
+// ---- batch-wide reordering.  The work of a matrix depends on its spectrum (real roots or a complex pair, pair
+// refinement, branch-cut pair, the geometry of the roots); a CTA's 128 matrices of a random batch span many such
+// classes, and a warp of one class runs up to twice as fast as a mixed one.  So the standalone launch first computes
+// the class key of every matrix (gmf_roots), orders the batch by it with a stable counting sort, and evaluates the
+// matrices in that order (results written at their own indices).  The scratch of the sort -- the order, the keys and
+// per-block counts, about 9 bytes per matrix -- lies in the caller's own largest output array (H, or J for order 1),
+// in the part that belongs to the last few matrices; those are evaluated afterwards by a plain launch, which
+// overwrites it.  Nothing is allocated, and concurrent calls share nothing.
+constexpr int GKEY_TPB = 256, GKEY_BINS = 256;
+
+template <int KIND, typename T>
+__global__ void __launch_bounds__(GKEY_TPB) gmf_key_kernel(int n, const T *__restrict__ A,
+                                                           unsigned char *__restrict__ keys,
+                                                           int *__restrict__ counts, int nblk) {
+  __shared__ int hist[GKEY_BINS];
+  for (int k = threadIdx.x; k < GKEY_BINS; k += GKEY_TPB) hist[k] = 0;
+  __syncthreads();
+  const int i = blockIdx.x * GKEY_TPB + threadIdx.x;
+  if (i < n) {
+    double a[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) a[k] = (double)A[(int64_t)i * 9 + k];
+    cx x[3];
+    const unsigned key = gmf_roots<KIND>(a, x) & (GKEY_BINS - 1);
+    keys[i] = (unsigned char)key;
+    atomicAdd(&hist[key], 1);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < GKEY_BINS; k += GKEY_TPB) counts[k * nblk + blockIdx.x] = hist[k];
+}
+
+// exclusive prefix sum of counts[0 .. total) in place, by one CTA of 1024 threads
+static __global__ void __launch_bounds__(1024) gmf_scan_kernel(int *__restrict__ counts, int total) {
+  __shared__ int part[1024];
+  const int per = (total + 1023) / 1024, lo = min(total, (int)threadIdx.x * per), hi = min(total, lo + per);
+  int s = 0;
+  for (int i = lo; i < hi; i++) s += counts[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int j = 0; j < 1024; j++) {
+      const int v = part[j];
+      part[j] = acc;
+      acc += v;
+    }
+  }
+  __syncthreads();
+  int acc = part[threadIdx.x];
+  for (int i = lo; i < hi; i++) {
+    const int v = counts[i];
+    counts[i] = acc;
+    acc += v;
+  }
+}
+
+// order[offset(key, block) + rank among the equal keys before it in its block] = i: a stable sort by key
+static __global__ void __launch_bounds__(GKEY_TPB) gmf_scatter_kernel(int n, const unsigned char *__restrict__ keys,
+                                                               const int *__restrict__ offs, int nblk,
+                                                               int *__restrict__ order) {
+  __shared__ int sk[GKEY_TPB];
+  const int i = blockIdx.x * GKEY_TPB + threadIdx.x;
+  sk[threadIdx.x] = i < n ? (int)keys[i] : -1;
+  __syncthreads();
+  if (i < n) {
+    const int key = sk[threadIdx.x];
+    int r = 0;
+    for (int j = 0; j < (int)threadIdx.x; j++) r += sk[j] == key;
+    order[offs[key * nblk + blockIdx.x] + r] = i;
+  }
 }
 
 template <int KIND, int ORDER, typename T>
 cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const T *A, T *F, T *J, T *H,
-                           const GmfCoef &C) {
+                           const GmfCoef &C, const int *idx = nullptr) {
   static bool attr = false;  // once per instantiation (idempotent; a racing second call sets the same value)
   if (!attr) {
     const cudaError_t e = cudaFuncSetAttribute(gmf_kernel<KIND, ORDER, T>,
@@ -250,15 +368,47 @@ cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const T 
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  gmf_kernel<KIND, ORDER, T><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C);
+  gmf_kernel<KIND, ORDER, T><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C, idx);
   return cudaGetLastError();
 }
+
+// orders 1 and 2 of a large batch: key, sort, reordered evaluation of the first nm matrices, plain evaluation of the
+// last n - nm (whose share of the largest output array held the scratch)
+template <int KIND, int ORDER, typename T>
+cudaError_t gmf_launch_sorted(cudaStream_t st, int64_t n, const T *A, T *F, T *J, T *H, const GmfCoef &C) {
+  T *big = ORDER == 2 ? H : J;
+  const int64_t per = ORDER == 2 ? 729 : 81;  // elements of the largest output per matrix
+  const int64_t nblk_n = (n + GKEY_TPB - 1) / GKEY_TPB;
+  const int64_t need = 4 * n + 4 * (int64_t)GKEY_BINS * nblk_n + n + 64;  // order, counts, keys (bytes)
+  const int64_t tail = (need + per * (int64_t)sizeof(T) - 1) / (per * (int64_t)sizeof(T)) + 1;
+  const int64_t nm = n - tail;
+  const int nblk = (int)((nm + GKEY_TPB - 1) / GKEY_TPB);
+  char *scr = reinterpret_cast<char *>(big + nm * per);
+  int *order = reinterpret_cast<int *>(scr);
+  int *counts = order + nm;
+  unsigned char *keys = reinterpret_cast<unsigned char *>(counts + (int64_t)GKEY_BINS * nblk);
+  gmf_key_kernel<KIND, T><<<nblk, GKEY_TPB, 0, st>>>((int)nm, A, keys, counts, nblk);
+  gmf_scan_kernel<<<1, 1024, 0, st>>>(counts, GKEY_BINS * nblk);
+  gmf_scatter_kernel<<<nblk, GKEY_TPB, 0, st>>>((int)nm, keys, counts, nblk, order);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((nm + GMF_TPB - 1) / GMF_TPB), nm, A, F, J, H, C, order);
+  if (e != cudaSuccess) return e;
+  return gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((tail + GMF_TPB - 1) / GMF_TPB), tail, A + nm * 9, F + nm * 9,
+                                        J + nm * 81, ORDER == 2 ? H + nm * 729 : nullptr, C);
+}
+
+constexpr int64_t GMF_SORT_MIN = 1 << 15;  // below this the reordering does not pay for its launches
 
 template <int KIND, typename T>
 cudaError_t gmf_launch_kind(int order, cudaStream_t st, unsigned blocks, int64_t n, const T *A, T *F, T *J, T *H,
                             const GmfCoef &C) {
-  if (order == 2) return gmf_launch_one<KIND, 2, T>(st, blocks, n, A, F, J, H, C);
-  if (order == 1) return gmf_launch_one<KIND, 1, T>(st, blocks, n, A, F, J, H, C);
+  // log and pow (the branch-cut pair and the wider spread of work); exp does not recover the ~1 ms of the sort
+  const bool sorted = (KIND != EXP) & (n >= GMF_SORT_MIN) & (n <= INT_MAX);
+  if (order == 2) return sorted ? gmf_launch_sorted<KIND, 2, T>(st, n, A, F, J, H, C)
+                                : gmf_launch_one<KIND, 2, T>(st, blocks, n, A, F, J, H, C);
+  if (order == 1) return sorted ? gmf_launch_sorted<KIND, 1, T>(st, n, A, F, J, H, C)
+                                : gmf_launch_one<KIND, 1, T>(st, blocks, n, A, F, J, H, C);
   return gmf_launch_one<KIND, 0, T>(st, blocks, n, A, F, J, H, C);
 }
 
