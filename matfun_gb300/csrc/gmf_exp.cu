@@ -3,7 +3,7 @@
 
 namespace mf {
 cudaError_t gmf_launch_exp(double al, int64_t n, const double *A, double *F, double *J, double *H,
-                            cudaStream_t st) {
-  return gmf_launch_t<EXP>(al, n, A, F, J, H, st);
+                            cudaStream_t st, bool reorder) {
+  return gmf_launch_t<EXP>(al, n, A, F, J, H, st, reorder);
 }
 }  // namespace mf

@@ -65,10 +65,12 @@ MF_D unsigned short hmap_entry(int w) {
 // persistent kernel run the same code).  T is the type of the arrays in HBM and of phase B: double for the FP64
 // path; float for the mixed-precision path, where phase A (spectral analysis, series, residues: the FP64 steps of
 // the method) stays in FP64 and its record -- with the scale factors folded in, in FP64 -- is rounded to FP32 once.
-// idx (optional): tile position p holds matrix idx[base + p] of the arrays instead of base + p (the reordered launch).
+// idx (optional): tile position p holds matrix idx[base + p] of the arrays instead of base + p (the reordered launch);
+// roots, keys (optional, by matrix): the closed-form roots and their key, already computed by gmf_key_kernel.
 template <int KIND, int ORDER, typename T = double>
 MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict__ F, T *__restrict__ J,
-                   T *__restrict__ H, const GmfCoef &C, GmfSmem &S, const int *__restrict__ idx = nullptr) {
+                   T *__restrict__ H, const GmfCoef &C, GmfSmem &S, const int *__restrict__ idx = nullptr,
+                   const double *__restrict__ roots = nullptr, const unsigned char *__restrict__ keys = nullptr) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int e = tid; e < cnt * 9; e += GMF_TPB) {
@@ -108,14 +110,21 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   // takes next (complex pair, pair refinement, branch-cut pair); the roots wait in the matrix's state slot
   unsigned key = 0xFFFFFFFFu;
   if (tid < cnt) {
-    double a[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) a[k] = S.x[tid * 9 + k];
-    cx x[3];
-    key = gmf_roots<KIND>(a, x);
     double *xs = reinterpret_cast<double *>(&S.state[tid]);
+    if (roots) {
+      const long long g = S.gidx[tid];
 #pragma unroll
-    for (int i = 0; i < 3; i++) { xs[2 * i] = x[i].re; xs[2 * i + 1] = x[i].im; }
+      for (int k = 0; k < 6; k++) xs[k] = roots[g * 6 + k];
+      key = keys[g];
+    } else {
+      double a[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) a[k] = S.x[tid * 9 + k];
+      cx x[3];
+      key = gmf_roots<KIND>(a, x);
+#pragma unroll
+      for (int i = 0; i < 3; i++) { xs[2 * i] = x[i].re; xs[2 * i + 1] = x[i].im; }
+    }
   }
   S.key[tid] = key;
   __syncthreads();
@@ -279,11 +288,12 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
 template <int KIND, int ORDER, typename T>
 __global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const T *__restrict__ A, T *__restrict__ F,
                                                       T *__restrict__ J, T *__restrict__ H, const GmfCoef C,
-                                                      const int *__restrict__ idx) {
+                                                      const int *__restrict__ idx, const double *__restrict__ roots,
+                                                      const unsigned char *__restrict__ keys) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GmfSmem &S = *reinterpret_cast<GmfSmem *>(smem_raw);
   const int64_t base = (int64_t)blockIdx.x * GMF_TPB;
-  gmf_tile<KIND, ORDER, T>(base, (int)min((int64_t)GMF_TPB, n - base), A, F, J, H, C, S, idx);
+  gmf_tile<KIND, ORDER, T>(base, (int)min((int64_t)GMF_TPB, n - base), A, F, J, H, C, S, idx, roots, keys);
 }
 
 // ---- batch-wide reordering.  The work of a matrix depends on its spectrum (real roots or a complex pair, pair
@@ -291,15 +301,17 @@ __global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const T *__rest
 // classes, and a warp of one class runs up to twice as fast as a mixed one.  So the standalone launch first computes
 // the class key of every matrix (gmf_roots), orders the batch by it with a stable counting sort, and evaluates the
 // matrices in that order (results written at their own indices).  The scratch of the sort -- the order, the keys and
-// per-block counts, about 9 bytes per matrix -- lies in the caller's own largest output array (H, or J for order 1),
-// in the part that belongs to the last few matrices; those are evaluated afterwards by a plain launch, which
-// overwrites it.  Nothing is allocated, and concurrent calls share nothing.
+// per-block counts, about 9 bytes per matrix, and for order 2 the roots (48 bytes), which the evaluation then reads
+// instead of recomputing them -- lies in the caller's own largest output array (H, or J for order 1), in the part
+// that belongs to the last few matrices; those are evaluated afterwards by a plain launch, which overwrites it.
+// Nothing is allocated, and concurrent calls share nothing.
 constexpr int GKEY_TPB = 256, GKEY_BINS = 256;
 
 template <int KIND, typename T>
 __global__ void __launch_bounds__(GKEY_TPB) gmf_key_kernel(int n, const T *__restrict__ A,
                                                            unsigned char *__restrict__ keys,
-                                                           int *__restrict__ counts, int nblk) {
+                                                           int *__restrict__ counts, int nblk,
+                                                           double *__restrict__ roots) {
   __shared__ int hist[GKEY_BINS];
   for (int k = threadIdx.x; k < GKEY_BINS; k += GKEY_TPB) hist[k] = 0;
   __syncthreads();
@@ -311,6 +323,10 @@ __global__ void __launch_bounds__(GKEY_TPB) gmf_key_kernel(int n, const T *__res
     cx x[3];
     const unsigned key = gmf_roots<KIND>(a, x) & (GKEY_BINS - 1);
     keys[i] = (unsigned char)key;
+    if (roots) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) { roots[(int64_t)i * 6 + 2 * k] = x[k].re; roots[(int64_t)i * 6 + 2 * k + 1] = x[k].im; }
+    }
     atomicAdd(&hist[key], 1);
   }
   __syncthreads();
@@ -360,7 +376,8 @@ static __global__ void __launch_bounds__(GKEY_TPB) gmf_scatter_kernel(int n, con
 
 template <int KIND, int ORDER, typename T>
 cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const T *A, T *F, T *J, T *H,
-                           const GmfCoef &C, const int *idx = nullptr) {
+                           const GmfCoef &C, const int *idx = nullptr, const double *roots = nullptr,
+                           const unsigned char *keys = nullptr) {
   static bool attr = false;  // once per instantiation (idempotent; a racing second call sets the same value)
   if (!attr) {
     const cudaError_t e = cudaFuncSetAttribute(gmf_kernel<KIND, ORDER, T>,
@@ -368,7 +385,7 @@ cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const T 
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  gmf_kernel<KIND, ORDER, T><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C, idx);
+  gmf_kernel<KIND, ORDER, T><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C, idx, roots, keys);
   return cudaGetLastError();
 }
 
@@ -379,7 +396,8 @@ cudaError_t gmf_launch_sorted(cudaStream_t st, int64_t n, const T *A, T *F, T *J
   T *big = ORDER == 2 ? H : J;
   const int64_t per = ORDER == 2 ? 729 : 81;  // elements of the largest output per matrix
   const int64_t nblk_n = (n + GKEY_TPB - 1) / GKEY_TPB;
-  const int64_t need = 4 * n + 4 * (int64_t)GKEY_BINS * nblk_n + n + 64;  // order, counts, keys (bytes)
+  // order, counts, keys (bytes) and, for order 2, the roots (48 bytes per matrix; the tail stays ~1 % of the batch)
+  const int64_t need = 4 * n + 4 * (int64_t)GKEY_BINS * nblk_n + n + (ORDER == 2 ? 48 * n + 8 : 0) + 64;
   const int64_t tail = (need + per * (int64_t)sizeof(T) - 1) / (per * (int64_t)sizeof(T)) + 1;
   const int64_t nm = n - tail;
   const int nblk = (int)((nm + GKEY_TPB - 1) / GKEY_TPB);
@@ -387,12 +405,18 @@ cudaError_t gmf_launch_sorted(cudaStream_t st, int64_t n, const T *A, T *F, T *J
   int *order = reinterpret_cast<int *>(scr);
   int *counts = order + nm;
   unsigned char *keys = reinterpret_cast<unsigned char *>(counts + (int64_t)GKEY_BINS * nblk);
-  gmf_key_kernel<KIND, T><<<nblk, GKEY_TPB, 0, st>>>((int)nm, A, keys, counts, nblk);
+  double *roots = nullptr;
+  if (ORDER == 2) {
+    const uintptr_t r = reinterpret_cast<uintptr_t>(keys + nm);
+    roots = reinterpret_cast<double *>((r + 7) & ~(uintptr_t)7);
+  }
+  gmf_key_kernel<KIND, T><<<nblk, GKEY_TPB, 0, st>>>((int)nm, A, keys, counts, nblk, roots);
   gmf_scan_kernel<<<1, 1024, 0, st>>>(counts, GKEY_BINS * nblk);
   gmf_scatter_kernel<<<nblk, GKEY_TPB, 0, st>>>((int)nm, keys, counts, nblk, order);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  e = gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((nm + GMF_TPB - 1) / GMF_TPB), nm, A, F, J, H, C, order);
+  e = gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((nm + GMF_TPB - 1) / GMF_TPB), nm, A, F, J, H, C, order, roots,
+                                     roots ? keys : nullptr);
   if (e != cudaSuccess) return e;
   return gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((tail + GMF_TPB - 1) / GMF_TPB), tail, A + nm * 9, F + nm * 9,
                                         J + nm * 81, ORDER == 2 ? H + nm * 729 : nullptr, C);
@@ -402,9 +426,9 @@ constexpr int64_t GMF_SORT_MIN = 1 << 15;  // below this the reordering does not
 
 template <int KIND, typename T>
 cudaError_t gmf_launch_kind(int order, cudaStream_t st, unsigned blocks, int64_t n, const T *A, T *F, T *J, T *H,
-                            const GmfCoef &C) {
+                            const GmfCoef &C, bool reorder = true) {
   // log and pow (the branch-cut pair and the wider spread of work); exp does not recover the ~1 ms of the sort
-  const bool sorted = (KIND != EXP) & (n >= GMF_SORT_MIN) & (n <= INT_MAX);
+  const bool sorted = reorder & (KIND != EXP) & (n >= GMF_SORT_MIN) & (n <= INT_MAX);
   if (order == 2) return sorted ? gmf_launch_sorted<KIND, 2, T>(st, n, A, F, J, H, C)
                                 : gmf_launch_one<KIND, 2, T>(st, blocks, n, A, F, J, H, C);
   if (order == 1) return sorted ? gmf_launch_sorted<KIND, 1, T>(st, n, A, F, J, H, C)
@@ -436,12 +460,12 @@ inline void gmf_coef(int kind, double al, int order, GmfCoef &C) {
 
 // one kind (instantiated in gmf_<kind>.cu and gmf_mixed_<kind>.cu so that they compile in parallel)
 template <int KIND, typename T = double>
-cudaError_t gmf_launch_t(double al, int64_t n, const T *A, T *F, T *J, T *H, cudaStream_t st) {
+cudaError_t gmf_launch_t(double al, int64_t n, const T *A, T *F, T *J, T *H, cudaStream_t st, bool reorder = true) {
   const int order = H ? 2 : (J ? 1 : 0);
   GmfCoef C;
   gmf_coef(KIND, al, order, C);
   const unsigned blocks = (unsigned)((n + GMF_TPB - 1) / GMF_TPB);
-  return gmf_launch_kind<KIND, T>(order, st, blocks, n, A, F, J, H, C);
+  return gmf_launch_kind<KIND, T>(order, st, blocks, n, A, F, J, H, C, reorder);
 }
 
 }  // namespace mf

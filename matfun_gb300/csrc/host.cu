@@ -55,12 +55,12 @@ cudaError_t ensure(DevState &d, size_t doubles) {
 }
 
 cudaError_t launch(int fam, int kind, double alpha, int64_t n, const double *x, double *F, double *J, double *H,
-                   cudaStream_t st, int *asym) {
+                   cudaStream_t st, int *asym, bool reorder = true) {
   if (fam == GENERAL) {
     switch (kind) {
-      case SMF_EXP: return mf::gmf_launch_exp(alpha, n, x, F, J, H, st);
-      case SMF_LOG: return mf::gmf_launch_log(alpha, n, x, F, J, H, st);
-      default: return mf::gmf_launch_pow(alpha, n, x, F, J, H, st);
+      case SMF_EXP: return mf::gmf_launch_exp(alpha, n, x, F, J, H, st, reorder);
+      case SMF_LOG: return mf::gmf_launch_log(alpha, n, x, F, J, H, st, reorder);
+      default: return mf::gmf_launch_pow(alpha, n, x, F, J, H, st, reorder);
     }
   }
   const bool mat = fam == MATRIX;
@@ -108,9 +108,10 @@ int host_eval(int fam, int kind, double alpha, int64_t n, const double *x, doubl
     const int64_t step = (int64_t)1 << 26;
     for (int64_t lo = 0; lo < n && e == cudaSuccess; lo += step) {
       const int64_t m = n - lo < step ? n - lo : step;
+      // (no batch-wide reordering here: its scratch would cross the host link twice)
       e = launch(fam, kind, alpha, m, (const double *)mx + lo * nin, (double *)mF + lo * nf,
                  J ? (double *)mJ + lo * nj : nullptr, H ? (double *)mH + lo * nh : nullptr, st,
-                 fam == MATRIX ? d.asym : nullptr);
+                 fam == MATRIX ? d.asym : nullptr, false);
     }
     int asym = 0;
     if (e == cudaSuccess && fam == MATRIX) e = cudaMemcpyAsync(&asym, d.asym, sizeof(int), cudaMemcpyDeviceToHost, st);

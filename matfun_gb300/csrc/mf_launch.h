@@ -14,8 +14,10 @@ MF_SMF_DECL(log)
 MF_SMF_DECL(sqrt)
 MF_SMF_DECL(pow)
 #undef MF_SMF_DECL
-#define MF_GMF_DECL(k) \
-  cudaError_t gmf_launch_##k(double al, int64_t n, const double *A, double *F, double *J, double *H, cudaStream_t st);
+// (reorder: allow the batch-wide ordering by spectral class, gmf_kernels.cuh; off where the arrays are host memory)
+#define MF_GMF_DECL(k)                                                                                      \
+  cudaError_t gmf_launch_##k(double al, int64_t n, const double *A, double *F, double *J, double *H, cudaStream_t st, \
+                             bool reorder = true);
 MF_GMF_DECL(exp)
 MF_GMF_DECL(log)
 MF_GMF_DECL(pow)

@@ -81,7 +81,9 @@ def test_pinned_buffers_and_names(shim):
 @pytest.mark.parametrize("fam", ["smf_matrix", "gmf"])
 def test_in_place_path_equals_chunked_copies(shim, fam):
     """every array page-locked: the kernels read and write host memory in place over the host link; the results are
-    those of the chunked copy path (pageable arrays) bit for bit, and -3 for a non-symmetric matrix as there"""
+    those of the chunked copy path (pageable arrays) -- bit for bit for smf; for gmf to 1e-13, since the device path
+    orders a batch by spectral class and a warp's neighbours can change the last bits of a series -- and -3 for a
+    non-symmetric matrix as there"""
     import torch
 
     import matfun_gb300
@@ -105,4 +107,7 @@ def test_in_place_path_equals_chunked_copies(shim, fam):
         outs[pinned] = [t.numpy() for t in tens[1:]]
     for a, b in zip(outs[True], outs[False]):
         assert np.array_equal(np.isnan(a), np.isnan(b))
-        assert np.array_equal(np.nan_to_num(a), np.nan_to_num(b))
+        if fam == "gmf":
+            assert maxrel(a, b) <= 1e-13
+        else:
+            assert np.array_equal(np.nan_to_num(a), np.nan_to_num(b))
