@@ -61,6 +61,7 @@ struct GadjSmem {
   GmfState state[GADJ_TPB];
   unsigned key[GADJ_TPB];
   int perm[GADJ_TPB];
+  long long gidx[GADJ_TPB];  // tile position -> matrix index (the ordered launch)
 };
 
 template <int KIND, int ORDER, typename T>
@@ -68,16 +69,19 @@ __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const 
                                                                const T *__restrict__ W, const T *__restrict__ V,
                                                                T *__restrict__ F, T *__restrict__ Abar,
                                                                T *__restrict__ JV, T *__restrict__ HWV,
-                                                               const GmfCoef C) {
+                                                               const GmfCoef C, const int *__restrict__ idx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GadjSmem &S = *reinterpret_cast<GadjSmem *>(smem_raw);
   const int tid = threadIdx.x;
   const int64_t base = (int64_t)blockIdx.x * GADJ_TPB;
   const int cnt = (int)min((int64_t)GADJ_TPB, n - base);
-  for (int e = tid; e < cnt * 9; e += GADJ_TPB) {
-    S.x[e] = A[base * 9 + e];
-    if (W) S.w[e] = W[base * 9 + e];
-    if (V) S.v[e] = V[base * 9 + e];
+  for (int e = tid; e < cnt * 9; e += GADJ_TPB) {  // (idx: position p holds matrix idx[base + p])
+    const int p = e / 9;
+    const long long g = idx ? (long long)idx[base + p] : base + p, ge = g * 9 + (e - 9 * p);
+    S.x[e] = A[ge];
+    if (W) S.w[e] = W[ge];
+    if (V) S.v[e] = V[ge];
+    if (e == 9 * p) S.gidx[p] = g;
   }
   __syncthreads();
   unsigned key = 0xFFFFFFFFu;
@@ -242,7 +246,7 @@ __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const 
 #pragma unroll
   for (int q = 0; q < 4; q++) {
     if (!dst[q]) continue;
-    for (int e = tid; e < cnt * 9; e += GADJ_TPB) dst[q][base * 9 + e] = (T)S.out[q][e];
+    for (int e = tid; e < cnt * 9; e += GADJ_TPB) dst[q][S.gidx[e / 9] * 9 + e % 9] = (T)S.out[q][e];
   }
 }
 
@@ -438,7 +442,7 @@ __global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel_f32(int64_t n, co
 // ------------------------------------------------------------------------------------------------ launchers
 template <int KIND, int ORDER, typename T>
 cudaError_t gmf_adjoint_one(unsigned blocks, int64_t n, const T *A, const T *W, const T *V, T *F, T *Abar, T *JV,
-                            T *HWV, const GmfCoef &C, cudaStream_t st) {
+                            T *HWV, const GmfCoef &C, cudaStream_t st, const int *idx = nullptr) {
   static bool attr = false;  // per instantiation (idempotent)
   if (!attr) {
     const cudaError_t e = cudaFuncSetAttribute(gmf_adjoint_kernel<KIND, ORDER, T>,
@@ -446,10 +450,14 @@ cudaError_t gmf_adjoint_one(unsigned blocks, int64_t n, const T *A, const T *W, 
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  gmf_adjoint_kernel<KIND, ORDER, T><<<blocks, GADJ_TPB, sizeof(GadjSmem), st>>>(n, A, W, V, F, Abar, JV, HWV, C);
+  gmf_adjoint_kernel<KIND, ORDER, T><<<blocks, GADJ_TPB, sizeof(GadjSmem), st>>>(n, A, W, V, F, Abar, JV, HWV, C,
+                                                                                  idx);
   return cudaGetLastError();
 }
 
+// the batch ordering of gmf_kernels.cuh (log, pow; large batches): the adjoint outputs are too small to hold the
+// scratch, so it comes from the stream-ordered allocator (cudaMallocAsync / cudaFreeAsync on the call's stream: no
+// synchronisation, capturable, nothing shared between calls); without it the unordered launch runs
 template <int KIND, typename T = double>
 cudaError_t gmf_adjoint_t(double al, int64_t n, const T *A, const T *W, const T *V, T *F, T *Abar, T *JV, T *HWV,
                           cudaStream_t st) {
@@ -457,8 +465,25 @@ cudaError_t gmf_adjoint_t(double al, int64_t n, const T *A, const T *W, const T 
   GmfCoef C;
   gmf_coef(KIND, al, order, C);
   const unsigned blocks = (unsigned)((n + GADJ_TPB - 1) / GADJ_TPB);
-  return order == 2 ? gmf_adjoint_one<KIND, 2, T>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st)
-                    : gmf_adjoint_one<KIND, 1, T>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st);
+  int *ord = nullptr;
+  if ((KIND != EXP) & (n >= GMF_SORT_MIN) & (n <= INT_MAX)) {
+    const int nblk = (int)((n + GKEY_TPB - 1) / GKEY_TPB);
+    void *scr = nullptr;
+    if (cudaMallocAsync(&scr, (size_t)(4 * n + 4 * (int64_t)GKEY_BINS * nblk + n + 16), st) == cudaSuccess) {
+      ord = static_cast<int *>(scr);
+      int *counts = ord + n;
+      unsigned char *keys = reinterpret_cast<unsigned char *>(counts + (int64_t)GKEY_BINS * nblk);
+      gmf_key_kernel<KIND, T><<<nblk, GKEY_TPB, 0, st>>>((int)n, A, keys, counts, nblk, nullptr);
+      gmf_scan_kernel<<<1, 1024, 0, st>>>(counts, GKEY_BINS * nblk);
+      gmf_scatter_kernel<<<nblk, GKEY_TPB, 0, st>>>((int)n, keys, counts, nblk, ord);
+    } else {
+      cudaGetLastError();  // no pool memory: the unordered launch
+    }
+  }
+  const cudaError_t e = order == 2 ? gmf_adjoint_one<KIND, 2, T>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st, ord)
+                                   : gmf_adjoint_one<KIND, 1, T>(blocks, n, A, W, V, F, Abar, JV, HWV, C, st, ord);
+  if (ord) cudaFreeAsync(ord, st);
+  return e;
 }
 
 template <int KIND>
