@@ -481,8 +481,15 @@ def run_ours(args, rank, world, local):
         e2e_step()  # synchronous: returns when the results are in host memory
     e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0) / e2e_steps, world)
     e2e_value = whole_job_rate(n, e2e_ms, world)
-    # result check of the last e2e step against the device result
-    assert torch.equal(hH[:4].to(dev), dH[:4]) and torch.equal(hF[-4:].to(dev), dF[-4:])
+    # result check of the last e2e step against the device result: the host path evaluates the batch in its given
+    # order, the device path ordered by spectral class, so a matrix may take the real or the complex form of the
+    # series depending on its warp neighbours (last-bit differences)
+    for h, d in ((hH[:4], dH[:4]), (hF[-4:], dF[-4:])):
+        d = d.cpu()
+        assert torch.equal(torch.isnan(h), torch.isnan(d))
+        ok = ~torch.isnan(d)
+        if ok.any():
+            assert (h - d).abs()[ok].max() <= 1e-13 * d.abs()[ok].max()
 
     hbm, peak_kind = peaks()
     import ctypes

@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const 
   const int mine = S.perm[tid];
   if (mine < cnt) {
     GmfRec R;
-    gmf_finish<KIND, ORDER>(S.state[mine], C, R);
+    gmf_finish<KIND, ORDER, sizeof(T) == 4>(S.state[mine], C, R);
     // FP32: fold the scale factors into D2', D3' in FP64 when finite and nonzero, then round the record once
     constexpr bool MIXED = sizeof(T) == 4;
     const double rsc2 = ORDER >= 2 ? R.sc2 : 1.0;

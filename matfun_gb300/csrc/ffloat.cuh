@@ -48,6 +48,29 @@ MF_D ffl ff_mul(ffl x, ffl y) {
   return fast_two_sum(p.hi, p.lo);
 }
 MF_D ffl ff_from(float a) { return {a, 0.f}; }
+MF_D ffl ff_of(double x) {  // a double rounded to float-float (48 bits; x within FP32's range)
+  const float h = (float)x;
+  return {h, (float)(x - (double)h)};
+}
+MF_D double ff_dbl(ffl x) { return (double)x.hi + (double)x.lo; }
+MF_D ffl ff_prod(ffl x, ffl y) {  // x * y, not renormalised (hi = fl(x.hi y.hi), lo the remainder)
+  const float p = x.hi * y.hi;
+  return {p, fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)))};
+}
+MF_D ffl ff_add_s(ffl x, ffl y) {  // x + y with one two_sum (error relative to |x| + |y|), renormalised
+  const ffl s = two_sum(x.hi, y.hi);
+  return fast_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
+MF_D ffl ff_add3(ffl x, ffl y, ffl z) {  // x + y + z, renormalised
+  const ffl s = two_sum(x.hi, y.hi), t = two_sum(s.hi, z.hi);
+  return fast_two_sum(t.hi, ((x.lo + y.lo) + (z.lo + s.lo)) + t.lo);
+}
+MF_D ffl ff_sel(bool m, ffl a, ffl b) { return {m ? a.hi : b.hi, m ? a.lo : b.lo}; }
+MF_D void acc_ff_add(ffl &A, ffl p) {  // Sum2 accumulator (A.hi = running sum, A.lo = collected errors) += p
+  const ffl t = two_sum(A.hi, p.hi);
+  A.hi = t.hi;
+  A.lo += t.lo + p.lo;
+}
 
 // running compensated sum (Sum2 / Dot2 of Ogita-Rump-Oishi): S + E, every term added through two_sum
 struct ffacc {

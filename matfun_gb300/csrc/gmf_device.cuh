@@ -11,7 +11,7 @@
 // D2' and D3' with r into J and H through symmetric tensors (gmf_kernels.cu).
 // Written with sel() and non-short-circuit &, | (see mf_common.cuh) instead of long ?: / && chains.
 #pragma once
-#include "mf_common.cuh"
+#include "ffloat.cuh"
 
 namespace mf {
 
@@ -25,6 +25,8 @@ struct GmfCoef {
   double bh[3], bl[3];    // al - k split exactly (k = 0, 1, 2)
   double bt[G_KMAX];      // series coefficients b_j of f(c (1 + u)) (gmf_kernel.hpp:48-53)
   float lterm[G_KMAX];    // log2(|b_(n+k)| C(k + n, n)), n = 3 (order + 1) - 1: the term bound of gmf_kernel.hpp:73-97
+  float bth[G_KMAX], btl[G_KMAX];  // bt as float-float (hi + lo)
+  int ffser;              // 1: the group series may run in float-float (log, pow with every |b_j| <= 2^100)
 };
 
 // the 19 divided differences f[x0^a x1^b x2^c], a >= b >= c, a >= 1, in lexicographic order of (a, b, c); each is
@@ -168,9 +170,14 @@ MF_D cx coef0(const GmfCoef &C, double sig, double m, cx x, cx mu, int k) {
 // below 1e-17 of the largest, the pole series until C(k+2, 2) q^k <= 1e-17.  Evaluated on log2 values in FP32 (the
 // FP64 pipe is the bottleneck of this kernel) with a threshold 2^-0.05 below 1e-17, so that the count is never
 // smaller than the FP64 bound's; one term more changes a result by less than 1e-17 relative.
-MF_D int nterms(const GmfCoef &C, int n, double r, double q) {
+//
+// Also the term indices j1, j2 from which on every term is 2^-8 (j1) and 2^-32 (j2) below the largest term bound (the
+// bound is unimodal in k): group_series sums the terms from j1 on in float-float and from j2 on in FP32, whose
+// rounding errors (2^-48 and 2^-24 of the term) then stay below 2^-56 of the largest term, under the FP64 rounding of
+// the leading terms.
+MF_D int nterms(const GmfCoef &C, int n, double r, double q, int &j1, int &j2) {
   constexpr float L17 = -56.5237f - 0.05f;  // log2(1e-17) less a margin
-  int M = 1;
+  int M = 1, k1 = G_KMAX, k2 = G_KMAX;
   if (r > 0) {
     const float lr = log2f((float)r);
     float best = -INFINITY;
@@ -179,9 +186,13 @@ MF_D int nterms(const GmfCoef &C, int n, double r, double q) {
       const float t = C.lterm[k] + lk;
       best = fmaxf(best, t);
       M = k;
+      k1 = (k1 == G_KMAX) & (t <= best - 8.0f) ? k : k1;
+      k2 = (k2 == G_KMAX) & (t <= best - 32.0f) ? k : k2;
       if (((k > 2) & (t <= best + L17)) | (lk < -1074.0f)) break;
     }
   }
+  j1 = n + k1 < G_KMAX ? n + k1 : G_KMAX;
+  j2 = n + k2 < G_KMAX ? n + k2 : G_KMAX;
   if (q > 0) {
     const float lq = log2f((float)q);
     for (int k = 0; n + k < G_KMAX; k++) {
@@ -202,15 +213,108 @@ MF_D double log_b0(double sig, double m, double cxg, double cmu) {
 
 // the streamed group series (gmf_kernel.hpp:493-519) of the ND divided differences; REAL: every in-group offset
 // and hence every term is real (half the FP64 instructions of the complex recursion)
+// the terms j1 <= j < K of group_series without a pole node (every entry's coefficient is b_j): float-float up to
+// j2, FP32 from there on (see nterms), added to D at the end; Ep0 is the FP64 recursion state after term j1 - 1
+template <int ND, bool REAL>
+MF_D void group_tail(int K, int j1, int j2, const GmfCoef &C, const bool *inG, const cx *u, const cx *Ep0, cx *D) {
+  const ffl zero = {0.f, 0.f};
+  ffl ur[3], ui[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    ur[i] = ff_of(u[i].re);
+    ui[i] = REAL ? zero : ff_of(u[i].im);
+  }
+  ffl Er[ND], Ei[ND], Fr[ND], Fi[ND], Sr[ND], Si[ND];
+#pragma unroll
+  for (int c = 0; c < ND; c++) {
+    Er[c] = ff_of(Ep0[c].re);
+    Ei[c] = REAL ? zero : ff_of(Ep0[c].im);
+    Sr[c] = zero;
+    Si[c] = zero;
+  }
+  const int jb = K < j2 ? K : j2;
+  for (int j = j1; j < jb; j++) {
+    const ffl bj = {C.bth[j], C.btl[j]};
+#pragma unroll
+    for (int c = 0; c < ND; c++) {
+      const int par = gpar(c), i = gnode(c);
+      ffl eppr = par < 0 ? zero : Er[par < 0 ? 0 : par];
+      ffl epcr = par < 0 ? zero : Fr[par < 0 ? 0 : par];
+      if (REAL) {
+        Fr[c] = ff_sel(inG[i], ff_add_s(eppr, ff_prod(ur[i], Er[c])), epcr);
+        acc_ff_add(Sr[c], ff_prod(Fr[c], bj));
+      } else {
+        ffl eppi = par < 0 ? zero : Ei[par < 0 ? 0 : par];
+        ffl epci = par < 0 ? zero : Fi[par < 0 ? 0 : par];
+        ffl tr = ff_add3(eppr, ff_prod(ur[i], Er[c]), ff_neg(ff_prod(ui[i], Ei[c])));
+        ffl ti = ff_add3(eppi, ff_prod(ur[i], Ei[c]), ff_prod(ui[i], Er[c]));
+        Fr[c] = ff_sel(inG[i], tr, epcr);
+        Fi[c] = ff_sel(inG[i], ti, epci);
+        acc_ff_add(Sr[c], ff_prod(Fr[c], bj));
+        acc_ff_add(Si[c], ff_prod(Fi[c], bj));
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < ND; c++) {
+      Er[c] = Fr[c];
+      if (!REAL) Ei[c] = Fi[c];
+    }
+  }
+  float er[ND], ei[ND], fr[ND], fi[ND], sr[ND], si[ND], vr[3], vi[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    vr[i] = ur[i].hi;
+    vi[i] = ui[i].hi;
+  }
+#pragma unroll
+  for (int c = 0; c < ND; c++) {
+    er[c] = Er[c].hi;
+    ei[c] = REAL ? 0.f : Ei[c].hi;
+    sr[c] = 0.f;
+    si[c] = 0.f;
+  }
+  for (int j = jb > j1 ? jb : j1; j < K; j++) {
+    const float bj = C.bth[j];
+#pragma unroll
+    for (int c = 0; c < ND; c++) {
+      const int par = gpar(c), i = gnode(c);
+      float eppr = par < 0 ? 0.f : er[par < 0 ? 0 : par], epcr = par < 0 ? 0.f : fr[par < 0 ? 0 : par];
+      if (REAL) {
+        fr[c] = inG[i] ? fmaf(vr[i], er[c], eppr) : epcr;
+        sr[c] = fmaf(fr[c], bj, sr[c]);
+      } else {
+        float eppi = par < 0 ? 0.f : ei[par < 0 ? 0 : par], epci = par < 0 ? 0.f : fi[par < 0 ? 0 : par];
+        float tr = fmaf(-vi[i], ei[c], fmaf(vr[i], er[c], eppr)), ti = fmaf(vi[i], er[c], fmaf(vr[i], ei[c], eppi));
+        fr[c] = inG[i] ? tr : epcr;
+        fi[c] = inG[i] ? ti : epci;
+        sr[c] = fmaf(fr[c], bj, sr[c]);
+        si[c] = fmaf(fi[c], bj, si[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < ND; c++) {
+      er[c] = fr[c];
+      if (!REAL) ei[c] = fi[c];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < ND; c++) {
+    D[c].re = D[c].re + (ff_dbl(Sr[c]) + (double)sr[c]);
+    if (!REAL) D[c].im = D[c].im + (ff_dbl(Si[c]) + (double)si[c]);
+  }
+}
+
+// the streamed group series (FP64 terms up to j1, the tail by group_tail; j1 >= K: all in FP64)
 template <int ND, bool REAL>
 MF_D void group_series(int K, double b0, const GmfCoef &C, const bool *inG, const bool *pk, const cx *u, double iap,
-                       cx *D) {
+                       cx *D, int j1 = G_KMAX, int j2 = G_KMAX) {
   cx Ep[ND], Ec[ND];
 #pragma unroll
   for (int c = 0; c < ND; c++)
     Ep[c] = csel(inG[gnode(c)], cmk(0.0, 0.0), gpar(c) < 0 ? cmk(1.0, 0.0) : Ep[gpar(c) < 0 ? 0 : gpar(c)]);
   double q1 = 0.0, q2 = 0.0, q3 = 0.0;
-  for (int j = 0; j < K; j++) {
+  const int ja = K < j1 ? K : j1;
+  for (int j = 0; j < ja; j++) {
     double bj = j == 0 ? b0 : C.bt[j];
     double g1 = (bj - q1) * iap, g2 = (g1 - q2) * iap, g3 = (g2 - q3) * iap;
     q1 = g1; q2 = g2; q3 = g3;
@@ -233,6 +337,81 @@ MF_D void group_series(int K, double b0, const GmfCoef &C, const bool *inG, cons
 #pragma unroll
     for (int c = 0; c < ND; c++) Ep[c] = Ec[c];
   }
+  if (K > ja) group_tail<ND, REAL>(K, ja, j2, C, inG, u, Ep, D);
+}
+
+// group_series entirely in float-float arithmetic on the FP32 pipe, for the FP32-storage kernels (about 48
+// significant bits: 2^-48 of the largest term, amplified by the cancellation of the series, stays far below their
+// FP32 results' rounding, but not below that of FP64 results, hence the split of group_tail there).  The same recursion
+// and terms, rescaled by S = 2^-e (2^e > |iap|, e <= 8) so that every intermediate stays inside FP32's exponent
+// range: offsets u/S, coefficients b_j S^j, pole recursion with the factor S iap (|S iap| < 1, so the pole
+// coefficients no longer grow like iap^j); then D[c] = S^-d D~[c] with d = (multiplicity of c's in-group and pole
+// nodes) - 1, exact powers of two.  The terms are summed with Sum2 (two_sum per term, errors collected).
+template <int ND, bool REAL>
+MF_D void group_series_ff(int K, double b0, const GmfCoef &C, const bool *inG, const bool *pk, const cx *u,
+                          double iap, int e, cx *D) {
+  const double up = __longlong_as_double((long long)(1023 + e) << 52);  // 2^e
+  const float S = __int_as_float((127 - e) << 23);                      // 2^-e
+  ffl ur[3], ui[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    ur[i] = ff_of(u[i].re * up);
+    ui[i] = REAL ? ffl{0.f, 0.f} : ff_of(u[i].im * up);
+  }
+  const ffl qh = ff_of(iap / up), zero = {0.f, 0.f}, one = {1.f, 0.f}, b0f = ff_of(b0);
+  ffl Epr[ND], Epi[ND], Ecr[ND], Eci[ND], Dr[ND], Di[ND];
+#pragma unroll
+  for (int c = 0; c < ND; c++) {
+    Epr[c] = ff_sel(inG[gnode(c)], zero, gpar(c) < 0 ? one : Epr[gpar(c) < 0 ? 0 : gpar(c)]);
+    Epi[c] = zero;
+    Dr[c] = zero;
+    Di[c] = zero;
+  }
+  ffl q1 = zero, q2 = zero, q3 = zero;
+  float sp = 1.f;
+  for (int j = 0; j < K; j++) {
+    ffl bj = {C.bth[j] * sp, C.btl[j] * sp};
+    bj = ff_sel(j == 0, b0f, bj);
+    sp *= S;
+    ffl g1 = ff_mul(ff_add_s(bj, ff_neg(q1)), qh), g2 = ff_mul(ff_add_s(g1, ff_neg(q2)), qh),
+        g3 = ff_mul(ff_add_s(g2, ff_neg(q3)), qh);
+    q1 = g1; q2 = g2; q3 = g3;
+    ffl qv[4] = {bj, g1, g2, g3};
+#pragma unroll
+    for (int c = 0; c < ND; c++) {
+      const int par = gpar(c), i = gnode(c);
+      ffl eppr = par < 0 ? ff_sel(j == 0, one, zero) : Epr[par < 0 ? 0 : par];
+      ffl epcr = par < 0 ? zero : Ecr[par < 0 ? 0 : par];
+      ffl g = ff_sel(pk[0], qv[gms(c, 0)], ff_sel(pk[1], qv[gms(c, 1)], ff_sel(pk[2], qv[gms(c, 2)], qv[0])));
+      if (REAL) {
+        Ecr[c] = ff_sel(inG[i], ff_add_s(eppr, ff_prod(ur[i], Epr[c])), epcr);
+        acc_ff_add(Dr[c], ff_prod(Ecr[c], g));
+      } else {
+        ffl eppi = par < 0 ? zero : Epi[par < 0 ? 0 : par];
+        ffl epci = par < 0 ? zero : Eci[par < 0 ? 0 : par];
+        ffl tr = ff_add3(eppr, ff_prod(ur[i], Epr[c]), ff_neg(ff_prod(ui[i], Epi[c])));
+        ffl ti = ff_add3(eppi, ff_prod(ur[i], Epi[c]), ff_prod(ui[i], Epr[c]));
+        Ecr[c] = ff_sel(inG[i], tr, epcr);
+        Eci[c] = ff_sel(inG[i], ti, epci);
+        acc_ff_add(Dr[c], ff_prod(Ecr[c], g));
+        acc_ff_add(Di[c], ff_prod(Eci[c], g));
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < ND; c++) {
+      Epr[c] = Ecr[c];
+      if (!REAL) Epi[c] = Eci[c];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < ND; c++) {
+    int d = -1;
+#pragma unroll
+    for (int i = 0; i < 3; i++) d += (inG[i] | pk[i]) ? gms(c, i) : 0;
+    d = d < 0 ? 0 : e * d;
+    const double sc = __longlong_as_double((long long)(1023 + d) << 52);
+    D[c] = cmk(ff_dbl(Dr[c]) * sc, REAL ? 0.0 : ff_dbl(Di[c]) * sc);
+  }
 }
 
 // the state after the spectral analysis (eigenvalues, refinement, node order, groups, offsets, series length):
@@ -243,7 +422,7 @@ struct GmfState {
   double sig, m, cxg, cmu, xshift, iap, L, iL;
   cx x[3], mu[3], u[3];
   int K;                            // series terms; 0 without a group
-  int flags;                        // ab (bits 0-2), inG (3-5), pk (6-8), bad (9), real offsets (10)
+  int flags;  // ab (bits 0-2), inG (3-5), pk (6-8), bad (9), real offsets (10), series split j1 (12-19), j2 (20-27)
 };
 constexpr int GMF_STATE_D = 9 + 8 + 18;  // doubles of a packed state (K and flags in two ints apart)
 
@@ -510,7 +689,12 @@ MF_D void gmf_classify_from(const double *a, const cx *xr, const GmfCoef &C, Gmf
   double rr = tmax(cabs_s(u[0]), tmax(cabs_s(u[1]), cabs_s(u[2])));
   double rq = sel((pk[0] | pk[1] | pk[2]) & (rr * fabs(iap) <= 1.0), rr * fabs(iap), 0.0);
   rr = sel(hasg & (rr <= G_R_EXP + 0.5), rr, 0.0);
-  St.K = hasg ? nterms(C, 3 * (ORDER + 1) - 1, rr, rq) : 0;
+  int j1, j2;
+  St.K = hasg ? nterms(C, 3 * (ORDER + 1) - 1, rr, rq, j1, j2) : 0;
+  // the float-float / FP32 tail of the series: log and pow without a pole node, coefficients within FP32's range
+  const bool tail = (KIND != EXP) & (C.ffser != 0) & !(pk[0] | pk[1] | pk[2]) & (rr <= 4.0);
+  j1 = tail ? j1 : G_KMAX;
+  j2 = tail ? j2 : G_KMAX;
   bool real = (u[0].im == 0) & (u[1].im == 0) & (u[2].im == 0);
 #pragma unroll
   for (int k = 0; k < 9; k++) St.As[k] = As[k];
@@ -519,7 +703,7 @@ MF_D void gmf_classify_from(const double *a, const cx *xr, const GmfCoef &C, Gmf
   for (int i = 0; i < 3; i++) { St.x[i] = x[i]; St.mu[i] = mu[i]; St.u[i] = u[i]; }
   St.flags = (ab[0] ? 1 : 0) | (ab[1] ? 2 : 0) | (ab[2] ? 4 : 0) | (inG[0] ? 8 : 0) | (inG[1] ? 16 : 0) |
              (inG[2] ? 32 : 0) | (pk[0] ? 64 : 0) | (pk[1] ? 128 : 0) | (pk[2] ? 256 : 0) | (bad ? 512 : 0) |
-             (real ? 1024 : 0);
+             (real ? 1024 : 0) | (j1 << 12) | (j2 << 20);
 }
 
 template <int KIND, int ORDER>
@@ -530,7 +714,7 @@ MF_D void gmf_classify(const double *a, const GmfCoef &C, GmfState &St) {
 }
 
 // the second half: divided differences (series, residues), real basis, F and the reduced D2', D3'
-template <int KIND, int ORDER>
+template <int KIND, int ORDER, bool FF = false>
 MF_D void gmf_finish(const GmfState &St, const GmfCoef &C, GmfRec &R) {
   constexpr int ND = ORDER == 0 ? 3 : (ORDER == 1 ? 9 : 19);
   double As[9], S[9];
@@ -555,8 +739,22 @@ MF_D void gmf_finish(const GmfState &St, const GmfCoef &C, GmfRec &R) {
   for (int c = 0; c < ND; c++) D[c] = cmk(0.0, 0.0);
   if (hasg) {
     const bool real = (fl & 1024) != 0;
-    if (__all_sync(__activemask(), real)) group_series<ND, true>(St.K, b0, C, inG, pk, u, iap, D);
-    else group_series<ND, false>(St.K, b0, C, inG, pk, u, iap, D);
+    const unsigned am = __activemask();
+    // FP32 storage: the whole series in float-float where coefficients, offsets and pole factor fit FP32's range
+    const double aiap = fabs(iap);
+    const int e = aiap > 1.0 ? (int)((__double_as_longlong(aiap) >> 52) & 0x7FF) - 1022 : 0;
+    const bool ffok = FF & (KIND != EXP) & (C.ffser != 0) & (aiap < 256.0) & (fabs(b0) < 1e30) &
+                      (cabs_s(u[0]) <= 4.0) & (cabs_s(u[1]) <= 4.0) & (cabs_s(u[2]) <= 4.0);
+    if (FF && KIND != EXP && __all_sync(am, ffok)) {
+      if (__all_sync(am, real)) group_series_ff<ND, true>(St.K, b0, C, inG, pk, u, iap, e, D);
+      else group_series_ff<ND, false>(St.K, b0, C, inG, pk, u, iap, e, D);
+    } else {
+      // FP64 leading terms, float-float / FP32 tail from this matrix's own split points (so that its result does
+      // not depend on the matrices beside it in the warp)
+      const int j1 = (fl >> 12) & 255, j2 = (fl >> 20) & 255;
+      if (__all_sync(am, real)) group_series<ND, true>(St.K, b0, C, inG, pk, u, iap, D, j1, j2);
+      else group_series<ND, false>(St.K, b0, C, inG, pk, u, iap, D, j1, j2);
+    }
 #pragma unroll
     for (int c = 0; c < ND; c++) {
       const int nn = gms(c, 0) + gms(c, 1) + gms(c, 2) - 1, k = gms(c, 0) - 1;

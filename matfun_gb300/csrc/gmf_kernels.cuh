@@ -177,7 +177,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   const int mine = S.perm[tid];
   if (mine < cnt) {
     GmfRec R;
-    gmf_finish<KIND, ORDER>(S.state[mine], C, R);
+    gmf_finish<KIND, ORDER, sizeof(T) == 4>(S.state[mine], C, R);
 #pragma unroll
     for (int k = 0; k < 9; k++) F[S.gidx[mine] * 9 + k] = (T)R.F[k];
     if (ORDER >= 1) {
@@ -449,6 +449,12 @@ inline void gmf_coef(int kind, double al, int order, GmfCoef &C) {
   C.bt[0] = 1.0;
   for (int j = 1; j < G_KMAX; j++)
     C.bt[j] = kind == EXP ? C.bt[j - 1] / j : (kind == LOG ? (j % 2 ? 1.0 : -1.0) / j : C.bt[j - 1] * (al - j + 1) / j);
+  C.ffser = kind != EXP;
+  for (int j = 0; j < G_KMAX; j++) {
+    C.ffser &= std::fabs(C.bt[j]) <= 0x1p100;  // (false for a NaN)
+    C.bth[j] = (float)C.bt[j];
+    C.btl[j] = C.ffser ? (float)(C.bt[j] - (double)C.bth[j]) : 0.f;
+  }
   const int nn = 3 * (order + 1) - 1;
   double c = 1.0;
   for (int k = 0; k < G_KMAX; k++) {

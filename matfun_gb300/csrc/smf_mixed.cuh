@@ -350,7 +350,6 @@ struct SmfSpecF {
 };
 
 MF_D bool ff_less(ffl a, ffl b) { return (a.hi < b.hi) | ((a.hi == b.hi) & (a.lo < b.lo)); }
-MF_D ffl ff_sel(bool c, ffl a, ffl b) { return {self(c, a.hi, b.hi), self(c, a.lo, b.lo)}; }
 
 template <int KIND, bool LO>
 MF_D void smf_spectrum_f(const SmfInF &in, const SmfCoefF &C, SmfSpecF &Sp) {
