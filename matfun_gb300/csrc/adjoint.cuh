@@ -469,13 +469,13 @@ cudaError_t gmf_adjoint_t(double al, int64_t n, const T *A, const T *W, const T 
   if ((KIND != EXP) & (n >= GMF_SORT_MIN) & (n <= INT_MAX)) {
     const int nblk = (int)((n + GKEY_TPB - 1) / GKEY_TPB);
     void *scr = nullptr;
-    if (cudaMallocAsync(&scr, (size_t)(4 * n + 4 * (int64_t)GKEY_BINS * nblk + n + 16), st) == cudaSuccess) {
+    if (cudaMallocAsync(&scr, (size_t)(4 * n + 4 * (int64_t)GKEY_BINS * (nblk + 1) + n + 16), st) == cudaSuccess) {
       ord = static_cast<int *>(scr);
-      int *counts = ord + n;
-      unsigned char *keys = reinterpret_cast<unsigned char *>(counts + (int64_t)GKEY_BINS * nblk);
+      int *counts = ord + n, *totals = counts + (int64_t)GKEY_BINS * nblk;
+      unsigned char *keys = reinterpret_cast<unsigned char *>(totals + GKEY_BINS);
       gmf_key_kernel<KIND, T><<<nblk, GKEY_TPB, 0, st>>>((int)n, A, keys, counts, nblk, nullptr);
-      gmf_scan_kernel<<<1, 1024, 0, st>>>(counts, GKEY_BINS * nblk);
-      gmf_scatter_kernel<<<nblk, GKEY_TPB, 0, st>>>((int)n, keys, counts, nblk, ord);
+      gmf_scan_kernel<<<GKEY_BINS, 1024, 0, st>>>(counts, nblk, totals);
+      gmf_scatter_kernel<<<nblk, GKEY_TPB, 0, st>>>((int)n, keys, counts, totals, nblk, ord);
     } else {
       cudaGetLastError();  // no pool memory: the unordered launch
     }

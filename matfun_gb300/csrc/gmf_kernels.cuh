@@ -333,44 +333,68 @@ __global__ void __launch_bounds__(GKEY_TPB) gmf_key_kernel(int n, const T *__res
   for (int k = threadIdx.x; k < GKEY_BINS; k += GKEY_TPB) counts[k * nblk + blockIdx.x] = hist[k];
 }
 
-// exclusive prefix sum of counts[0 .. total) in place, by one CTA of 1024 threads
-static __global__ void __launch_bounds__(1024) gmf_scan_kernel(int *__restrict__ counts, int total) {
-  __shared__ int part[1024];
-  const int per = (total + 1023) / 1024, lo = min(total, (int)threadIdx.x * per), hi = min(total, lo + per);
-  int s = 0;
-  for (int i = lo; i < hi; i++) s += counts[i];
-  part[threadIdx.x] = s;
+// exclusive prefix sums of the rows counts[k nblk .. (k + 1) nblk) in place (one CTA of 1024 threads per key k,
+// coalesced; warp shuffles, then the 32 warp sums) and the row totals
+static __global__ void __launch_bounds__(1024) gmf_scan_kernel(int *__restrict__ counts, int nblk,
+                                                                int *__restrict__ totals) {
+  __shared__ int wsum[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int *row = counts + (int64_t)blockIdx.x * nblk;
+  int carry = 0;
+  for (int base = 0; base < nblk; base += 1024) {
+    const int i = base + (int)threadIdx.x;
+    const int v = i < nblk ? row[i] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      x += lane >= o ? y : 0;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = wsum[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+        w += lane >= o ? y : 0;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    if (i < nblk) row[i] = carry + (warp ? wsum[warp - 1] : 0) + x - v;
+    carry += wsum[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+// order[start(key) + offset(key, block) + rank among the equal keys before it in its block] = i: a stable sort by
+// key; start(key) = the exclusive prefix sum of the row totals (GKEY_BINS = GKEY_TPB entries, scanned here)
+static __global__ void __launch_bounds__(GKEY_TPB) gmf_scatter_kernel(int n, const unsigned char *__restrict__ keys,
+                                                                      const int *__restrict__ offs,
+                                                                      const int *__restrict__ totals, int nblk,
+                                                                      int *__restrict__ order) {
+  __shared__ int sk[GKEY_TPB], start[GKEY_BINS];
+  static_assert(GKEY_BINS == GKEY_TPB, "one key per thread in the scan of the totals");
+  const int i = blockIdx.x * GKEY_TPB + threadIdx.x;
+  sk[threadIdx.x] = i < n ? (int)keys[i] : -1;
+  start[threadIdx.x] = totals[threadIdx.x];
   __syncthreads();
   if (threadIdx.x == 0) {
     int acc = 0;
-    for (int j = 0; j < 1024; j++) {
-      const int v = part[j];
-      part[j] = acc;
+    for (int k = 0; k < GKEY_BINS; k++) {
+      const int v = start[k];
+      start[k] = acc;
       acc += v;
     }
   }
-  __syncthreads();
-  int acc = part[threadIdx.x];
-  for (int i = lo; i < hi; i++) {
-    const int v = counts[i];
-    counts[i] = acc;
-    acc += v;
-  }
-}
-
-// order[offset(key, block) + rank among the equal keys before it in its block] = i: a stable sort by key
-static __global__ void __launch_bounds__(GKEY_TPB) gmf_scatter_kernel(int n, const unsigned char *__restrict__ keys,
-                                                               const int *__restrict__ offs, int nblk,
-                                                               int *__restrict__ order) {
-  __shared__ int sk[GKEY_TPB];
-  const int i = blockIdx.x * GKEY_TPB + threadIdx.x;
-  sk[threadIdx.x] = i < n ? (int)keys[i] : -1;
   __syncthreads();
   if (i < n) {
     const int key = sk[threadIdx.x];
     int r = 0;
     for (int j = 0; j < (int)threadIdx.x; j++) r += sk[j] == key;
-    order[offs[key * nblk + blockIdx.x] + r] = i;
+    order[start[key] + offs[key * nblk + blockIdx.x] + r] = i;
   }
 }
 
@@ -396,23 +420,24 @@ cudaError_t gmf_launch_sorted(cudaStream_t st, int64_t n, const T *A, T *F, T *J
   T *big = ORDER == 2 ? H : J;
   const int64_t per = ORDER == 2 ? 729 : 81;  // elements of the largest output per matrix
   const int64_t nblk_n = (n + GKEY_TPB - 1) / GKEY_TPB;
-  // order, counts, keys (bytes) and, for order 2, the roots (48 bytes per matrix; the tail stays ~1 % of the batch)
-  const int64_t need = 4 * n + 4 * (int64_t)GKEY_BINS * nblk_n + n + (ORDER == 2 ? 48 * n + 8 : 0) + 64;
+  // order, counts, totals, keys (bytes) and, for order 2, the roots (48 bytes per matrix; the tail stays ~1 % of the
+  // batch)
+  const int64_t need = 4 * n + 4 * (int64_t)GKEY_BINS * (nblk_n + 1) + n + (ORDER == 2 ? 48 * n + 8 : 0) + 64;
   const int64_t tail = (need + per * (int64_t)sizeof(T) - 1) / (per * (int64_t)sizeof(T)) + 1;
   const int64_t nm = n - tail;
   const int nblk = (int)((nm + GKEY_TPB - 1) / GKEY_TPB);
   char *scr = reinterpret_cast<char *>(big + nm * per);
   int *order = reinterpret_cast<int *>(scr);
-  int *counts = order + nm;
-  unsigned char *keys = reinterpret_cast<unsigned char *>(counts + (int64_t)GKEY_BINS * nblk);
+  int *counts = order + nm, *totals = counts + (int64_t)GKEY_BINS * nblk;
+  unsigned char *keys = reinterpret_cast<unsigned char *>(totals + GKEY_BINS);
   double *roots = nullptr;
   if (ORDER == 2) {
     const uintptr_t r = reinterpret_cast<uintptr_t>(keys + nm);
     roots = reinterpret_cast<double *>((r + 7) & ~(uintptr_t)7);
   }
   gmf_key_kernel<KIND, T><<<nblk, GKEY_TPB, 0, st>>>((int)nm, A, keys, counts, nblk, roots);
-  gmf_scan_kernel<<<1, 1024, 0, st>>>(counts, GKEY_BINS * nblk);
-  gmf_scatter_kernel<<<nblk, GKEY_TPB, 0, st>>>((int)nm, keys, counts, nblk, order);
+  gmf_scan_kernel<<<GKEY_BINS, 1024, 0, st>>>(counts, nblk, totals);
+  gmf_scatter_kernel<<<nblk, GKEY_TPB, 0, st>>>((int)nm, keys, counts, totals, nblk, order);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((nm + GMF_TPB - 1) / GMF_TPB), nm, A, F, J, H, C, order, roots,
