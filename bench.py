@@ -28,13 +28,21 @@ sys.path.insert(0, ROOT)
 KINDS = {"exp": 0, "log": 1, "pow": 2, "sqrt": 3}
 BYTES_PER_MATRIX = {0: 72 + 72, 1: 72 + 72 + 648, 2: 72 + 72 + 648 + 5832}  # FP64 in + F (+ J) (+ H)
 METRIC = "gmf log order-2 matrices/s (FP64)"
-# FP64 floating-point operations per matrix executed by gmf_kernel<KIND, 2> on this workload (2 per DFMA), from the
-# ncu counters smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum (profiles/gmf_kernel_log_o2_c1.md)
-FP64_FLOP_PER_MATRIX = {"log": 2 * 3456 + 1805 + 1283}
-# DRAM bytes per matrix of gmf_kernel<LOG, 2> from one ncu capture at n = 65536 on the same workload (374.2 MB read +
-# written; the last writes of that launch still sit in L2 when the kernel ends, so a full launch moves up to the
-# algorithmic 6624 B per matrix)
-NCU_DRAM_BYTES_PER_MATRIX = 374.2e6 / 65536
+# FP64 floating-point operations per matrix of one order-2 call on this workload (2 per DFMA): the ordered gmf_kernel
+# <LOG, 2> (DFMA 2355, DADD 1006, DMUL 723) plus gmf_key_kernel (the closed-form roots: 144, 64, 76), from the ncu
+# counters smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum at n = 262144
+# (profiles/gmf_kernel_log_o2_c1.md)
+FP64_FLOP_PER_MATRIX = {"log": 2 * (2355 + 144) + (1006 + 64) + (723 + 76)}
+# DRAM bytes per matrix of the ordered gmf_kernel<LOG, 2> launch from one ncu capture at n = 262144 on the same
+# workload (101.4 MB read + 1752.0 MB written for 259 584 matrices; the algorithmic bytes are 6624 per matrix, the
+# extra reads are the partial sectors at the ends of the rows the ordered launch scatters)
+NCU_DRAM_BYTES_PER_MATRIX = (101.44e6 + 1752.03e6) / 259584
+
+
+def launches_per_call(kind, n):
+    """kernels one order-2 gmf_cuda_eval call launches: key, scan, scatter, the ordered launch and the tail launch
+    (log, sqrt, pow with 2^15 <= n <= 2^31 - 1), else one plain launch"""
+    return 5 if kind != "exp" and (1 << 15) <= n <= (1 << 31) - 1 else 1
 
 
 def peaks():
@@ -460,8 +468,9 @@ def run_ours(args, rank, world, local):
     ms = max_over_ranks(ms, world)
     value = whole_job_rate(n, ms, world)
 
-    # e2e: the host-buffer C ABI (gmf_cuda_eval_host: the reference's gmf_eval signature on host arrays; chunks
-    # copied in, evaluated and copied out on two streams) on page-locked host arrays, copies inside the timed region
+    # e2e: the host-buffer C ABI (gmf_cuda_eval_host: the reference's gmf_eval signature on host arrays) on
+    # page-locked host arrays: the kernels read A and write F, J, H in host memory over the host link, inside the
+    # timed region
     hA = torch.from_numpy(X).pin_memory()
     hF = torch.empty((n, 9), dtype=torch.float64).pin_memory()
     hJ = torch.empty((n, 81), dtype=torch.float64).pin_memory()
@@ -510,20 +519,21 @@ def run_ours(args, rank, world, local):
                             "frac": achieved / hbm, "peak_source": peak_kind,
                             "traffic": (NCU_DRAM_BYTES_PER_MATRIX * n / 1e9) if args.kind == "log" else None,
                             "traffic_unit": "GB per launch",
-                            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of gmf_kernel<LOG,2> "
-                                              "at n=65536 (374.2 MB), scaled by n",
+                            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the ordered "
+                                              "gmf_kernel<LOG,2> launch at n=262144 (1853.5 MB), scaled by n",
                             "note": "algorithmic bytes (72 in + 6552 out per matrix) / event time; the kernel is "
                                     "bound by the FP64 pipe (see fp64), not by HBM"},
                "fp64": {"peak_tflops": fp64_peak.value if fp64_ok else None,
                         "peak_source": "measured live: 8 independent DFMA chains per thread (matfun_cuda_fp64_peak)",
                         "achieved_tflops": FP64_FLOP_PER_MATRIX.get(args.kind, 0) * n / (ms * 1e-3) / 1e12 or None,
                         "flop_per_matrix": FP64_FLOP_PER_MATRIX.get(args.kind),
-                        "flop_source": "ncu dfma x2 + dadd + dmul per matrix, gmf_kernel<LOG,2>, this workload"},
+                        "flop_source": "ncu dfma x2 + dadd + dmul per matrix, gmf_kernel<LOG,2> + gmf_key_kernel, "
+                                       "this workload"},
                "e2e": {"value": e2e_value, "unit": "matrices/s", "h2d_bytes_per_step": int(hA.numel() * 8),
                        "d2h_bytes_per_step": int((hF.numel() + hJ.numel() + hH.numel()) * 8),
                        "ms_per_step": e2e_ms, "api": "gmf_cuda_eval_host",
                        "timer": "host wall clock around the synchronous call"},
-               "gpu_launches": args.steps,
+               "gpu_launches": args.steps * launches_per_call(args.kind, n),
                "clocks": clk.summary()}
     del dA, dF, dJ, dH
     if rank == 0 and not args.no_mixed:
