@@ -200,9 +200,9 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
-def _mixed_pair(x32, nf, fn32, fn64, steps, dev):
-    """time the FP32 entry point and the FP64 one (log, order 2) on the same values; max relative error of the FP32
-    results against the FP64 ones (max-norm per output array) on a sample of 65536 matrices"""
+def _mixed_pair(x32, nf, fn32, fn64, steps, dev, kind=1, alpha=0.0, order=2):
+    """time the FP32 entry point and the FP64 one (default: log, order 2) on the same values; max relative error of
+    the FP32 results against the FP64 ones (max-norm per output array) on a sample of 65536 matrices"""
     import torch
     n = x32.shape[0]
     d32 = x32.to(dev)
@@ -210,9 +210,10 @@ def _mixed_pair(x32, nf, fn32, fn64, steps, dev):
     outs = {}
     for tag, dt, x, fn in (("f32", torch.float32, d32, fn32), ("f64", torch.float64, d64, fn64)):
         F = torch.empty((n, nf), dtype=dt, device=dev)
-        J = torch.empty((n, nf ** 2), dtype=dt, device=dev)
-        H = torch.empty((n, nf ** 3), dtype=dt, device=dev)
-        call = lambda: fn(1, 0.0, n, x.data_ptr(), F.data_ptr(), J.data_ptr(), H.data_ptr(), None)
+        J = torch.empty((n, nf ** 2), dtype=dt, device=dev) if order >= 1 else None
+        H = torch.empty((n, nf ** 3), dtype=dt, device=dev) if order >= 2 else None
+        p = lambda t: None if t is None else t.data_ptr()
+        call = lambda: fn(kind, alpha, n, x.data_ptr(), p(F), p(J), p(H), None)
         for _ in range(2):
             assert call() == 0
         torch.cuda.synchronize()
@@ -226,7 +227,7 @@ def _mixed_pair(x32, nf, fn32, fn64, steps, dev):
         del F, J, H
     idx = torch.arange(0, n, max(1, n // 65536), device=dev)
     err = {}
-    for k, name in ((1, "F"), (2, "J"), (3, "H")):
+    for k, name in ((1, "F"), (2, "J"), (3, "H"))[:order + 1]:
         a, b = outs["f32"][k][idx].double(), outs["f64"][k][idx]
         both = torch.isnan(a) & torch.isnan(b)
         d = torch.where(both, torch.zeros_like(a), (a - b).abs())
@@ -254,6 +255,30 @@ def mixed_vs_fp64(lib, args, dev, hbm):
             "mixed_hbm_frac": bytes32 * n / (ms32 * 1e-3) / 1e9 / hbm, "bytes_per_matrix_fp32": bytes32}
 
 
+def mixed_sweep(lib, args, dev, hbm):
+    """the C2 workload over every kind and order (smf Voigt, n = 2^24 SPD stored as FP32; pow with one exponent
+    alpha ~ U(0.1, 0.9) per call, seeded): the mixed-precision path against the FP64 path on the same values"""
+    import torch
+
+    from matfun_gb300 import workloads as w
+    n = args.mixed_n
+    x32 = torch.from_numpy(w.c2_smf_spd(n, seed=2))
+    rng = np.random.default_rng(2)
+    rows = []
+    for name, kind in (("exp", 0), ("log", 1), ("sqrt", 3), ("pow", 2)):
+        alpha = float(rng.uniform(0.1, 0.9)) if kind == 2 else 0.0
+        for order in (0, 1, 2):
+            ms32, ms64, err, ns = _mixed_pair(x32, 6, lib.smf_cuda_eval_f32, lib.smf_cuda_eval, args.mixed_steps,
+                                              dev, kind, alpha, order)
+            b32 = 4 * (6 + (6, 42, 258)[order])
+            rows.append({"kind": name, "alpha": alpha, "order": order, "mixed_matrices_per_s": n / (ms32 * 1e-3),
+                         "fp64_matrices_per_s": n / (ms64 * 1e-3), "speedup_vs_fp64": ms64 / ms32,
+                         "mixed_hbm_frac": b32 * n / (ms32 * 1e-3) / 1e9 / hbm, "max_rel_err_vs_fp64": err})
+            torch.cuda.empty_cache()
+    return {"workload": f"C2: smf Voigt, n={n} SPD, condition log-uniform [1,1e6], smallest gap log-uniform "
+                        "[1e-12,1], FP32 storage; every kind and order", "err_sample": ns, "rows": rows}
+
+
 def mixed_gmf_vs_fp64(lib, args, dev, hbm):
     """gmf log order 2 on the C1 workload (n = 2^20, the four groups), stored as FP32: the mixed-precision gmf path
     (FP64 spectral analysis and series, FP32 storage and J / H assembly) against the FP64 path on the same values"""
@@ -269,6 +294,55 @@ def mixed_gmf_vs_fp64(lib, args, dev, hbm):
             "speedup_vs_fp64": ms64 / ms32, "mixed_ms": ms32, "fp64_ms": ms64,
             "max_rel_err_vs_fp64": err, "err_sample": ns,
             "mixed_hbm_frac": bytes32 * n / (ms32 * 1e-3) / 1e9 / hbm, "bytes_per_matrix_fp32": bytes32}
+
+
+def tangent_vs_materialised(lib, args, dev):
+    """the tangent of psi(A) = |log A|^2 / 2 (G = J^T F, K = J^T J + F : H) on the C1 workload, n = 2^20 FP64: the
+    fused kernel (gmf_cuda_tangent, no J or H formed) against evaluating F, J, H (gmf_cuda_eval) and contracting them
+    with torch (bmm / einsum), with the max relative difference of the two on the whole batch"""
+    import torch
+
+    from matfun_gb300 import workloads as w
+    n = args.n
+    A = torch.from_numpy(w.c1_gmf_groups(n, seed=1).reshape(n, 9)).to(dev)
+    F, G, K = (torch.empty((n, k), dtype=torch.float64, device=dev) for k in (9, 9, 81))
+    Fe, Je, He = (torch.empty((n, k), dtype=torch.float64, device=dev) for k in (9, 81, 729))
+    st = torch.cuda.current_stream().cuda_stream
+
+    def fused():
+        assert lib.gmf_cuda_tangent(1, 0.0, n, A.data_ptr(), F.data_ptr(), G.data_ptr(), K.data_ptr(), st) == 0
+
+    def unfused():
+        assert lib.gmf_cuda_eval(1, 0.0, n, A.data_ptr(), Fe.data_ptr(), Je.data_ptr(), He.data_ptr(), st) == 0
+        Jm = Je.view(n, 9, 9)
+        Gu = torch.bmm(Fe.view(n, 1, 9), Jm).view(n, 9)
+        Ku = torch.bmm(Jm.transpose(1, 2), Jm) + torch.bmm(Fe.view(n, 1, 9), He.view(n, 9, 81)).view(n, 9, 9)
+        return Gu, Ku
+
+    def timed(fn, steps):
+        for _ in range(2):
+            out = fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            out = fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / steps, out
+
+    t_f, _ = timed(fused, 3)
+    t_u, (Gu, Ku) = timed(unfused, 3)
+
+    def rel(a, b):
+        d = torch.where(torch.isnan(a) & torch.isnan(b), torch.zeros_like(a), (a - b).abs())
+        return float(d.max() / torch.nan_to_num(b, nan=0.0).abs().max())
+
+    return {"workload": f"psi(A) = |log A|^2 / 2 on C1, n={n} FP64: F, G = J^T F, K = J^T J + F : H",
+            "fused_matrices_per_s": n / (t_f * 1e-3), "fused_ms": t_f,
+            "materialised_matrices_per_s": n / (t_u * 1e-3), "materialised_ms": t_u, "speedup": t_u / t_f,
+            "bytes_written_per_matrix": {"fused": 8 * (9 + 9 + 81), "materialised": 8 * (9 + 81 + 729) + 8 * 90},
+            "max_rel_diff_G": rel(G, Gu), "max_rel_diff_K": rel(K, Ku.reshape(n, 81))}
 
 
 def adjoint_vs_materialised(lib, args, dev):
@@ -539,8 +613,11 @@ def run_ours(args, rank, world, local):
     if rank == 0 and not args.no_mixed:
         out["mixed"] = mixed_vs_fp64(lib, args, dev, hbm)
         out["mixed_gmf"] = mixed_gmf_vs_fp64(lib, args, dev, hbm)
+    if rank == 0 and args.mixed_sweep:
+        out["mixed_sweep"] = mixed_sweep(lib, args, dev, hbm)
     if rank == 0 and not args.no_adjoint:
         out["adjoint"] = adjoint_vs_materialised(lib, args, dev)
+        out["tangent"] = tangent_vs_materialised(lib, args, dev)
     if rank == 0 and not args.no_batched:
         out["batched"] = batched_c3(lib, args, dev)
     if rank == 0 and not args.no_cpu:
@@ -574,6 +651,7 @@ def main():
     ap.add_argument("--mixed-n", type=int, default=1 << 24)
     ap.add_argument("--mixed-steps", type=int, default=5)
     ap.add_argument("--gmf-mixed-n", type=int, default=1 << 20)
+    ap.add_argument("--mixed-sweep", action="store_true", help="also the C2 workload over every kind and order")
     args = ap.parse_args()
     args.alpha = 0.5 if args.kind == "sqrt" else 0.0
     if args.kind == "sqrt":

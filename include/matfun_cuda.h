@@ -77,6 +77,17 @@ int smf_cuda_adjoint_f32(int kind, double alpha, int64_t n, const float *A, cons
 int gmf_cuda_adjoint_f32(int kind, double alpha, int64_t n, const float *A, const float *W, const float *V, float *F,
                          float *Abar, float *JV, float *HWV, void *stream);
 
+/* Tangent of psi(A) = |f(A)|^2 / 2 (no counterpart in the reference; the consumer-side contraction of the
+ * reference's theory.md:190, e.g. the Hencky-type potential |log A|^2 / 2 of a Newton method), general family, FP64,
+ * matrix layout, without forming J or H:
+ *   F = f(A)                      (n, 3, 3), optional
+ *   G = J^T F                     (n, 3, 3), optional: G_cd = sum_ab F_ab dF_ab/dA_cd, the gradient of psi
+ *   K = J^T J + F : H             (n, 9, 9): K_{cd,ef} = sum_ab (dF_ab/dA_cd dF_ab/dA_ef + F_ab d2F_ab/dA_cd dA_ef),
+ *                                 the Hessian of psi (symmetric)
+ * Returns 0, -1 (invalid kind / alpha, n < 0, A or K missing for n > 0), -2 (CUDA error).  Asynchronous on
+ * `stream`; allocates nothing (the batch order's scratch lies in K's last rows, evaluated afterwards). */
+int gmf_cuda_tangent(int kind, double alpha, int64_t n, const double *A, double *F, double *G, double *K, void *stream);
+
 /* Batched evaluation (no counterpart in the reference): many requests of uneven size and
  * mixed family / kind / order / precision in ONE launch of a persistent kernel.  A request: */
 typedef struct mf_request {

@@ -32,6 +32,7 @@ SIGNATURES = {
     "gmf_cuda_adjoint": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [ctypes.c_void_p] * 8),
     "smf_cuda_adjoint_f32": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [ctypes.c_void_p] * 8),
     "gmf_cuda_adjoint_f32": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [ctypes.c_void_p] * 8),
+    "gmf_cuda_tangent": (ctypes.c_int, _EVAL),
     "smf_cuda_eval_host": (ctypes.c_int, _EVAL[:-1]),
     "smf_cuda_eval_matrix_host": (ctypes.c_int, _EVAL[:-1]),
     "gmf_cuda_eval_host": (ctypes.c_int, _EVAL[:-1]),

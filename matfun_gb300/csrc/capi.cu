@@ -75,6 +75,24 @@ extern "C" int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A,
   return mf::eval_f64(2, kind, alpha, n, A, F, J, H, (cudaStream_t)stream, nullptr);
 }
 
+extern "C" int gmf_cuda_tangent(int kind, double alpha, int64_t n, const double *A, double *F, double *G, double *K,
+                                void *stream) {
+  if (kind < SMF_EXP || kind > SMF_SQRT || n < 0 || (kind == SMF_POW && !(alpha > 0))) return -1;
+  if (n > 0 && (!A || !K)) return -1;
+  if (kind == SMF_SQRT) kind = SMF_POW, alpha = 0.5;
+  if (kind != SMF_POW) alpha = 0.0;
+  if (n == 0) return 0;
+  if (n > GMF_MAX_N) return -2;
+  const cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  switch (kind) {
+    case SMF_EXP: e = mf::gmf_tangent_launch_exp(alpha, n, A, F, G, K, st); break;
+    case SMF_LOG: e = mf::gmf_tangent_launch_log(alpha, n, A, F, G, K, st); break;
+    default: e = mf::gmf_tangent_launch_pow(alpha, n, A, F, G, K, st); break;
+  }
+  return e == cudaSuccess ? 0 : -2;
+}
+
 namespace {
 int smf_call_f32(int kind, double alpha, int64_t n, const float *x, bool mat, float *F, float *J, float *H,
                  void *stream) {

@@ -61,6 +61,91 @@ MF_D unsigned short hmap_entry(int w) {
   return (unsigned short)(sym3(x1, y1, z1) | (sym3(x2, y2, z2) << 8));
 }
 
+// the tangent of psi(A) = |f(A)|^2 / 2 for one matrix, by the 32 lanes of a warp from its record rc (r1, r2, D2', D3'
+// and the factors sc1, sc2 left to apply) and F = f(A): the gradient G = J^T F (9) and the tangent K = J^T J + F : H
+// (81, symmetric), with J and H never formed.  With L_m = sum_n D2'_mn r_n (the Y2 of the J assembly),
+// J_{ab,cd} = sc1 sum_m (r_m)_ac (L_m)_db and H as in the J / H assembly:
+//   G_cd       = sc1 sum_m (r_m^T F L_m^T)_cd
+//   (J^T J)_{cd,ef} = sc1^2 sum_mk (r_m^T r_k)_ce (L_m L_k^T)_df
+//   (F : H)_{cd,ef} = sc2 sum_q ((r_q)_de N_q,cf + (r_q)_fc N_q,ed),  N_q = sum_mp D3'_mqp r_m^T F r_p^T
+// wk: 351 doubles of the warp's work area; G, K: this matrix's rows of the outputs (G may be null)
+MF_D double gmf_rm(const double *r1, const double *r2, int m, int x) {
+  return m == 0 ? (x % 4 == 0 ? 1.0 : 0.0) : (m == 1 ? r1[x] : r2[x]);
+}
+
+MF_D void gmf_tangent_warp(const double *rc, const double *Fm, double *wk, int lane, double *G, double *K) {
+  const double *r1 = rc, *r2 = rc + 9, *d3 = rc + 24;
+  const double sc1 = rc[34], sc2 = rc[35];
+  double *L = wk, *P = wk + 27, *Q = P + 81, *FR = Q + 81, *M = FR + 27, *N = M + 81, *FL = N + 27;
+  if (lane < 27) {  // L_m[y] at 3 y + m; FR_p[af] = (F r_p^T)_af
+    const int y = lane / 3, m = lane % 3;
+    const int i0 = m == 0 ? 0 : (m == 1 ? 3 : 4), i1 = m == 0 ? 3 : (m == 1 ? 1 : 5), i2 = m == 0 ? 4 : (m == 1 ? 5 : 2);
+    L[lane] = (y % 4 == 0 ? rc[18 + i0] : 0.0) + rc[18 + i1] * r1[y] + rc[18 + i2] * r2[y];
+    const int p = lane / 9, a = (lane % 9) / 3, f = lane % 3;
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) s += Fm[3 * a + k] * gmf_rm(r1, r2, p, 3 * f + k);
+    FR[lane] = s;
+  }
+  __syncwarp();
+  for (int t = lane; t < 81; t += 32) {  // P, Q, M by (m k | m p) * 9 + (c e | d f | c f)
+    const int m = t / 27, k = (t / 9) % 3, u = (t % 9) / 3, v = t % 3;
+    double sp = 0.0, sq = 0.0, sm = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const double rma = gmf_rm(r1, r2, m, 3 * a + u);
+      sp += rma * gmf_rm(r1, r2, k, 3 * a + v);
+      sq += L[3 * (3 * u + a) + m] * L[3 * (3 * v + a) + k];
+      sm += rma * FR[9 * k + 3 * a + v];
+    }
+    P[t] = sp;
+    Q[t] = sq;
+    M[t] = sm;
+  }
+  if (lane < 27) {  // FL_m[ad] = (F L_m^T)_ad
+    const int m = lane / 9, a = (lane % 9) / 3, d = lane % 3;
+    double s = 0.0;
+#pragma unroll
+    for (int b = 0; b < 3; b++) s += Fm[3 * a + b] * L[3 * (3 * d + b) + m];
+    FL[lane] = s;
+  }
+  __syncwarp();
+  if (lane < 27) {  // N_q[cf] = sum_mp D3'_mqp M_mp[cf]
+    const int q = lane / 9, cf = lane % 9;
+    double s = 0.0;
+#pragma unroll
+    for (int m = 0; m < 3; m++)
+#pragma unroll
+      for (int p = 0; p < 3; p++) {
+        int i0 = m, i1 = q, i2 = p;
+        sort3(i0, i1, i2);
+        s += d3[sym3(i0, i1, i2)] * M[9 * (3 * m + p) + cf];
+      }
+    N[lane] = s;
+  }
+  __syncwarp();
+  for (int w = lane; w < 81; w += 32) {  // K[(3c + d) * 9 + 3e + f]
+    const int c = w / 27, d = (w / 9) % 3, e = (w / 3) % 3, f = w % 3;
+    double k1 = 0.0, k2 = 0.0;
+#pragma unroll
+    for (int mk = 0; mk < 9; mk++) k1 += P[9 * mk + 3 * c + e] * Q[9 * mk + 3 * d + f];
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+      k2 += gmf_rm(r1, r2, q, 3 * d + e) * N[9 * q + 3 * c + f] + gmf_rm(r1, r2, q, 3 * f + c) * N[9 * q + 3 * e + d];
+    K[w] = (sc1 == 1.0 ? k1 : sc1 * sc1 * k1) + (sc2 == 1.0 ? k2 : sc2 * k2);
+  }
+  if (G && lane < 9) {
+    const int c = lane / 3, d = lane % 3;
+    double s = 0.0;
+#pragma unroll
+    for (int m = 0; m < 3; m++)
+#pragma unroll
+      for (int a = 0; a < 3; a++) s += gmf_rm(r1, r2, m, 3 * a + c) * FL[9 * m + 3 * a + d];
+    G[lane] = sc1 == 1.0 ? s : sc1 * s;
+  }
+  __syncwarp();
+}
+
 // one tile: matrices base .. base + cnt - 1 by a CTA of GMF_TPB threads (the standalone kernel and the batched
 // persistent kernel run the same code).  T is the type of the arrays in HBM and of phase B: double for the FP64
 // path; float for the mixed-precision path, where phase A (spectral analysis, series, residues: the FP64 steps of
@@ -79,7 +164,9 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
     S.x[e] = (double)A[g * 9 + (e - 9 * p)];
     if (e == 9 * p) S.gidx[p] = g;
   }
-  if (ORDER >= 2) {  // index tables of phase B
+  static_assert(ORDER < 3 || sizeof(T) == 8, "the tangent form is FP64");
+  constexpr int OD = ORDER == 3 ? 2 : ORDER;  // the order of the derivatives the record holds
+  if (ORDER == 2) {  // index tables of phase B
     for (int t = tid; t < 405; t += GMF_TPB) {  // t = 45 (ab) + sym2(cd, ef), cd <= ef
       const int p = t % 45;
       int ef = 0;
@@ -153,7 +240,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
 #pragma unroll
       for (int i = 0; i < 3; i++) x[i] = cmk(xs[2 * i], xs[2 * i + 1]);
       GmfState St;
-      gmf_classify_from<KIND, ORDER>(a, x, C, St);
+      gmf_classify_from<KIND, OD>(a, x, C, St);
       S.state[mi] = St;
       const unsigned cls = St.K == 0 ? 0u : ((St.flags & 1024) ? 1u : 2u);
       key2 = (cls << 16) | ((unsigned)(255 - St.K) << 6) | (unsigned)((St.flags >> 3) & 63);
@@ -177,10 +264,16 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   const int mine = S.perm[tid];
   if (mine < cnt) {
     GmfRec R;
-    gmf_finish<KIND, ORDER, sizeof(T) == 4>(S.state[mine], C, R);
+    gmf_finish<KIND, OD, sizeof(T) == 4>(S.state[mine], C, R);
+    if (F) {
 #pragma unroll
-    for (int k = 0; k < 9; k++) F[S.gidx[mine] * 9 + k] = (T)R.F[k];
-    if (ORDER >= 1) {
+      for (int k = 0; k < 9; k++) F[S.gidx[mine] * 9 + k] = (T)R.F[k];
+    }
+    if (ORDER == 3) {  // the tangent contracts with F: F stays in the matrix's input slot
+#pragma unroll
+      for (int k = 0; k < 9; k++) S.x[mine * 9 + k] = R.F[k];
+    }
+    if (OD >= 1) {
       // the scale factors sc1 / sc2 are folded into D2' / D3' when finite and nonzero; otherwise each output entry
       // is multiplied by them (keeping the reference's NaN / Inf); rc[34] / rc[35] hold the factor left to apply
       T *rc = reinterpret_cast<T *>(S.rec) + tid * GMF_REC;
@@ -191,7 +284,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
 #pragma unroll
       for (int k = 0; k < 6; k++) rc[18 + k] = (T)(R.D2[k] * s1);
       rc[34] = (T)sel(f1, 1.0, R.sc1);
-      if (ORDER >= 2) {
+      if (OD >= 2) {
         const bool f2 = isfinite(R.sc2) & (R.sc2 != 0.0);
         const double s2 = sel(f2, R.sc2, 1.0);
 #pragma unroll
@@ -211,6 +304,11 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
     if (mi >= cnt) break;  // the padding slots sort last
     const T *rc = reinterpret_cast<const T *>(S.rec) + sl * GMF_REC;
     const T *r1 = rc, *r2 = rc + 9;
+    if constexpr (ORDER == 3) {
+      gmf_tangent_warp(rc, reinterpret_cast<const T *>(S.x) + mi * 9, wk, lane, J ? J + S.gidx[mi] * 9 : nullptr,
+                       H + S.gidx[mi] * 81);
+      continue;
+    }
     {
       const T sc1 = rc[34];
       if (lane < 27) {  // Y2[y][m] = sum_n D2'_mn r_n[y]
@@ -417,8 +515,8 @@ cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const T 
 // last n - nm (whose share of the largest output array held the scratch)
 template <int KIND, int ORDER, typename T>
 cudaError_t gmf_launch_sorted(cudaStream_t st, int64_t n, const T *A, T *F, T *J, T *H, const GmfCoef &C) {
-  T *big = ORDER == 2 ? H : J;
-  const int64_t per = ORDER == 2 ? 729 : 81;  // elements of the largest output per matrix
+  T *big = ORDER >= 2 ? H : J;
+  const int64_t per = ORDER == 2 ? 729 : 81;  // elements of the largest output per matrix (ORDER 3: the tangent K)
   const int64_t nblk_n = (n + GKEY_TPB - 1) / GKEY_TPB;
   // order, counts, totals, keys (bytes) and, for order 2, the roots (48 bytes per matrix; the tail stays ~1 % of the
   // batch)
@@ -443,8 +541,13 @@ cudaError_t gmf_launch_sorted(cudaStream_t st, int64_t n, const T *A, T *F, T *J
   e = gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((nm + GMF_TPB - 1) / GMF_TPB), nm, A, F, J, H, C, order, roots,
                                      roots ? keys : nullptr);
   if (e != cudaSuccess) return e;
-  return gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((tail + GMF_TPB - 1) / GMF_TPB), tail, A + nm * 9, F + nm * 9,
-                                        J + nm * 81, ORDER == 2 ? H + nm * 729 : nullptr, C);
+  // the tail's rows of the outputs: F (9 per matrix; optional for ORDER 3), J (81) and H (729) for orders 1, 2,
+  // G (9, optional) and K (81) for the tangent
+  T *Ft = F ? F + nm * 9 : nullptr;
+  T *Jt = ORDER == 3 ? (J ? J + nm * 9 : nullptr) : J + nm * 81;
+  T *Ht = ORDER == 3 ? H + nm * 81 : (ORDER == 2 ? H + nm * 729 : nullptr);
+  return gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((tail + GMF_TPB - 1) / GMF_TPB), tail, A + nm * 9, Ft, Jt, Ht,
+                                        C);
 }
 
 constexpr int64_t GMF_SORT_MIN = 1 << 15;  // below this the reordering does not pay for its launches
@@ -459,6 +562,16 @@ cudaError_t gmf_launch_kind(int order, cudaStream_t st, unsigned blocks, int64_t
   if (order == 1) return sorted ? gmf_launch_sorted<KIND, 1, T>(st, n, A, F, J, H, C)
                                 : gmf_launch_one<KIND, 1, T>(st, blocks, n, A, F, J, H, C);
   return gmf_launch_one<KIND, 0, T>(st, blocks, n, A, F, J, H, C);
+}
+
+// the tangent form (ORDER 3): F (optional), G = J^T F (optional), K = J^T J + F : H of a batch, in the order of the
+// batch-wide sort like the order-2 evaluation (without the reuse of the roots, whose scratch would not fit K's tail)
+template <int KIND>
+cudaError_t gmf_launch_tangent_kind(cudaStream_t st, int64_t n, const double *A, double *F, double *G, double *K,
+                                    const GmfCoef &C) {
+  const bool sorted = (KIND != EXP) & (n >= GMF_SORT_MIN) & (n <= INT_MAX);
+  return sorted ? gmf_launch_sorted<KIND, 3, double>(st, n, A, F, G, K, C)
+                : gmf_launch_one<KIND, 3, double>(st, (unsigned)((n + GMF_TPB - 1) / GMF_TPB), n, A, F, G, K, C);
 }
 
 // host: launch constants (series coefficients gmf_kernel.hpp:48-53; the binomial factors of the term bound by the
@@ -497,6 +610,13 @@ cudaError_t gmf_launch_t(double al, int64_t n, const T *A, T *F, T *J, T *H, cud
   gmf_coef(KIND, al, order, C);
   const unsigned blocks = (unsigned)((n + GMF_TPB - 1) / GMF_TPB);
   return gmf_launch_kind<KIND, T>(order, st, blocks, n, A, F, J, H, C, reorder);
+}
+
+template <int KIND>
+cudaError_t gmf_tangent_t(double al, int64_t n, const double *A, double *F, double *G, double *K, cudaStream_t st) {
+  GmfCoef C;
+  gmf_coef(KIND, al, 2, C);
+  return gmf_launch_tangent_kind<KIND>(st, n, A, F, G, K, C);
 }
 
 }  // namespace mf

@@ -6,4 +6,8 @@ cudaError_t gmf_launch_pow(double al, int64_t n, const double *A, double *F, dou
                             cudaStream_t st, bool reorder) {
   return gmf_launch_t<POW>(al, n, A, F, J, H, st, reorder);
 }
+cudaError_t gmf_tangent_launch_pow(double al, int64_t n, const double *A, double *F, double *G, double *K,
+                                  cudaStream_t st) {
+  return gmf_tangent_t<POW>(al, n, A, F, G, K, st);
+}
 }  // namespace mf

@@ -22,6 +22,14 @@ MF_GMF_DECL(exp)
 MF_GMF_DECL(log)
 MF_GMF_DECL(pow)
 #undef MF_GMF_DECL
+// the tangent of |f(A)|^2 / 2 (F, G = J^T F, K = J^T J + F : H; F and G may be null), general family, FP64
+#define MF_GMFT_DECL(k)                                                                                         \
+  cudaError_t gmf_tangent_launch_##k(double al, int64_t n, const double *A, double *F, double *G, double *K, \
+                                     cudaStream_t st);
+MF_GMFT_DECL(exp)
+MF_GMFT_DECL(log)
+MF_GMFT_DECL(pow)
+#undef MF_GMFT_DECL
 // mixed precision (FP32 storage, FP32 bulk arithmetic, FP64 deviator and Rayleigh quotients), symmetric family
 #define MF_SMFX_DECL(k)                                                                                            \
   cudaError_t smf_mixed_launch_##k(double al, int64_t n, const float *x, bool mat, float *F, float *J, float *H, \

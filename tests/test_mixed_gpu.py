@@ -137,3 +137,43 @@ def test_smf_mixed_nonfinite_inputs_give_nan():
         good = np.ones(len(X), bool)
         good[[3, 7, 9]] = False
         assert not np.isnan(g[good]).any()
+
+
+def run_f32_any(fam, kind, alpha, X32):
+    """F, J, H of the FP32 entry point of fam ("smf": smf_cuda_eval_f32 on Voigt vectors, "gmf": gmf_cuda_eval_f32)"""
+    import torch
+
+    import matfun_gb300
+    lib = matfun_gb300.load()
+    nf = 6 if fam == "smf" else 9
+    n = len(X32)
+    dX = torch.from_numpy(np.ascontiguousarray(X32, dtype=np.float32)).cuda()
+    out = [torch.full((n, nf ** (k + 1)), 7.0, dtype=torch.float32, device="cuda") for k in range(3)]
+    fn = lib.smf_cuda_eval_f32 if fam == "smf" else lib.gmf_cuda_eval_f32
+    r = fn(kind, alpha, n, dX.data_ptr(), *[t.data_ptr() for t in out], None)
+    torch.cuda.synchronize()
+    assert r == 0
+    return [t.cpu().numpy().astype(np.float64) for t in out]
+
+
+@pytest.mark.parametrize("fam", ["smf", "gmf"])
+def test_golden_f32(fam):
+    """the FP32 golden cases (tests/golden/make_golden_f32.py): the reference's golden inputs rounded to FP32, the
+    FP64 oracle's results for those inputs, the FP32 path's per-kind error statement as the per-case tolerance"""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"cases_{fam}_f32.npz"))
+    worst = {}
+    for kind in np.unique(g["kind"]):
+        for alpha in np.unique(g["alpha"][g["kind"] == kind]):
+            sel = np.where((g["kind"] == kind) & (g["alpha"] == alpha))[0]
+            F, J, H = run_f32_any(fam, int(kind), float(alpha), g["x"][sel])
+            for row, i in enumerate(sel):
+                for got, name in ((F, "F"), (J, "J"), (H, "H")):
+                    ref = g[name][i]
+                    assert np.array_equal(np.isnan(got[row]), np.isnan(ref)), f"{fam} case {i} {name}: NaN positions"
+                    e = maxrel(got[row], ref)
+                    key = (int(kind), float(alpha), name)
+                    worst[key] = max(worst.get(key, 0.0), e / g["tol"][i])
+    print(f"FP32 golden {fam}, worst error / tolerance: " +
+          ", ".join(f"k{k} a{a} {n} {e:.2f}" for (k, a, n), e in sorted(worst.items())))
+    assert max(worst.values()) <= 1.0
