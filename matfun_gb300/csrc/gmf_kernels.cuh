@@ -124,15 +124,20 @@ MF_D void gmf_tangent_warp(const double *rc, const double *Fm, double *wk, int l
     N[lane] = s;
   }
   __syncwarp();
-  for (int w = lane; w < 81; w += 32) {  // K[(3c + d) * 9 + 3e + f]
-    const int c = w / 27, d = (w / 9) % 3, e = (w / 3) % 3, f = w % 3;
+  for (int t = lane; t < 45; t += 32) {  // K[9 x + y] = K[9 y + x], x = 3c + d <= y = 3e + f (K is symmetric)
+    int y = 0;
+    while (sym2(0, y + 1) <= t) y++;
+    const int x = t - sym2(0, y);
+    const int c = x / 3, d = x % 3, e = y / 3, f = y % 3;
     double k1 = 0.0, k2 = 0.0;
 #pragma unroll
     for (int mk = 0; mk < 9; mk++) k1 += P[9 * mk + 3 * c + e] * Q[9 * mk + 3 * d + f];
 #pragma unroll
     for (int q = 0; q < 3; q++)
       k2 += gmf_rm(r1, r2, q, 3 * d + e) * N[9 * q + 3 * c + f] + gmf_rm(r1, r2, q, 3 * f + c) * N[9 * q + 3 * e + d];
-    K[w] = (sc1 == 1.0 ? k1 : sc1 * sc1 * k1) + (sc2 == 1.0 ? k2 : sc2 * k2);
+    const double v = (sc1 == 1.0 ? k1 : sc1 * sc1 * k1) + (sc2 == 1.0 ? k2 : sc2 * k2);
+    K[9 * x + y] = v;
+    K[9 * y + x] = v;
   }
   if (G && lane < 9) {
     const int c = lane / 3, d = lane % 3;
