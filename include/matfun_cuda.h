@@ -101,9 +101,11 @@ typedef struct mf_request {
   void *F, *J, *H; /* device outputs (J for order >= 1, H for order 2) */
 } mf_request;
 
-/* All requests queued on `stream` as one launch (the request table is uploaded on `stream` first).  Returns 0, -1 when
- * a request breaks the rules of its single entry point (then nothing runs), -2 for a CUDA error.  Results equal those
- * of the single entry points. */
+/* All requests queued on `stream` as one launch of the persistent kernel (the request table is uploaded on `stream`
+ * first; gmf requests of log / pow at orders 1-2 with >= 2048 matrices are first ordered by spectral class, three
+ * small kernels each, as the single gmf entry point orders large batches).  Returns 0, -1 when a request breaks the
+ * rules of its single entry point (then nothing runs), -2 for a CUDA error.  Results equal those of the single entry
+ * points to rounding (1e-13 relative, FP64). */
 int matfun_cuda_batched(const mf_request *requests, int count, void *stream);
 /* The same as a plan: the table is validated and uploaded once (synchronously); matfun_cuda_batched_run then only
  * clears the tile cursor and launches, so it can be captured in a CUDA graph and replayed.  The arrays the requests

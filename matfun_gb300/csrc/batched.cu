@@ -9,12 +9,16 @@
 //
 // Two ways to run it:
 //   matfun_cuda_batched(requests, count, stream)          table in a per-device cached buffer, uploaded on `stream`
+// gmf requests of log / pow at orders 1, 2 with at least BT_SORT_MIN matrices are evaluated in the batch order of the
+// standalone launch (by spectral class): their permutations are computed on the stream before the persistent kernel,
+// into an order region after the table (in the cached buffer, or in the plan's allocation).
 //   matfun_cuda_batched_plan / _run / _free                 table uploaded once; _run only clears the cursor and
 //                                                           launches, so it can be captured in a CUDA graph
 // The CTAs per SM and the order in which requests are laid out (as given, or longest tile work first) come from
 // matfun_cuda_batched_tune (set by the autotuner of matfun_gb300/autotune.py).
 #include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -104,13 +108,31 @@ struct Tuning {
 };
 Tuning g_tune;
 
+// a gmf request whose matrices are evaluated in the batch order of the standalone launch (log, pow; orders 1, 2;
+// at least BT_SORT_MIN matrices): its permutation, block histograms, their totals and keys lie at `off` of the order
+// region that follows the table and the cursor
+struct Ord {
+  int req, kind, dtype;
+  long long n;
+  const void *x;
+  size_t off;
+};
+constexpr long long BT_SORT_MIN = 2048;
+
 struct Table {                  // a validated request list laid out for the device
   std::vector<unsigned char> bytes;  // DevReq[count] | tile_start[count + 1] | coefficient blocks
   size_t off_tiles = 0, off_coef = 0;
   int count = 0;
+  std::vector<Ord> ords;
+  size_t ord_bytes = 0;
 };
 
 size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+long long key_blocks(long long n) { return (n + GKEY_TPB - 1) / GKEY_TPB; }
+// order (4 n) | counts (4 GKEY_BINS blocks) | totals (4 GKEY_BINS) | keys (n bytes)
+size_t ord_size(long long n) {
+  return align16(4 * (size_t)n) + 4 * (size_t)GKEY_BINS * key_blocks(n) + 4 * (size_t)GKEY_BINS + align16((size_t)n);
+}
 
 // -1: invalid request (the rules of the single entry points), 0: ok
 int build_table(const mf_request *req, int count, Table &T) {
@@ -138,7 +160,7 @@ int build_table(const mf_request *req, int count, Table &T) {
     if (kind != SMF_POW) al = kind == SMF_SQRT ? 0.5 : 0.0;
     Item it;
     it.d = DevReq{r.family, kind, r.order, r.dtype, al, (long long)r.n, r.x, r.F, r.order >= 1 ? r.J : nullptr,
-                  r.order >= 2 ? r.H : nullptr, 0};
+                  r.order >= 2 ? r.H : nullptr, 0, nullptr};
     if (r.family == 2) {
       GmfCoef C;
       gmf_coef(kind, al, r.order, C);
@@ -181,7 +203,49 @@ int build_table(const mf_request *req, int count, Table &T) {
     co += align16(items[i].coef.size());
   }
   std::memcpy(T.bytes.data() + T.off_tiles + sizeof(long long) * T.count, &tiles, sizeof tiles);
+  for (int i = 0; i < T.count; i++) {
+    const DevReq &d = items[i].d;
+    if ((d.family == 2) & (d.kind != SMF_EXP) & (d.order >= 1) & (d.n >= BT_SORT_MIN) & (d.n <= INT_MAX)) {
+      T.ords.push_back(Ord{i, d.kind, d.dtype, d.n, d.x, T.ord_bytes});
+      T.ord_bytes += ord_size(d.n);
+    }
+  }
   return 0;
+}
+
+// the device address of each ordered request's permutation, written into its DevReq before the table is uploaded
+void patch_idx(Table &T, unsigned char *ord_base) {
+  for (const Ord &o : T.ords) {
+    const int *idx = reinterpret_cast<const int *>(ord_base + o.off);
+    std::memcpy(T.bytes.data() + sizeof(DevReq) * o.req + offsetof(DevReq, idx), &idx, sizeof idx);
+  }
+}
+
+template <int KIND, typename T>
+void launch_order(const Ord &o, unsigned char *ord_base, cudaStream_t st) {
+  const int n = (int)o.n, nblk = (int)key_blocks(o.n);
+  int *order = reinterpret_cast<int *>(ord_base + o.off);
+  int *counts = reinterpret_cast<int *>(ord_base + o.off + align16(4 * (size_t)n));
+  int *totals = counts + (size_t)GKEY_BINS * nblk;
+  unsigned char *keys = reinterpret_cast<unsigned char *>(totals + GKEY_BINS);
+  gmf_key_kernel<KIND, T><<<nblk, GKEY_TPB, 0, st>>>(n, static_cast<const T *>(o.x), keys, counts, nblk, nullptr);
+  gmf_scan_kernel<<<GKEY_BINS, 1024, 0, st>>>(counts, nblk, totals);
+  gmf_scatter_kernel<<<nblk, GKEY_TPB, 0, st>>>(n, keys, counts, totals, nblk, order);
+}
+
+// the permutations of the ordered requests (key, scan and scatter kernels of gmf_kernels.cuh), queued on `st` before
+// the persistent kernel that reads them
+cudaError_t launch_orders(const Table &T, unsigned char *ord_base, cudaStream_t st) {
+  for (const Ord &o : T.ords) {
+    if (o.dtype == 0) {
+      if (o.kind == SMF_LOG) launch_order<LOG, double>(o, ord_base, st);
+      else launch_order<POW, double>(o, ord_base, st);
+    } else {
+      if (o.kind == SMF_LOG) launch_order<LOG, float>(o, ord_base, st);
+      else launch_order<POW, float>(o, ord_base, st);
+    }
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t prepare_kernel() {
@@ -238,7 +302,8 @@ extern "C" int matfun_cuda_batched(const mf_request *requests, int count, void *
   Scratch &S = g_scratch[dev];
   std::lock_guard<std::mutex> lock(S.mu);
   const cudaStream_t st = (cudaStream_t)stream;
-  const size_t need = align16(T.bytes.size()) + sizeof(unsigned long long);
+  const size_t ord_at = align16(T.bytes.size()) + 16;  // order region after the table and the cursor
+  const size_t need = ord_at + T.ord_bytes;
   if (S.size < need) {
     if (S.dev) {
       if (S.last) cudaEventSynchronize(S.last);
@@ -252,8 +317,10 @@ extern "C" int matfun_cuda_batched(const mf_request *requests, int count, void *
   if (!S.last && cudaEventCreateWithFlags(&S.last, cudaEventDisableTiming) != cudaSuccess) return -2;
   // the previous launch on another stream may still read the buffer: order this upload after it
   if (cudaStreamWaitEvent(st, S.last, 0) != cudaSuccess) return -2;
+  patch_idx(T, S.dev + ord_at);
   // (a copy from pageable memory is staged before the call returns, so the host table may go out of scope)
   cudaError_t e = cudaMemcpyAsync(S.dev, T.bytes.data(), T.bytes.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = launch_orders(T, S.dev + ord_at, st);
   if (e == cudaSuccess)
     e = launch_table(S.dev, T, (unsigned long long *)(S.dev + align16(T.bytes.size())), st);
   if (e == cudaSuccess) e = cudaEventRecord(S.last, st);
@@ -269,7 +336,10 @@ extern "C" int matfun_cuda_batched_plan(const mf_request *requests, int count, v
     return -1;
   }
   P->cursor_off = align16(P->table.bytes.size());
-  if (cudaMalloc(&P->dev, P->cursor_off + sizeof(unsigned long long)) != cudaSuccess ||
+  const size_t ord_at = P->cursor_off + 16;
+  const bool ok = cudaMalloc(&P->dev, ord_at + P->table.ord_bytes) == cudaSuccess;
+  if (ok) patch_idx(P->table, P->dev + ord_at);
+  if (!ok ||
       cudaMemcpy(P->dev, P->table.bytes.data(), P->table.bytes.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
     if (P->dev) cudaFree(P->dev);
     delete P;
@@ -282,8 +352,9 @@ extern "C" int matfun_cuda_batched_plan(const mf_request *requests, int count, v
 extern "C" int matfun_cuda_batched_run(void *plan, void *stream) {
   Plan *P = (Plan *)plan;
   if (!P) return -1;
-  const cudaError_t e = launch_table(P->dev, P->table, (unsigned long long *)(P->dev + P->cursor_off),
-                                     (cudaStream_t)stream);
+  cudaError_t e = launch_orders(P->table, P->dev + P->cursor_off + 16, (cudaStream_t)stream);
+  if (e == cudaSuccess)
+    e = launch_table(P->dev, P->table, (unsigned long long *)(P->dev + P->cursor_off), (cudaStream_t)stream);
   return e == cudaSuccess ? 0 : -2;
 }
 
@@ -308,7 +379,8 @@ extern "C" int matfun_cuda_batched_tune(int ctas_per_sm, int longest_first) {
 // plugin that is only handed device arrays.  matfun_cuda_batched caches a table buffer it allocates with cudaMalloc;
 // this entry point instead writes the request table and the tile cursor into one fixed array of device memory that
 // is part of the library image (NOALLOC_BYTES, loaded with the library on every GPU that uses it and held until the
-// process exits).  It calls no cudaMalloc, cudaFree or other device-allocating routine.
+// process exits).  It calls no cudaMalloc, cudaFree or other device-allocating routine.  Having no room for the
+// permutations, it evaluates gmf requests in their given order.
 namespace {
 constexpr size_t NOALLOC_BYTES = 256 * 1024;  // cursor (16 bytes) + request table: ~100 gmf or ~700 smf requests
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];

@@ -16,6 +16,7 @@ struct DevReq {
   const void *x;
   void *F, *J, *H;
   long long coef_off;  // byte offset of the coefficient block
+  const int *idx;      // gmf: position p of the request holds matrix idx[p] (the batch order by spectral class), or null
 };
 
 template <int ORDER, bool MAT>
