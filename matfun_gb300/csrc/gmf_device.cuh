@@ -26,7 +26,9 @@ struct GmfCoef {
   double bt[G_KMAX];      // series coefficients b_j of f(c (1 + u)) (gmf_kernel.hpp:48-53)
   float lterm[G_KMAX];    // log2(|b_(n+k)| C(k + n, n)), n = 3 (order + 1) - 1: the term bound of gmf_kernel.hpp:73-97
   float bth[G_KMAX], btl[G_KMAX];  // bt as float-float (hi + lo)
-  int ffser;              // 1: the group series may run in float-float (log, pow with every |b_j| <= 2^100)
+  int ffser;              // 1: the group series may run on the FP32 pipe (every |bth[j]| <= 2^100)
+  int tsh;                // bth, btl hold b_j 2^(tsh j) and group_tail takes the offsets times 2^-tsh (exp: 2, so
+                          // that 4^j / j! stays in FP32's range; log, pow: 0)
 };
 
 // the 19 divided differences f[x0^a x1^b x2^c], a >= b >= c, a >= 1, in lexicographic order of (a, b, c); each is
@@ -211,24 +213,36 @@ MF_D double log_b0(double sig, double m, double cxg, double cmu) {
   return near ? log(sig * ms) + 0.5 * log1p(zr * (2.0 + zr)) : log(sig * fabs(cmu));
 }
 
-// the streamed group series (gmf_kernel.hpp:493-519) of the ND divided differences; REAL: every in-group offset
-// and hence every term is real (half the FP64 instructions of the complex recursion)
+// an exact power of two, -1022 <= e <= 1023
+MF_D double pow2i(int e) { return __longlong_as_double((long long)(1023 + e) << 52); }
+// d_c of group_tail: the in-group multiplicity of entry c less one (0 for an entry without in-group nodes)
+MF_D int gdeg(int c, const bool *inG) {
+  const int d = (inG[0] ? gms(c, 0) : 0) + (inG[1] ? gms(c, 1) : 0) + (inG[2] ? gms(c, 2) : 0) - 1;
+  return d < 0 ? 0 : d;
+}
+
 // the terms j1 <= j < K of group_series without a pole node (every entry's coefficient is b_j): float-float up to
-// j2, FP32 from there on (see nterms), added to D at the end; Ep0 is the FP64 recursion state after term j1 - 1
+// j2, FP32 from there on (see nterms), added to D at the end; Ep0 is the FP64 recursion state after term j1 - 1.
+// With tsh > 0 (exp) the tail runs on u~ = u 2^-tsh and b~_j = b_j 2^(tsh j): entry c at step j is homogeneous of
+// degree j - d_c in u (d_c = its in-group multiplicity - 1), so its state enters as Ep0 2^(-tsh (j1 - 1 - d_c)) and
+// its tail sum leaves times 2^(-tsh d_c), all exact powers of two.
 template <int ND, bool REAL>
 MF_D void group_tail(int K, int j1, int j2, const GmfCoef &C, const bool *inG, const cx *u, const cx *Ep0, cx *D) {
   const ffl zero = {0.f, 0.f};
+  const int sh = C.tsh;
+  const double us = pow2i(-sh);
   ffl ur[3], ui[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    ur[i] = ff_of(u[i].re);
-    ui[i] = REAL ? zero : ff_of(u[i].im);
+    ur[i] = ff_of(u[i].re * us);
+    ui[i] = REAL ? zero : ff_of(u[i].im * us);
   }
   ffl Er[ND], Ei[ND], Fr[ND], Fi[ND], Sr[ND], Si[ND];
 #pragma unroll
   for (int c = 0; c < ND; c++) {
-    Er[c] = ff_of(Ep0[c].re);
-    Ei[c] = REAL ? zero : ff_of(Ep0[c].im);
+    const double es = pow2i(-sh * (j1 - 1 - gdeg(c, inG)));
+    Er[c] = ff_of(Ep0[c].re * es);
+    Ei[c] = REAL ? zero : ff_of(Ep0[c].im * es);
     Sr[c] = zero;
     Si[c] = zero;
   }
@@ -299,12 +313,15 @@ MF_D void group_tail(int K, int j1, int j2, const GmfCoef &C, const bool *inG, c
   }
 #pragma unroll
   for (int c = 0; c < ND; c++) {
-    D[c].re = D[c].re + (ff_dbl(Sr[c]) + (double)sr[c]);
-    if (!REAL) D[c].im = D[c].im + (ff_dbl(Si[c]) + (double)si[c]);
+    const double os = pow2i(-sh * gdeg(c, inG));
+    D[c].re = D[c].re + (ff_dbl(Sr[c]) + (double)sr[c]) * os;
+    if (!REAL) D[c].im = D[c].im + (ff_dbl(Si[c]) + (double)si[c]) * os;
   }
 }
 
-// the streamed group series (FP64 terms up to j1, the tail by group_tail; j1 >= K: all in FP64)
+// the streamed group series (gmf_kernel.hpp:493-519) of the ND divided differences; REAL: every in-group offset
+// and hence every term is real (half the FP64 instructions of the complex recursion).  FP64 terms up to j1, the tail
+// by group_tail (j1 >= K: all in FP64)
 template <int ND, bool REAL>
 MF_D void group_series(int K, double b0, const GmfCoef &C, const bool *inG, const bool *pk, const cx *u, double iap,
                        cx *D, int j1 = G_KMAX, int j2 = G_KMAX) {
@@ -692,7 +709,7 @@ MF_D void gmf_classify_from(const double *a, const cx *xr, const GmfCoef &C, Gmf
   int j1, j2;
   St.K = hasg ? nterms(C, 3 * (ORDER + 1) - 1, rr, rq, j1, j2) : 0;
   // the float-float / FP32 tail of the series: log and pow without a pole node, coefficients within FP32's range
-  const bool tail = (KIND != EXP) & (C.ffser != 0) & !(pk[0] | pk[1] | pk[2]) & (rr <= 4.0);
+  const bool tail = (C.ffser != 0) & !(pk[0] | pk[1] | pk[2]) & (rr <= 4.0);
   j1 = tail ? j1 : G_KMAX;
   j2 = tail ? j2 : G_KMAX;
   bool real = (u[0].im == 0) & (u[1].im == 0) & (u[2].im == 0);

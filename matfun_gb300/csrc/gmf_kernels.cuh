@@ -592,12 +592,15 @@ inline void gmf_coef(int kind, double al, int order, GmfCoef &C) {
   C.bt[0] = 1.0;
   for (int j = 1; j < G_KMAX; j++)
     C.bt[j] = kind == EXP ? C.bt[j - 1] / j : (kind == LOG ? (j % 2 ? 1.0 : -1.0) / j : C.bt[j - 1] * (al - j + 1) / j);
-  C.ffser = kind != EXP;
+  C.tsh = kind == EXP ? 2 : 0;
+  C.ffser = 1;
   for (int j = 0; j < G_KMAX; j++) {
-    C.ffser &= std::fabs(C.bt[j]) <= 0x1p100;  // (false for a NaN)
-    C.bth[j] = (float)C.bt[j];
-    C.btl[j] = C.ffser ? (float)(C.bt[j] - (double)C.bth[j]) : 0.f;
+    const double bs = std::ldexp(C.bt[j], C.tsh * j);
+    C.ffser &= std::fabs(bs) <= 0x1p100;  // (false for a NaN)
+    C.bth[j] = (float)bs;
   }
+  for (int j = 0; j < G_KMAX; j++)
+    C.btl[j] = C.ffser ? (float)(std::ldexp(C.bt[j], C.tsh * j) - (double)C.bth[j]) : 0.f;
   const int nn = 3 * (order + 1) - 1;
   double c = 1.0;
   for (int k = 0; k < G_KMAX; k++) {
