@@ -41,8 +41,8 @@ NCU_DRAM_BYTES_PER_MATRIX = (101.44e6 + 1752.03e6) / 259584
 
 def launches_per_call(kind, n):
     """kernels one order-2 gmf_cuda_eval call launches: key, scan, scatter, the ordered launch and the tail launch
-    (log, sqrt, pow with 2^15 <= n <= 2^31 - 1), else one plain launch"""
-    return 5 if kind != "exp" and (1 << 15) <= n <= (1 << 31) - 1 else 1
+    (every kind with 2^15 <= n <= 2^31 - 1), else one plain launch"""
+    return 5 if (1 << 15) <= n <= (1 << 31) - 1 else 1
 
 
 def peaks():

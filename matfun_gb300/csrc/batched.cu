@@ -9,7 +9,8 @@
 //
 // Two ways to run it:
 //   matfun_cuda_batched(requests, count, stream)          table in a per-device cached buffer, uploaded on `stream`
-// gmf requests of log / pow at orders 1, 2 with at least BT_SORT_MIN matrices are evaluated in the batch order of the
+// gmf requests of log / pow at orders 1, 2 (exp at order 2) with at least BT_SORT_MIN matrices are evaluated in the
+// batch order of the
 // standalone launch (by spectral class): their permutations are computed on the stream before the persistent kernel,
 // into an order region after the table (in the cached buffer, or in the plan's allocation).
 //   matfun_cuda_batched_plan / _run / _free                 table uploaded once; _run only clears the cursor and
@@ -108,8 +109,8 @@ struct Tuning {
 };
 Tuning g_tune;
 
-// a gmf request whose matrices are evaluated in the batch order of the standalone launch (log, pow; orders 1, 2;
-// at least BT_SORT_MIN matrices): its permutation, block histograms, their totals and keys lie at `off` of the order
+// a gmf request whose matrices are evaluated in the batch order of the standalone launch (log, pow at orders 1, 2;
+// exp at order 2; at least BT_SORT_MIN matrices): its permutation, block histograms, their totals and keys lie at `off` of the order
 // region that follows the table and the cursor
 struct Ord {
   int req, kind, dtype;
@@ -205,7 +206,8 @@ int build_table(const mf_request *req, int count, Table &T) {
   std::memcpy(T.bytes.data() + T.off_tiles + sizeof(long long) * T.count, &tiles, sizeof tiles);
   for (int i = 0; i < T.count; i++) {
     const DevReq &d = items[i].d;
-    if ((d.family == 2) & (d.kind != SMF_EXP) & (d.order >= 1) & (d.n >= BT_SORT_MIN) & (d.n <= INT_MAX)) {
+    const bool kind_ok = (d.kind != SMF_EXP) | (d.order == 2);  // as the single gmf launch
+    if ((d.family == 2) & kind_ok & (d.order >= 1) & (d.n >= BT_SORT_MIN) & (d.n <= INT_MAX)) {
       T.ords.push_back(Ord{i, d.kind, d.dtype, d.n, d.x, T.ord_bytes});
       T.ord_bytes += ord_size(d.n);
     }
@@ -238,10 +240,12 @@ void launch_order(const Ord &o, unsigned char *ord_base, cudaStream_t st) {
 cudaError_t launch_orders(const Table &T, unsigned char *ord_base, cudaStream_t st) {
   for (const Ord &o : T.ords) {
     if (o.dtype == 0) {
-      if (o.kind == SMF_LOG) launch_order<LOG, double>(o, ord_base, st);
+      if (o.kind == SMF_EXP) launch_order<EXP, double>(o, ord_base, st);
+      else if (o.kind == SMF_LOG) launch_order<LOG, double>(o, ord_base, st);
       else launch_order<POW, double>(o, ord_base, st);
     } else {
-      if (o.kind == SMF_LOG) launch_order<LOG, float>(o, ord_base, st);
+      if (o.kind == SMF_EXP) launch_order<EXP, float>(o, ord_base, st);
+      else if (o.kind == SMF_LOG) launch_order<LOG, float>(o, ord_base, st);
       else launch_order<POW, float>(o, ord_base, st);
     }
   }

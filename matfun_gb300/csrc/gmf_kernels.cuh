@@ -560,8 +560,9 @@ constexpr int64_t GMF_SORT_MIN = 1 << 15;  // below this the reordering does not
 template <int KIND, typename T>
 cudaError_t gmf_launch_kind(int order, cudaStream_t st, unsigned blocks, int64_t n, const T *A, T *F, T *J, T *H,
                             const GmfCoef &C, bool reorder = true) {
-  // log and pow (the branch-cut pair and the wider spread of work); exp does not recover the ~1 ms of the sort
-  const bool sorted = reorder & (KIND != EXP) & (n >= GMF_SORT_MIN) & (n <= INT_MAX);
+  // log and pow (the branch-cut pair and the wider spread of work); exp only at order 2 (measured at n = 2^20:
+  // order 2 10.2 -> 9.6 ms ordered, order 1 4.7 -> 5.0 ms, so order 1 keeps the plain launch)
+  const bool sorted = reorder & ((KIND != EXP) | (order == 2)) & (n >= GMF_SORT_MIN) & (n <= INT_MAX);
   if (order == 2) return sorted ? gmf_launch_sorted<KIND, 2, T>(st, n, A, F, J, H, C)
                                 : gmf_launch_one<KIND, 2, T>(st, blocks, n, A, F, J, H, C);
   if (order == 1) return sorted ? gmf_launch_sorted<KIND, 1, T>(st, n, A, F, J, H, C)
@@ -574,7 +575,7 @@ cudaError_t gmf_launch_kind(int order, cudaStream_t st, unsigned blocks, int64_t
 template <int KIND>
 cudaError_t gmf_launch_tangent_kind(cudaStream_t st, int64_t n, const double *A, double *F, double *G, double *K,
                                     const GmfCoef &C) {
-  const bool sorted = (KIND != EXP) & (n >= GMF_SORT_MIN) & (n <= INT_MAX);
+  const bool sorted = (n >= GMF_SORT_MIN) & (n <= INT_MAX);
   return sorted ? gmf_launch_sorted<KIND, 3, double>(st, n, A, F, G, K, C)
                 : gmf_launch_one<KIND, 3, double>(st, (unsigned)((n + GMF_TPB - 1) / GMF_TPB), n, A, F, G, K, C);
 }
