@@ -159,7 +159,10 @@ void *GmfValueJacHessCuda(void *call_frame);
  *     one to three results (F, J, H), attributes kind, alpha;
  *   SmfAdjointCuda, GmfAdjointCuda (F64) and SmfAdjointF32Cuda, GmfAdjointF32Cuda (F32): arguments A, W, V
  *     ((..., 3, 3); W or V with no elements when not given), attributes kind, alpha and outputs (int64 bit mask:
- *     1 F, 2 J^T W, 4 J V, 8 W.H.V), one result per set bit in that order (smf_cuda_adjoint / gmf_cuda_adjoint). */
+ *     1 F, 2 J^T W, 4 J V, 8 W.H.V), one result per set bit in that order (smf_cuda_adjoint / gmf_cuda_adjoint);
+ *   GmfTangentCuda (F64): argument A, attributes kind, alpha and outputs (1 F, 2 G = J^T F, 4 K = J^T J + F : H;
+ *     K required), one result per set bit in that order, F and G of A's shape, K with 9 times its elements
+ *     (gmf_cuda_tangent). */
 void *SmfValueF32Cuda(void *call_frame);
 void *SmfMatrixValueF32Cuda(void *call_frame);
 void *GmfValueF32Cuda(void *call_frame);
@@ -167,6 +170,7 @@ void *SmfAdjointCuda(void *call_frame);
 void *GmfAdjointCuda(void *call_frame);
 void *SmfAdjointF32Cuda(void *call_frame);
 void *GmfAdjointF32Cuda(void *call_frame);
+void *GmfTangentCuda(void *call_frame);
 
 /* XLA FFI API version the handlers implement, major * 1000 + minor (reference: cuda/src/matfun_cuda.cu:265) */
 int smf_xla_ffi_api_version(void);

@@ -247,6 +247,45 @@ void *handle_adjoint(mfx_call_frame *cf) {
   return launch_error(api, res, cudaPeekAtLastError());
 }
 
+// A -> the selected ones of F = f(A), G = J^T F, K = J^T J + F : H (gmf_cuda_tangent; attribute `outputs`: bit 0 F,
+// bit 1 G, bit 2 K, which is required), results in that order; F and G of A's shape, K of 9 times its elements
+void *handle_tangent(mfx_call_frame *cf) {
+  const mfx_api *api = cf->api;
+  bool done;
+  if (void *r = frame_checks(cf, 1, 3, &done); done) return r;
+  cudaStream_t st;
+  if (void *e = get_stream(cf, &st)) return e;
+  std::string why;
+  const mfx_buffer *A = typed_buffer(cf->args.types[0], cf->args.args[0], MFX_ARG_BUFFER, MFX_DT_F64, "argument", why);
+  const void *kind_p = scalar_attr(cf->attrs, "kind", MFX_DT_S64, why);
+  const void *alpha_p = scalar_attr(cf->attrs, "alpha", MFX_DT_F64, why);
+  const void *outs_p = scalar_attr(cf->attrs, "outputs", MFX_DT_S64, why);
+  if (!why.empty()) return invalid(api, "Failed to decode all FFI handler operands: " + why);
+  const int64_t r = A->rank;
+  if (!(r >= 2 && A->dims[r - 1] == 3 && A->dims[r - 2] == 3))
+    return invalid(api, "matfun: expected matrices of shape (..., 3, 3)");
+  const int64_t cnt = elements(A);
+  const int64_t outs = *static_cast<const int64_t *>(outs_p);
+  if (outs < 4 || outs > 7) return invalid(api, "matfun: outputs must select K and optionally F, G");
+  const int want = 1 + (int)(outs & 1) + (int)((outs >> 1) & 1);
+  if (cf->rets.size != want) return invalid(api, "matfun: one result per selected output expected");
+  double *o[3] = {nullptr, nullptr, nullptr};
+  for (int b = 0, i = 0; b < 3; b++) {
+    if (!((outs >> b) & 1)) continue;
+    const mfx_buffer *rb =
+        typed_buffer(cf->rets.types[i], cf->rets.rets[i], MFX_RET_BUFFER, MFX_DT_F64, "result", why);
+    if (rb == nullptr) return invalid(api, "Failed to decode result " + std::to_string(i) + ": " + why);
+    if (elements(rb) != (b == 2 ? 9 * cnt : cnt)) return invalid(api, "matfun: F and G have A's shape, K 9 times it");
+    o[b] = static_cast<double *>(rb->data);
+    i++;
+  }
+  const int kind = clamp_kind(*static_cast<const int64_t *>(kind_p));
+  const double alpha = *static_cast<const double *>(alpha_p);
+  if (cnt == 0) return nullptr;
+  const int res = gmf_cuda_tangent(kind, alpha, cnt / 9, static_cast<const double *>(A->data), o[0], o[1], o[2], st);
+  return launch_error(api, res, cudaPeekAtLastError());
+}
+
 }  // namespace
 
 #define MF_FFI_HANDLER(name, fam, T) \
@@ -274,5 +313,7 @@ MF_FFI_ADJOINT(SmfAdjointCuda, false, double)
 MF_FFI_ADJOINT(GmfAdjointCuda, true, double)
 MF_FFI_ADJOINT(SmfAdjointF32Cuda, false, float)
 MF_FFI_ADJOINT(GmfAdjointF32Cuda, true, float)
+
+extern "C" void *GmfTangentCuda(void *call_frame) { return handle_tangent(static_cast<mfx_call_frame *>(call_frame)); }
 
 extern "C" int smf_xla_ffi_api_version(void) { return MFX_API_MAJOR * 1000 + MFX_API_MINOR; }

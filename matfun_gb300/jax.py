@@ -13,6 +13,8 @@ f is a jax.custom_vjp whose backward (J^T W) is itself a custom_vjp whose backwa
 (the contraction has no derivative rule), and forward mode (jvp, jacfwd, hessian) is not defined on custom_vjp.  smf
 treats A as symmetric (the derivatives of A -> f((A + A^T) / 2)).  float32 arrays run the FP32 kernels.
 
+gmf_tangent(kind, A) returns F, J^T F and J^T J + F : H of |f(A)|^2 / 2 in one custom call (GmfTangentCuda).
+
 The values F, J, H themselves (order 0, 1, 2) are the reference's own matfun.jax over this library: it binds the
 handlers SmfValueCuda ... GmfValueJacHessCuda that libmatfun_cuda exports (MATFUN_CUDA_LIB).
 """
@@ -29,7 +31,8 @@ OUT_F, OUT_ABAR, OUT_JV, OUT_HWV = 1, 2, 4, 8
 _TARGETS = {("smf", False): ("matfun_gb300_smf_adjoint", "SmfAdjointCuda"),
             ("gmf", False): ("matfun_gb300_gmf_adjoint", "GmfAdjointCuda"),
             ("smf", True): ("matfun_gb300_smf_adjoint_f32", "SmfAdjointF32Cuda"),
-            ("gmf", True): ("matfun_gb300_gmf_adjoint_f32", "GmfAdjointF32Cuda")}
+            ("gmf", True): ("matfun_gb300_gmf_adjoint_f32", "GmfAdjointF32Cuda"),
+            ("tangent", False): ("matfun_gb300_gmf_tangent", "GmfTangentCuda")}
 _state = {"registered": False}
 
 
@@ -119,3 +122,20 @@ def smf(kind, A, alpha=None):
     """f(A) for symmetric 3x3 matrices A (..., 3, 3), twice differentiable in reverse mode by the adjoint kernels"""
     k, a = _norm(kind, alpha)
     return _value("smf", k, a, A)
+
+
+def gmf_tangent(kind, A, alpha=None):
+    """(F, G, K) of psi(A) = |f(A)|^2 / 2 for general float64 matrices A (..., 3, 3): F = f(A), the gradient
+    G = J^T F and the Hessian K = J^T J + F : H (..., 3, 3, 3, 3), one custom call (GmfTangentCuda) that never forms J
+    or H; for f = log the tangent of the Hencky-type potential |log A|^2 / 2 (not differentiable itself)"""
+    k, a = _norm(kind, alpha)
+    _register()
+    if A.shape[-2:] != (3, 3) or A.dtype != jnp.float64:
+        raise TypeError("expected float64 matrices (..., 3, 3) (with jax_enable_x64)")
+    out = [jax.ShapeDtypeStruct(A.shape, A.dtype), jax.ShapeDtypeStruct(A.shape, A.dtype),
+           jax.ShapeDtypeStruct(A.shape[:-2] + (3, 3, 3, 3), A.dtype)]
+    try:
+        call = _ffi().ffi_call(_TARGETS[("tangent", False)][0], out, vmap_method="broadcast_all")
+    except TypeError:  # jax releases before vmap_method
+        call = _ffi().ffi_call(_TARGETS[("tangent", False)][0], out, vectorized=True)
+    return tuple(call(A, kind=np.int64(k), alpha=np.float64(a), outputs=np.int64(7)))

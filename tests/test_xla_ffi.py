@@ -162,3 +162,29 @@ def test_adjoint_frames_checked_before_launch(lib):
         xla = xf.FakeXla()
         cf, keep = xf.frame3(xla, [E, E, E], [E, E], at(1, 0.0, 1 | 8))
         assert call(lib, nm, cf) is None and xla.errors == []
+
+
+def test_tangent_frames_checked_before_launch(lib):
+    """GmfTangentCuda: the argument shape, the output mask (K required), the result count and shapes are checked
+    before anything runs; an empty batch succeeds without a launch"""
+    A = (xf.DT_F64, 16, (4, 3, 3))
+    K = (xf.DT_F64, 16, (4, 3, 3, 3, 3))
+    at = xf.adjoint_attrs
+    cases = [
+        ("no K", [A], at(1, 0.0, 1 | 2), [A, A], "outputs"),
+        ("mask beyond 3 bits", [A], at(1, 0.0, 8 | 4), [K], "outputs"),
+        ("result count", [A], at(1, 0.0, 1 | 4), [K], "one result per selected output"),
+        ("K of A's shape", [A], at(1, 0.0, 4), [A], "K 9 times"),
+        ("A not (..., 3, 3)", [(xf.DT_F64, 16, (4, 9))], at(1, 0.0, 4), [K], "(..., 3, 3)"),
+        ("F32 buffer", [(xf.DT_F32, 16, (4, 3, 3))], at(1, 0.0, 4), [K], "dtype"),
+        ("pow without alpha", [A], at(2, 0.0, 4), [K], "invalid kind or alpha"),
+    ]
+    for label, args, attrs, rets, text in cases:
+        xla = xf.FakeXla()
+        cf, keep = xf.frame3(xla, args, rets, attrs)
+        assert call(lib, "GmfTangentCuda", cf) is not None, label
+        assert xla.errors[-1][0] == xf.ERR_INVALID_ARGUMENT and text in xla.errors[-1][1], (label, xla.errors[-1])
+    E = (xf.DT_F64, 16, (0, 3, 3))
+    xla = xf.FakeXla()
+    cf, keep = xf.frame3(xla, [E], [E, (xf.DT_F64, 16, (0, 9, 9))], at(1, 0.0, 1 | 4))
+    assert call(lib, "GmfTangentCuda", cf) is None and xla.errors == []

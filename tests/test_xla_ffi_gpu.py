@@ -119,3 +119,29 @@ def test_adjoint_handlers_equal_c_abi(fam, dt, mask):
     torch.cuda.synchronize()
     for o, b in zip(outs, sel):
         assert torch.equal(torch.nan_to_num(o), torch.nan_to_num(ref[b]))
+
+
+@pytest.mark.parametrize("mask", [4, 1 | 2 | 4])
+def test_tangent_handler_equals_c_abi(mask):
+    """GmfTangentCuda (F, G = J^T F, K = J^T J + F : H selected by a bit mask) gives the results of gmf_cuda_tangent"""
+    import torch
+
+    import matfun_gb300
+    lib = matfun_gb300.load()
+    raw = C.CDLL(matfun_gb300.library_path())
+    batch = (4, 9)
+    A = inputs("general", batch, seed=5)
+    n = int(np.prod(batch))
+    shapes = {0: A.shape, 1: A.shape, 2: (*batch, 3, 3, 3, 3)}
+    sel = [b for b in range(3) if mask >> b & 1]
+    outs = [torch.full(shapes[b], 5.0, dtype=torch.float64, device="cuda") for b in sel]
+    xla = xf.FakeXla()
+    cf, keep = xf.frame3(xla, [(xf.DT_F64, A.data_ptr(), tuple(A.shape))],
+                         [(xf.DT_F64, o.data_ptr(), tuple(o.shape)) for o in outs], xf.adjoint_attrs(1, 0.0, mask))
+    assert xf.handler(raw, "GmfTangentCuda")(C.addressof(cf)) is None, xla.errors
+    ref = [torch.full(shapes[b], 7.0, dtype=torch.float64, device="cuda") if mask >> b & 1 else None for b in range(3)]
+    p = lambda t: None if t is None else t.data_ptr()
+    assert lib.gmf_cuda_tangent(1, 0.0, n, A.data_ptr(), *map(p, ref), None) == 0
+    torch.cuda.synchronize()
+    for o, b in zip(outs, sel):
+        assert torch.equal(torch.nan_to_num(o), torch.nan_to_num(ref[b]))
