@@ -176,3 +176,13 @@ def test_streams_and_python_api():
     assert maxrel(H.cpu().numpy(), Ho) <= TOL and maxrel(F.cpu().numpy(), Fo) <= TOL
     Fs = matfun_gb300.smf("sqrt", torch.from_numpy(_spd(10, 1)).cuda())
     assert maxrel(Fs.cpu().numpy(), ol.smf("sqrt", _spd(10, 1))) <= TOL
+
+
+@pytest.mark.parametrize("kind,alpha,name", [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3")])
+@pytest.mark.parametrize("order", [1, 2])
+def test_gmf_ordered_launch(kind, alpha, name, order):
+    """n >= 2^15: the launch ordered by spectral class (key, scan, scatter, the ordered evaluation and the plain
+    evaluation of the last rows, whose share of J or H held the scratch) against the oracle on the whole batch"""
+    from matfun_gb300 import workloads as w
+    X = w.c1_gmf_groups(36000, seed=31).reshape(-1, 9)
+    _cmp("gmf_eval", kind, alpha, X, order, 9)
