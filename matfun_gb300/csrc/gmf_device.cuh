@@ -173,10 +173,10 @@ MF_D cx coef0(const GmfCoef &C, double sig, double m, cx x, cx mu, int k) {
 // FP64 pipe is the bottleneck of this kernel) with a threshold 2^-0.05 below 1e-17, so that the count is never
 // smaller than the FP64 bound's; one term more changes a result by less than 1e-17 relative.
 //
-// Also the term indices j1, j2 from which on every term is 2^-8 (j1) and 2^-32 (j2) below the largest term bound (the
+// Also the term indices j1, j2 from which on every term is 2^-6 (j1) and 2^-30 (j2) below the largest term bound (the
 // bound is unimodal in k): group_series sums the terms from j1 on in float-float and from j2 on in FP32, whose
-// rounding errors (2^-48 and 2^-24 of the term) then stay below 2^-56 of the largest term, under the FP64 rounding of
-// the leading terms.
+// rounding errors (2^-48 and 2^-24 of the term) then stay below 2^-54 of the largest term, under the FP64 rounding of
+// the leading terms (2^-53 of the largest).
 MF_D int nterms(const GmfCoef &C, int n, double r, double q, int &j1, int &j2) {
   constexpr float L17 = -56.5237f - 0.05f;  // log2(1e-17) less a margin
   int M = 1, k1 = G_KMAX, k2 = G_KMAX;
@@ -188,8 +188,8 @@ MF_D int nterms(const GmfCoef &C, int n, double r, double q, int &j1, int &j2) {
       const float t = C.lterm[k] + lk;
       best = fmaxf(best, t);
       M = k;
-      k1 = (k1 == G_KMAX) & (t <= best - 8.0f) ? k : k1;
-      k2 = (k2 == G_KMAX) & (t <= best - 32.0f) ? k : k2;
+      k1 = (k1 == G_KMAX) & (t <= best - 6.0f) ? k : k1;
+      k2 = (k2 == G_KMAX) & (t <= best - 30.0f) ? k : k2;
       if (((k > 2) & (t <= best + L17)) | (lk < -1074.0f)) break;
     }
   }
