@@ -65,10 +65,10 @@ cudaError_t launch(int fam, int kind, double alpha, int64_t n, const double *x, 
   }
   const bool mat = fam == MATRIX;
   switch (kind) {
-    case SMF_EXP: return mf::smf_launch_exp(alpha, n, x, mat, F, J, H, st, asym);
-    case SMF_LOG: return mf::smf_launch_log(alpha, n, x, mat, F, J, H, st, asym);
-    case SMF_SQRT: return mf::smf_launch_sqrt(alpha, n, x, mat, F, J, H, st, asym);
-    default: return mf::smf_launch_pow(alpha, n, x, mat, F, J, H, st, asym);
+    case SMF_EXP: return mf::smf_launch_exp(alpha, n, x, mat, F, J, H, st, asym, reorder);
+    case SMF_LOG: return mf::smf_launch_log(alpha, n, x, mat, F, J, H, st, asym, reorder);
+    case SMF_SQRT: return mf::smf_launch_sqrt(alpha, n, x, mat, F, J, H, st, asym, reorder);
+    default: return mf::smf_launch_pow(alpha, n, x, mat, F, J, H, st, asym, reorder);
   }
 }
 

@@ -8,7 +8,7 @@
 namespace mf {
 #define MF_SMF_DECL(k)                                                                                          \
   cudaError_t smf_launch_##k(double al, int64_t n, const double *x, bool mat, double *F, double *J, double *H, \
-                             cudaStream_t st, int *asym = nullptr);
+                             cudaStream_t st, int *asym = nullptr, bool reorder = true);
 MF_SMF_DECL(exp)
 MF_SMF_DECL(log)
 MF_SMF_DECL(sqrt)

@@ -3,7 +3,7 @@
 
 namespace mf {
 cudaError_t smf_launch_pow(double al, int64_t n, const double *x, bool mat, double *F, double *J, double *H,
-                            cudaStream_t st, int *asym) {
-  return smf_launch_t<POW>(al, n, x, mat, F, J, H, st, asym);
+                            cudaStream_t st, int *asym, bool reorder) {
+  return smf_launch_t<POW>(al, n, x, mat, F, J, H, st, asym, reorder);
 }
 }  // namespace mf

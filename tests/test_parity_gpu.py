@@ -186,3 +186,21 @@ def test_gmf_ordered_launch(kind, alpha, name, order):
     from matfun_gb300 import workloads as w
     X = w.c1_gmf_groups(36000, seed=31).reshape(-1, 9)
     _cmp("gmf_eval", kind, alpha, X, order, 9)
+
+
+@pytest.mark.parametrize("kind,alpha,name", [(0, 0.0, "exp"), (1, 0.0, "log"), (2, 0.3, "pow 0.3")])
+@pytest.mark.parametrize("mat", [False, True])
+def test_smf_ordered_launch(kind, alpha, name, mat):
+    """n >= 2^17, order 2: the smf launch ordered by the branch pattern of the second divided differences (key,
+    scan, scatter, the ordered evaluation and the plain evaluation of the last rows, whose share of H held the
+    scratch) against the oracle on the whole batch; in the matrix layout one non-symmetric matrix gives NaN"""
+    from matfun_gb300 import workloads as w
+    n = (1 << 17) + 77
+    if mat:
+        A = w.c0_smf_spd(n, seed=41, as_voigt=False)
+        A[n - 5, 0, 2] += 1.0  # in the plain tail
+        A[1000, 1, 2] += 1.0   # in the ordered part
+        g, _ = _cmp("smf_eval_matrix", kind, alpha, A.reshape(n, 9), 2, 9)
+        assert np.isnan(g[1][n - 5]).all() and np.isnan(g[1][1000]).all()
+    else:
+        _cmp("smf_eval", kind, alpha, w.c0_smf_spd(n, seed=41), 2, 6)
