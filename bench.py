@@ -296,6 +296,31 @@ def mixed_gmf_vs_fp64(lib, args, dev, hbm):
             "mixed_hbm_frac": bytes32 * n / (ms32 * 1e-3) / 1e9 / hbm, "bytes_per_matrix_fp32": bytes32}
 
 
+def smf_c0(lib, args, dev):
+    """C0: smf log order 2 on Voigt vectors, FP64 (n = 65536 SPD matrices with 10 % repeated and 2 % triple
+    eigenvalues), through smf_cuda_eval; batches of 2^17 or more run the ordered launch"""
+    import torch
+
+    from matfun_gb300 import workloads as w
+    n = args.smf_n
+    V = torch.from_numpy(w.c0_smf_spd(n)).to(dev)
+    F, J, H = (torch.empty((n, k), dtype=torch.float64, device=dev) for k in (6, 36, 216))
+    call = lambda: lib.smf_cuda_eval(1, 0.0, n, V.data_ptr(), F.data_ptr(), J.data_ptr(), H.data_ptr(), None)
+    for _ in range(3):
+        assert call() == 0
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(args.steps, 10)
+    e0.record()
+    for _ in range(steps):
+        call()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"workload": f"C0: smf log order 2, Voigt, n={n} SPD (10 % repeated, 2 % triple eigenvalues), FP64",
+            "ms": ms, "matrices_per_s": n / (ms * 1e-3), "ordered": n >= (1 << 17)}
+
+
 def tangent_vs_materialised(lib, args, dev):
     """the tangent of psi(A) = |log A|^2 / 2 (G = J^T F, K = J^T J + F : H) on the C1 workload, n = 2^20 FP64: the
     fused kernel (gmf_cuda_tangent, no J or H formed) against evaluating F, J, H (gmf_cuda_eval) and contracting them
@@ -613,6 +638,8 @@ def run_ours(args, rank, world, local):
     if rank == 0 and not args.no_mixed:
         out["mixed"] = mixed_vs_fp64(lib, args, dev, hbm)
         out["mixed_gmf"] = mixed_gmf_vs_fp64(lib, args, dev, hbm)
+    if rank == 0:
+        out["smf_c0"] = smf_c0(lib, args, dev)
     if rank == 0 and args.mixed_sweep:
         out["mixed_sweep"] = mixed_sweep(lib, args, dev, hbm)
     if rank == 0 and not args.no_adjoint:
@@ -652,6 +679,7 @@ def main():
     ap.add_argument("--mixed-steps", type=int, default=5)
     ap.add_argument("--gmf-mixed-n", type=int, default=1 << 20)
     ap.add_argument("--mixed-sweep", action="store_true", help="also the C2 workload over every kind and order")
+    ap.add_argument("--smf-n", type=int, default=1 << 16, help="matrices of the C0 section (smf log order 2)")
     args = ap.parse_args()
     args.alpha = 0.5 if args.kind == "sqrt" else 0.0
     if args.kind == "sqrt":
