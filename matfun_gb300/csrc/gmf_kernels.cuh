@@ -22,7 +22,10 @@
 // The reference forms Y (27), Z (81) and Yh (243) per matrix and evaluates each of the 729 H entries with 6
 // multiply-adds in every thread (gmf_kernel.hpp:636-691); the symmetric form needs about a third of the FP64
 // instructions, which bound this kernel on GB300 (FP64 at 1/74 of the FP32 rate).  Spreading one matrix over the
-// warp keeps the shared memory per CTA small (31 KB), so the occupancy is set by the registers of phase A.
+// warp keeps phase B's work area at 4.5 KB per warp; the CTA's ~106 KB of shared memory (states and records of its
+// 128 matrices) and phase A's 255 registers per thread both allow two CTAs per SM.
+// Large batches (log, pow at orders 1 and 2, exp at order 2, n >= 2^15) are first ordered batch-wide by spectral
+// class (gmf_launch_sorted below), so that a CTA's matrices share their branches before the CTA-local orderings.
 #pragma once
 #include <climits>
 

@@ -1,4 +1,4 @@
-// smf_kernels.cu -- symmetric family (smf_cuda_eval / smf_cuda_eval_matrix): F, J, H of f(A) for symmetric 3x3
+// smf_kernels.cuh -- symmetric family (smf_cuda_eval / smf_cuda_eval_matrix): F, J, H of f(A) for symmetric 3x3
 // matrices, FP64, Voigt or matrix layout.  Replaces smf_eval_kernel / smf_hess_kernel of the reference
 // (cuda/src/matfun_cuda.cu:28-96).
 //
@@ -6,9 +6,11 @@
 // differences and the distinct entries of J (21 values of the symmetric form K) and H (56 values of the symmetric
 // form G'), see smf_device.cuh, into shared memory.  Both forms are evaluated through the product vectors
 // P_kl = (V_ka V_la)_a of rows of V: J from the 21 values of B(x, y) = sum D_ab x_a y_b, H from the 56 values of
-// T(x, y, z) = sum D2_amb x_a y_m z_b, about half the FP64 instructions of assembling V S V^T per index pair.  Phase B: the CTA expands them into the output layout with
-// fully coalesced stores (64 consecutive doubles per store instruction); the layout weights (powers of two) are
-// applied on the exponent bits, not on the FP64 pipe.
+// T(x, y, z) = sum D2_amb x_a y_m z_b, about half the FP64 instructions of assembling V S V^T per index pair.
+// Phase B: the CTA expands them into the output layout with coalesced stores (64 consecutive doubles of a row per
+// store instruction); the layout weights (powers of two) are applied on the exponent bits, not on the FP64 pipe.
+// Order-2 batches of 2^17 matrices or more are first ordered by the predicted branch pattern of their second divided
+// differences (smf_launch_sorted below).
 #pragma once
 #include <climits>
 
