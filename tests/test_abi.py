@@ -76,6 +76,12 @@ def test_abi_error_codes_need_no_device(lib):
     assert lib.smf_cuda_eval(0, 0.0, -1, None, None, None, None, None) == -1
     assert lib.smf_cuda_eval(0, 0.0, 0, None, None, None, None, None) == 0
     assert lib.smf_cuda_eval(0, 0.0, 10, None, None, None, None, None) == -1  # null input with n > 0
+    # the tangent entry point: invalid kind, pow without alpha, n < 0, no A or no K for n > 0; empty batch
+    assert lib.gmf_cuda_tangent(4, 0.0, 10, None, None, None, None, None) == -1
+    assert lib.gmf_cuda_tangent(2, -1.0, 10, None, None, None, None, None) == -1
+    assert lib.gmf_cuda_tangent(1, 0.0, -3, None, None, None, None, None) == -1
+    assert lib.gmf_cuda_tangent(1, 0.0, 10, None, None, None, None, None) == -1
+    assert lib.gmf_cuda_tangent(1, 0.0, 0, None, None, None, None, None) == 0
 
 
 def test_workloads_shapes_and_spectra():
