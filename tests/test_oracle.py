@@ -95,3 +95,27 @@ def test_oracle_domain_nan():
         assert r == 0
         assert np.isnan(F[1]).all() == (kind != 0)
         assert np.isfinite(F[[0, 2]]).all()
+
+
+@pytest.mark.parametrize("fam,fn,nf", [("smf", "smf_eval", 6), ("gmf", "gmf_eval", 9)])
+def test_fp32_golden_fixtures_reproduce(fam, fn, nf):
+    """tests/golden/cases_*_f32.npz (tests/golden/make_golden_f32.py): the expected values are the oracle's F, J, H
+    of the stored FP32 inputs (a sample of every kind, 1e-14: another host's libm may differ in the last bits), and
+    every tolerance is the stated one of its kind"""
+    import importlib.util
+    here = os.path.dirname(os.path.abspath(__file__))
+    g = np.load(os.path.join(here, "golden", f"cases_{fam}_f32.npz"))
+    spec = importlib.util.spec_from_file_location("make_golden_f32", os.path.join(here, "golden", "make_golden_f32.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    assert g["x"].dtype == np.float32
+    for i in range(len(g["kind"])):
+        assert g["tol"][i] == mk.tol(fam, int(g["kind"][i]), float(g["alpha"][i]))
+    for kind in np.unique(g["kind"]):
+        for i in np.where(g["kind"] == kind)[0][:6]:
+            r, F, J, H = ol.call(ol.oracle(), fn, int(kind), float(g["alpha"][i]), g["x"][i:i + 1].astype(np.float64),
+                                 2, nf)
+            assert r == 0
+            for got, name in ((F, "F"), (J, "J"), (H, "H")):
+                assert np.array_equal(np.isnan(got[0]), np.isnan(g[name][i]))
+                assert maxrel(got[0], g[name][i]) <= 1e-14, (fam, i, name)
