@@ -406,23 +406,25 @@ def adjoint_vs_materialised(lib, args, dev):
             return e0.elapsed_time(e1) / reps
 
         t_vjp, t_hvp = timeit(vjp), timeit(hvp)
-        # materialised: J (and H) by the eval kernel in chunks of 2^20, then the contractions
-        ch = 1 << 20
+        # materialised: J (and H) by the eval kernel in chunks of at most 2^20, then the contractions
+        ch = min(1 << 20, n)
         Fm = torch.empty((ch, 9), dtype=torch.float64, device=dev)
         Jm = torch.empty((ch, 81), dtype=torch.float64, device=dev)
         Hm = torch.empty((ch, 729), dtype=torch.float64, device=dev)
 
         def mat_vjp():
             for lo in range(0, n, ch):
-                ev(kind, alpha, ch, A[lo:].data_ptr(), Fm.data_ptr(), Jm.data_ptr(), None, None)
-                Abar[lo:lo + ch] = torch.einsum("nab,nabcd->ncd", W[lo:lo + ch], Jm.view(ch, 3, 3, 3, 3))
+                m = min(ch, n - lo)  # the matrices of this chunk (the last may be shorter)
+                ev(kind, alpha, m, A[lo:].data_ptr(), Fm.data_ptr(), Jm.data_ptr(), None, None)
+                Abar[lo:lo + m] = torch.einsum("nab,nabcd->ncd", W[lo:lo + m], Jm[:m].view(m, 3, 3, 3, 3))
 
         def mat_hvp():
             for lo in range(0, n, ch):
-                ev(kind, alpha, ch, A[lo:].data_ptr(), Fm.data_ptr(), Jm.data_ptr(), Hm.data_ptr(), None)
-                HV = torch.einsum("nabcdef,ncd->nabef", Hm.view(ch, 3, 3, 3, 3, 3, 3), V[lo:lo + ch])
-                HWV[lo:lo + ch] = torch.einsum("nab,nabef->nef", W[lo:lo + ch], HV)
-                JV[lo:lo + ch] = torch.einsum("nabcd,ncd->nab", Jm.view(ch, 3, 3, 3, 3), V[lo:lo + ch])
+                m = min(ch, n - lo)
+                ev(kind, alpha, m, A[lo:].data_ptr(), Fm.data_ptr(), Jm.data_ptr(), Hm.data_ptr(), None)
+                HV = torch.einsum("nabcdef,ncd->nabef", Hm[:m].view(m, 3, 3, 3, 3, 3, 3), V[lo:lo + m])
+                HWV[lo:lo + m] = torch.einsum("nab,nabef->nef", W[lo:lo + m], HV)
+                JV[lo:lo + m] = torch.einsum("nabcd,ncd->nab", Jm[:m].view(m, 3, 3, 3, 3), V[lo:lo + m])
 
         t_mvjp, t_mhvp = timeit(mat_vjp, 1), timeit(mat_hvp, 1)
         del Fm, Jm, Hm
