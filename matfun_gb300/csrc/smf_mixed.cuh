@@ -233,7 +233,14 @@ MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E) {
   for (int i = 0; i < 3; i++) kd = max(kd, __float_as_int(dv[i]) & 0x7FFFFFFF);
 #pragma unroll
   for (int k = 0; k < 3; k++) kd = max(kd, __float_as_int(o[k].hi) & 0x7FFFFFFF);
-  const bool iso = (kd == 0) | bad;
+  // A within 2^-40 of its largest entry (scaled into [1, 2)) of a multiple of I: its FP32 diagonal entries are then
+  // equal, and dropping the off-diagonal entries makes it isotropic (V = I, the diagonal as eigenvalues), which
+  // neglects less than 2^-40 |A| |f'| in F, far below FP32 output.  The rotation of the general path is not taken for
+  // these: on GB300 one such matrix (deviator 2^-54 |A|) came out of it with eigenvectors 0.6 % from orthonormal.
+  const bool flat = kd < ((127 - 40) << 23);
+#pragma unroll
+  for (int k = 0; k < 3; k++) o[k] = ff_sel(flat, ffl{0.f, 0.f}, o[k]);
+  const bool iso = flat | bad;
   const int ed = min(max((kd >> 23) & 0xFF, 1), 253);
   const float dsc = __int_as_float(ed << 23), ids = __int_as_float((254 - ed) << 23);
   float g0 = dv[0] * ids, g1 = dv[1] * ids, g2 = dv[2] * ids;

@@ -75,6 +75,55 @@ def test_smf_mixed_c0_and_golden_inputs():
     assert max(errs) <= 1e-5
 
 
+def near_isotropic_f32():
+    """FP32 matrices within 2^-30 .. 2^-70 of a multiple of I: c (I + 2^-e S), S symmetric with zero diagonal (the
+    deviator exactly representable in FP32), and row 29913 of C0 (n = 65536, seed 4), whose FP32 eigenvectors came out
+    of the general path of smf_eigsys_ff 0.6 % from orthonormal on GB300 (F 3e-3 from the oracle)"""
+    from matfun_gb300 import workloads as w
+    rng = np.random.default_rng(29913)
+    parts = [w.c0_smf_spd(65536, seed=4, as_voigt=False)[29913:29914]]
+    for e in (30, 39, 41, 52, 60, 70):
+        c = np.exp(rng.uniform(-2, 2, 256))
+        S = rng.standard_normal((256, 3, 3))
+        S = S + S.transpose(0, 2, 1)
+        S[:, [0, 1, 2], [0, 1, 2]] = 0.0
+        parts.append(c[:, None, None] * (np.eye(3) + 2.0 ** -e * S))
+    return np.concatenate(parts).astype(np.float32)
+
+
+@pytest.mark.xfail(strict=False, reason="the near-isotropic branch of smf_eigsys_ff has been checked on the CPU only")
+@pytest.mark.parametrize("kind,alpha,name", KINDS)
+def test_smf_mixed_near_isotropic(kind, alpha, name):
+    A = near_isotropic_f32()
+    errs, got, ref = errors(True, kind, alpha, A.reshape(-1, 9), 2)
+    row = [maxrel(g[:1], r[:1]) for g, r in zip(got, ref[1:])]
+    print(f"mixed smf near-isotropic {name}: max rel F J H {errs}; C0 row 29913 alone {row}")
+    assert max(errs) <= TOL and max(row) <= TOL
+
+
+@pytest.mark.xfail(strict=False, reason="the near-isotropic branch of smf_eigsys_ff has been checked on the CPU only")
+def test_smf_mixed_adjoint_near_isotropic():
+    """the FP32 VJP against the FP64 one on the same FP32 inputs (log: on a multiple of I, Abar = sym(W) / c)"""
+    import torch
+
+    import matfun_gb300
+    lib = matfun_gb300.load()
+    A32 = torch.from_numpy(near_isotropic_f32()).cuda()
+    n = A32.shape[0]
+    W32 = torch.from_numpy(np.random.default_rng(5).standard_normal((n, 3, 3)).astype(np.float32)).cuda()
+    Ab32 = torch.empty_like(A32)
+    A64, W64 = A32.double(), W32.double()
+    Ab64 = torch.empty_like(A64)
+    assert lib.smf_cuda_adjoint_f32(1, 0.0, n, A32.data_ptr(), W32.data_ptr(), None, None, Ab32.data_ptr(),
+                                    None, None, None) == 0
+    assert lib.smf_cuda_adjoint(1, 0.0, n, A64.data_ptr(), W64.data_ptr(), None, None, Ab64.data_ptr(),
+                                None, None, None) == 0
+    torch.cuda.synchronize()
+    err = maxrel(Ab32.double().cpu().numpy(), Ab64.cpu().numpy())
+    print(f"mixed smf adjoint near-isotropic log: max rel Abar {err:.2e}")
+    assert err <= TOL
+
+
 # ---- general family (gmf_cuda_eval_f32): FP64 spectral analysis and series, FP32 storage and J / H assembly
 GMF_KINDS = [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3")]
 GMF_TOL = 1e-6
