@@ -28,6 +28,27 @@ struct SmfCoef {
   double c2[DD2_TERMS];     // Taylor coefficients f^(k+2)/(k+2)! without the m-dependent factor (smf_kernel.hpp:135-146)
 };
 
+// host: the launch constants of a call (kind already normalised: sqrt has al = 0.5)
+inline void smf_coef(int kind, double al, SmfCoef &C) {
+  C.al = al;
+  double bh = al - 1.0, bb = bh - al;
+  C.bh1 = bh;
+  C.bl1 = (al - (bh - bb)) + (-1.0 - bb);
+  auto zpow = [](double e) { return e < 0 ? HUGE_VAL : (e == 0 ? 1.0 : 0.0); };
+  C.zp1 = zpow(al - 1.0);
+  C.z2 = al == 1.0 ? 0.0 : al * (al - 1.0) / 2.0 * zpow(al - 2.0);
+  C.tau = (kind == POW && 3.0 / al < DD2_TAU) ? 3.0 / al : DD2_TAU;
+  if (kind == EXP) {
+    double f = 0.5;
+    for (int k = 0; k < DD2_TERMS; k++) { C.c2[k] = f; f /= (k + 3.0); }
+  } else if (kind == LOG) {
+    for (int k = 0; k < DD2_TERMS; k++) C.c2[k] = (k % 2 ? 1.0 : -1.0) / (k + 2.0);
+  } else {
+    double b = al * (al - 1.0) / 2.0;
+    for (int k = 0; k < DD2_TERMS; k++) { C.c2[k] = b; b *= (al - k - 2.0) / (k + 3.0); }
+  }
+}
+
 template <int KIND>
 MF_D double smf_fun(double x, double al) {
   if (KIND == EXP) return exp(x);

@@ -1,433 +1,11 @@
-// smf_mixed.cuh -- mixed-precision symmetric family: FP32 input and output, FP32 for the bulk of the arithmetic.
-//
-// Beyond FP32 precision (float-float, ffloat.cuh, on the FP32 pipe) only where FP32 would lose the result:
-//   * the Rayleigh quotients that give the eigenvalues and the Gram matrix of the eigenvectors: with condition
-//     numbers up to 1e6 and eigenvalue gaps down to 1e-12 FP32 quotients lose the small eigenvalues and the
-//     near-degenerate pairs entirely;
-//   * the differences of eigenvalues that feed the near-coalescent branches of the divided differences (z, u, w and
-//     the denominators of the difference formulas), taken from the float-float eigenvalues before rounding to FP32.
-// f(lambda), the first and second divided differences (stable forms, cluster series), the product vectors and the
-// J / H forms of smf_kernels.cuh run in FP32.  The kernel executes no FP64 instruction (the FP64 kernel: ~2.5k per
-// matrix, at 1/74 of the FP32 rate on GB300), so it moves towards the HBM roofline, and FP32 storage halves the bytes.
-// Accuracy against the FP64 oracle is stated per kind and order in the tests (<= 1e-6 relative, max-norm).
+// smf_mixed.cuh -- mixed-precision symmetric family: the tile (coalesced FP32 input, eigensystem and divided
+// differences of smf_mixed_math.cuh per thread, the J / H forms of smf_kernels.cuh in FP32, coalesced FP32 output),
+// the standalone kernel and its launch.
 #pragma once
-#include "ffloat.cuh"
 #include "smf_kernels.cuh"
+#include "smf_mixed_math.cuh"
 
 namespace mf {
-
-// terms of the cluster series of the second divided difference in FP32: the offsets are at most tau = 0.25 of the
-// centre (exp: 1 in absolute terms, with factorial coefficients), so term k is below (k + 1) 0.25^k |c2[0]| and the
-// series is truncated below 1e-8 relative after 16 terms (the FP64 form keeps the reference's 30)
-constexpr int DD2_TERMS_F = 16;
-
-struct SmfCoefF {
-  float al, alm1;   // exponent and exponent - 1
-  float zp1, z2;    // 0^(al - 1), f''(0)/2 for powers
-  float tau;        // cluster radius of the second divided difference
-  float c2[DD2_TERMS];
-};
-
-MF_D float self(bool m, float a, float b) { return m ? a : b; }
-
-template <int KIND>
-MF_D float fun_f(float x, float al) {
-  if (KIND == EXP) return expf(x);
-  if (KIND == LOG) return logf(x);
-  if (!(x > 0.f)) return 0.f;
-  return KIND == SQRT ? sqrtf(x) : powf(x, al);
-}
-
-// Divided differences on eigenvalues sorted ascending, in FP32.  The eigenvalue differences are taken in FP64 and
-// rounded once (dab = b - a >= 0 and friends), so the near-coalescent branches see the same relative precision as
-// the FP64 kernel; with the order known, the choice of difference formula and of the cluster midpoint of the FP64
-// kernel becomes static.
-// f[a, b], a <= b, dab = b - a -- smf_kernel.hpp:84-115
-template <int KIND>
-MF_D float dd1s_f(float a, float b, float dab, float fa, float fb, const SmfCoefF &C) {
-  if (KIND == EXP) return fb * self(dab > 0.f, -expm1f(-dab) / dab, 1.f);
-  if (KIND == LOG) {
-    float s = 0.5f * (a + b), z = dab / (a + b), az = fabsf(z), z2 = z * z;
-    if (az < 1e-3f) return (1.f + z2 / 3.f + z2 * z2 / 5.f + z2 * z2 * z2 / 7.f) / s;
-    if (az >= 0.5f) return (logf(b) - logf(a)) / dab;
-    return atanhf(z) / z / s;
-  }
-  if (KIND == SQRT) return 1.f / (sqrtf(a) + sqrtf(b));
-  float s = 0.5f * (a + b), ss = self(s > 0.f, s, 1.f);
-  float z = dab / (2.f * ss), az = fabsf(z);
-  bool zero = az == 0.f, near = !zero & (az < 0.5f);
-  if (!zero & !near) return (fb - fa) / dab;
-  float g = zero ? C.al : (expm1f(C.al * log1pf(z)) - expm1f(C.al * log1pf(-z))) / (2.f * z);
-  return (s > 0.f ? powf(ss, C.alm1) : C.zp1) * g;
-}
-
-template <int KIND>
-MF_D float deriv_f(float x, float fx, const SmfCoefF &C) {
-  if (KIND == EXP) return fx;
-  if (KIND == LOG) return 1.f / x;
-  float xf = self(x > 0.f, x, 0.f);
-  if (KIND == SQRT) return 1.f / (2.f * sqrtf(xf));
-  return xf > 0.f ? C.al * powf(xf, C.alm1) : C.al * C.zp1;
-}
-
-// f[li, lj, lk] for li <= lj <= lk; dji = lj - li, dkj = lk - lj, dki = lk - li -- smf_kernel.hpp:148-192 (the widest
-// difference is the denominator, the middle eigenvalue the cluster centre)
-template <int KIND>
-MF_D float dd2s_f(float lj, float lk, float fj, float Dij, float Djk, float dji, float dkj, float dki,
-                  const SmfCoefF &C) {
-  bool cluster;
-  if (KIND == EXP) cluster = (dkj + dji) <= 1.f;
-  else cluster = (lj > 0.f) & (dji <= C.tau * lj) & (dkj <= C.tau * lj);
-  float out;
-  if (cluster) {
-    float u, w, scale;
-    if (KIND == EXP) {
-      u = -dji; w = dkj; scale = fj;
-    } else {
-      u = -dji / lj; w = dkj / lj;
-      scale = (KIND == LOG ? 1.f : fj) / (lj * lj);
-    }
-    float h = 1.f, wk = 1.f, sm = C.c2[0];
-#pragma unroll
-    for (int k = 1; k < DD2_TERMS_F; k++) {
-      wk = wk * w;
-      h = fmaf(u, h, wk);
-      sm = fmaf(C.c2[k], h, sm);
-    }
-    out = scale * sm;
-  } else {
-    out = (Djk - Dij) / self(dki != 0.f, dki, 1.f);
-  }
-  if (KIND == POW || KIND == SQRT) out = self(lk > 0.f, out, C.z2);
-  return out;
-}
-
-template <int KIND>
-MF_D float dd2_same_f(float lf, float fl, float Dll, const SmfCoefF &C) {
-  bool cluster = KIND == EXP ? true : (lf > 0.f);
-  float out = KIND == EXP ? self(cluster, fl * C.c2[0], Dll - Dll)
-                          : self(cluster, ((KIND == LOG ? 1.f : fl) / (lf * lf)) * C.c2[0], Dll - Dll);
-  if (KIND == POW || KIND == SQRT) out = self(lf > 0.f, out, C.z2);
-  return out;
-}
-
-MF_D float nrm3(float &x, float &y, float &z) {
-  float n = __fsqrt_rn(x * x + y * y + z * z), i = __fdiv_rn(1.f, n);
-  x *= i; y *= i; z *= i;
-  return n;
-}
-
-// The symmetric input of the mixed path: FP32 diagonal, float-float off-diagonal (the exact average of a_ij and a_ji
-// for the matrix layout; LO = false for Voigt input, whose off-diagonal entries are FP32 values)
-struct SmfInF {
-  float d[3];
-  ffl o[3];  // (0,1), (0,2), (1,2)
-};
-
-// x^T A x with the diagonal shifted by a float-float (A - mu I), compensated (Dot2) to float-float accuracy
-template <bool LO>
-MF_D ffl quad_ff(const ffl *dg, const ffl *o, float x0, float x1, float x2) {
-  const float x[3] = {x0, x1, x2};
-  ffacc A = {0.f, 0.f};
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    ffl p = two_prod(x[i], x[i]);
-    ffl t = two_prod(dg[i].hi, p.hi);
-    acc_add(A, t.hi);
-    A.e += fmaf(dg[i].hi, p.lo, fmaf(dg[i].lo, p.hi, t.lo));
-  }
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const int i = k == 2 ? 1 : 0, j = k == 0 ? 1 : 2;
-    ffl p = two_prod(2.f * x[i], x[j]);
-    ffl t = two_prod(o[k].hi, p.hi);
-    acc_add(A, t.hi);
-    A.e += LO ? fmaf(o[k].hi, p.lo, fmaf(o[k].lo, p.hi, t.lo)) : fmaf(o[k].hi, p.lo, t.lo);
-  }
-  return acc_ff(A);
-}
-
-// x^T A y (A as above)
-template <bool LO>
-MF_D ffl bil_ff(const ffl *dg, const ffl *o, const float *x, const float *y) {
-  ffacc A = {0.f, 0.f};
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    ffl p = two_prod(x[i], y[i]);
-    ffl t = two_prod(dg[i].hi, p.hi);
-    acc_add(A, t.hi);
-    A.e += fmaf(dg[i].hi, p.lo, fmaf(dg[i].lo, p.hi, t.lo));
-  }
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const int i = k == 2 ? 1 : 0, j = k == 0 ? 1 : 2;
-    ffl p1 = two_prod(x[i], y[j]), p2 = two_prod(x[j], y[i]);
-    ffl s = two_sum(p1.hi, p2.hi);
-    float sl = s.lo + (p1.lo + p2.lo);
-    ffl t = two_prod(o[k].hi, s.hi);
-    acc_add(A, t.hi);
-    A.e += LO ? fmaf(o[k].hi, sl, fmaf(o[k].lo, s.hi, t.lo)) : fmaf(o[k].hi, sl, t.lo);
-  }
-  return acc_ff(A);
-}
-
-MF_D ffl dot_ff(const float *x, const float *y) {
-  ffacc A = {0.f, 0.f};
-#pragma unroll
-  for (int i = 0; i < 3; i++) acc_prod(A, x[i], y[i]);
-  return acc_ff(A);
-}
-
-// q / n for n = 1 + e close to 1: q (1 - e + e^2), float-float
-MF_D ffl div_norm(ffl q, ffl n) {
-  float e = (n.hi - 1.f) + n.lo;
-  return ff_mul(q, fast_two_sum(1.f, e * e - e));
-}
-
-// The eigensystem of the mixed path, with no FP64: FP32 for the cubic's trigonometric root (on the deviator normalised
-// to max 1, where the root of the separated eigenvalue is insensitive to rounding of r), its eigenvector (largest
-// cross product of two rows of G - root I), the orthonormal complement and the 2x2 Jacobi rotation; float-float
-// (ffloat.cuh) for the deviator, the Rayleigh quotients of the FP32 vectors and their Gram matrix.  The quotients
-// are taken in A - mu I, mu the centre of the remaining pair, so that the pair's block is of the size of its own gap:
-// the rotation angle is accurate relative to the gap, and the quotients divided by the vectors' squared norms give
-// the eigenvalues to ~1e-14 relative to |A| (an FP32 vector error d moves a quotient by O(d^2)).  One Newton-Schulz
-// step V (3 I - V^T V) / 2 with the float-float Gram matrix leaves the FP32 vectors orthonormal to the rounding of
-// their components.  Input scaled by a power of two; eigenvalues and the deviator's eigenvalues (xd, for log near
-// the mean) in the units of the input.
-struct SmfEigF {
-  ffl lam[3], xd[3];
-  float m;
-  float V[3][3];
-};
-
-template <int KIND, bool LO>
-MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E) {
-  constexpr float SQRT6 = 2.4494897f, TWO_PI_3 = 2.0943951f;
-  // power-of-two scaling from the largest magnitude (integer compare of the bit patterns: NaN sorts above Inf)
-  int kb = 0;
-#pragma unroll
-  for (int i = 0; i < 3; i++) kb = max(kb, __float_as_int(in.d[i]) & 0x7FFFFFFF);
-#pragma unroll
-  for (int k = 0; k < 3; k++) kb = max(kb, __float_as_int(in.o[k].hi) & 0x7FFFFFFF);
-  const bool bad = kb >= 0x7F800000;  // NaN or infinite input: NaN vectors and results
-  int ex = min(max((kb >> 23) & 0xFF, 1), 253);
-  const float sig = __int_as_float(ex << 23), isig = __int_as_float((254 - ex) << 23);
-  float a[3];
-  ffl o[3];
-#pragma unroll
-  for (int i = 0; i < 3; i++) a[i] = in.d[i] * isig;
-#pragma unroll
-  for (int k = 0; k < 3; k++) o[k] = {in.o[k].hi * isig, LO ? in.o[k].lo * isig : 0.f};
-  // mean of the diagonal and deviator, float-float
-  ffl s01 = two_sum(a[0], a[1]), s = two_sum(s01.hi, a[2]);
-  s = fast_two_sum(s.hi, s.lo + s01.lo);
-  float q1 = s.hi / 3.f;
-  float q2 = (fmaf(-q1, 3.f, s.hi) + s.lo) / 3.f;
-  const ffl m = fast_two_sum(q1, q2);
-  float dv[3];  // deviator in FP32 (the input of the trigonometric root only)
-#pragma unroll
-  for (int i = 0; i < 3; i++) dv[i] = a[i] - m.hi;
-  // FP32: normalised deviator, trigonometric root, eigenvector, complement
-  int kd = 0;
-#pragma unroll
-  for (int i = 0; i < 3; i++) kd = max(kd, __float_as_int(dv[i]) & 0x7FFFFFFF);
-#pragma unroll
-  for (int k = 0; k < 3; k++) kd = max(kd, __float_as_int(o[k].hi) & 0x7FFFFFFF);
-  // A within 2^-40 of its largest entry (scaled into [1, 2)) of a multiple of I: its FP32 diagonal entries are then
-  // equal, and dropping the off-diagonal entries makes it isotropic (V = I, the diagonal as eigenvalues), which
-  // neglects less than 2^-40 |A| |f'| in F, far below FP32 output.  The rotation of the general path is not taken for
-  // these: on GB300 one such matrix (deviator 2^-54 |A|) came out of it with eigenvectors 0.6 % from orthonormal.
-  const bool flat = kd < ((127 - 40) << 23);
-#pragma unroll
-  for (int k = 0; k < 3; k++) o[k] = ff_sel(flat, ffl{0.f, 0.f}, o[k]);
-  const bool iso = flat | bad;
-  const int ed = min(max((kd >> 23) & 0xFF, 1), 253);
-  const float dsc = __int_as_float(ed << 23), ids = __int_as_float((254 - ed) << 23);
-  float g0 = dv[0] * ids, g1 = dv[1] * ids, g2 = dv[2] * ids;
-  float g3 = o[0].hi * ids, g4 = o[1].hi * ids, g5 = o[2].hi * ids;
-  float p = g0 * g0 + g1 * g1 + g2 * g2 + 2.f * (g3 * g3 + g4 * g4 + g5 * g5);
-  float q = g0 * (g1 * g2 - g5 * g5) - g3 * (g3 * g2 - g5 * g4) + g4 * (g3 * g5 - g1 * g4);
-  float pg = self(iso, 1.f, p), qg = self(iso, 0.f, q);
-  float r = 3.f * SQRT6 * qg / (pg * sqrtf(pg));
-  r = self(r > 1.f, 1.f, self(r < -1.f, -1.f, r));
-  float t = sqrtf(2.f * pg / 3.f), ph = acosf(r) / 3.f;
-  float sh = t * cosf(self(r >= 0.f, ph, ph + TWO_PI_3));
-  float m00 = g0 - sh, m11 = g1 - sh, m22 = g2 - sh;
-  float cxv = g3 * g5 - g4 * m11, cyv = g4 * g3 - m00 * g5, czv = m00 * m11 - g3 * g3;
-  float nn = cxv * cxv + cyv * cyv + czv * czv;
-  {
-    float bx = g3 * m22 - g4 * g5, by = g4 * g4 - m00 * m22, bz = m00 * g5 - g3 * g4;
-    float nb = bx * bx + by * by + bz * bz;
-    bool s1 = nb > nn;
-    cxv = self(s1, bx, cxv); cyv = self(s1, by, cyv); czv = self(s1, bz, czv); nn = self(s1, nb, nn);
-    float ex2 = m11 * m22 - g5 * g5, ey2 = g5 * g4 - g3 * m22, ez2 = g3 * g5 - m11 * g4;
-    float ne = ex2 * ex2 + ey2 * ey2 + ez2 * ez2;
-    bool s2 = ne > nn;
-    cxv = self(s2, ex2, cxv); cyv = self(s2, ey2, cyv); czv = self(s2, ez2, czv); nn = self(s2, ne, nn);
-  }
-  bool ok = (nn > 1e-30f) & !iso;
-  float v[3] = {self(ok, cxv, 1.f), self(ok, cyv, 0.f), self(ok, czv, 0.f)};
-  nrm3(v[0], v[1], v[2]);
-  float ax = fabsf(v[0]), ay = fabsf(v[1]), az = fabsf(v[2]);
-  bool k1 = ay < ax, k2 = az < self(k1, ay, ax);
-  float ex1 = self(k1 | k2, 0.f, 1.f), ey1 = self(k1 & !k2, 1.f, 0.f), ez1 = self(k2, 1.f, 0.f);
-  float vk = ex1 * v[0] + ey1 * v[1] + ez1 * v[2];
-  float u[3] = {ex1 - vk * v[0], ey1 - vk * v[1], ez1 - vk * v[2]};
-  nrm3(u[0], u[1], u[2]);
-  float w[3] = {v[1] * u[2] - v[2] * u[1], v[2] * u[0] - v[0] * u[2], v[0] * u[1] - v[1] * u[0]};
-  // float-float: quotients in A - mu I, mu = mean - root / 2 (the centre of the remaining pair)
-  const float mu = self(iso, m.hi, m.hi - 0.5f * (sh * dsc));
-  ffl dg[3];
-#pragma unroll
-  for (int i = 0; i < 3; i++) dg[i] = two_sum(a[i], -mu);
-  const ffl qv = quad_ff<LO>(dg, o, v[0], v[1], v[2]), nv = dot_ff(v, v);
-  const ffl b11 = quad_ff<LO>(dg, o, u[0], u[1], u[2]), b22 = quad_ff<LO>(dg, o, w[0], w[1], w[2]);
-  const ffl b12 = bil_ff<LO>(dg, o, u, w);
-  // FP32 Jacobi rotation of the pair from the block (its entries are of the size of the pair's gap)
-  ffl jd = ff_sub(b11, b22);
-  float jx = jd.hi + jd.lo, jy = 2.f * (b12.hi + b12.lo), jr = sqrtf(jx * jx + jy * jy);
-  bool jz = !(jr > 0.f), jpos = jx >= 0.f;
-  float jrs = self(jz, 1.f, jr);
-  float big = sqrtf((jrs + fabsf(jx)) / (2.f * jrs)), sml = jy / (2.f * jrs * big);
-  float sgn = self(jy >= 0.f, 1.f, -1.f);
-  float cs = self(jz, 1.f, self(jpos, big, sgn * sml)), sn = self(jz, 0.f, self(jpos, sml, sgn * big));
-  float r1[3] = {cs * u[0] + sn * w[0], cs * u[1] + sn * w[1], cs * u[2] + sn * w[2]};
-  float r2[3] = {cs * w[0] - sn * u[0], cs * w[1] - sn * u[1], cs * w[2] - sn * u[2]};
-  const ffl n1 = dot_ff(r1, r1), n2 = dot_ff(r2, r2);
-  const ffl q1f = quad_ff<LO>(dg, o, r1[0], r1[1], r1[2]), q2f = quad_ff<LO>(dg, o, r2[0], r2[1], r2[2]);
-  const ffl th[3] = {div_norm(qv, nv), div_norm(q1f, n1), div_norm(q2f, n2)};
-  const ffl mum = ff_sub(ff_from(mu), m);  // mu - mean
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    const ffl lam = ff_add(th[i], ff_from(mu));
-    E.lam[i] = {lam.hi * sig, lam.lo * sig};
-    const ffl xd = ff_add(th[i], mum);
-    E.xd[i] = {xd.hi * sig, xd.lo * sig};
-  }
-  E.m = m.hi * sig;
-  // Newton-Schulz step with the float-float Gram matrix
-  const ffl g01 = dot_ff(v, r1), g02 = dot_ff(v, r2), g12 = dot_ff(r1, r2);
-  float e00 = 0.5f * ((nv.hi - 1.f) + nv.lo), e11 = 0.5f * ((n1.hi - 1.f) + n1.lo);
-  float e22 = 0.5f * ((n2.hi - 1.f) + n2.lo);
-  float e01 = 0.5f * (g01.hi + g01.lo), e02 = 0.5f * (g02.hi + g02.lo), e12 = 0.5f * (g12.hi + g12.lo);
-  float nanv = __int_as_float(0x7FC00000);
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    E.V[i][0] = self(bad, nanv, v[i] - (v[i] * e00 + r1[i] * e01 + r2[i] * e02));
-    E.V[i][1] = self(bad, nanv, r1[i] - (v[i] * e01 + r1[i] * e11 + r2[i] * e12));
-    E.V[i][2] = self(bad, nanv, r2[i] - (v[i] * e02 + r1[i] * e12 + r2[i] * e22));
-  }
-  if (bad) {
-#pragma unroll
-    for (int i = 0; i < 3; i++) E.lam[i] = E.xd[i] = {nanv, nanv};
-  }
-}
-
-// Voigt input (FP32 values)
-MF_D void voigt_in_f(const float *xi, SmfInF &in) {
-#pragma unroll
-  for (int i = 0; i < 3; i++) in.d[i] = xi[i];
-#pragma unroll
-  for (int k = 0; k < 3; k++) in.o[k] = {xi[3 + k], 0.f};
-}
-
-// symmetric part of an FP32 3x3 matrix: the off-diagonal averages exactly as float-float; all NaN if
-// |a_ij - a_ji| > 1e-8 max |a_kl| (smf_kernel.hpp:408-421)
-MF_D void sym_in_f(const float *xi, SmfInF &in) {
-  float mx = 0.f;
-#pragma unroll
-  for (int k = 0; k < 9; k++) mx = fmaxf(mx, fabsf(xi[k]));
-  const float tol = 1e-8f * mx;
-  const bool sym = !(fabsf(xi[1] - xi[3]) > tol) & !(fabsf(xi[2] - xi[6]) > tol) & !(fabsf(xi[5] - xi[7]) > tol);
-  const float nanv = __int_as_float(0x7FC00000);
-  in.d[0] = self(sym, xi[0], nanv); in.d[1] = self(sym, xi[4], nanv); in.d[2] = self(sym, xi[8], nanv);
-  const int ia[3] = {1, 2, 5}, ib[3] = {3, 6, 7};
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    ffl t = two_sum(xi[ia[k]], xi[ib[k]]);
-    in.o[k] = {self(sym, 0.5f * t.hi, nanv), self(sym, 0.5f * t.lo, nanv)};
-  }
-}
-
-// the spectrum of the mixed path, eigenvalues sorted ascending: FP32 eigenvectors V (columns), eigenvalues lf,
-// their differences taken in float-float and rounded once (d10 = l1 - l0, d21, d20), and f(lambda) (log near the
-// mean through log1p of the deviator's eigenvalue, smf_kernel.hpp:283-290); powers see max(lambda, 0)
-struct SmfSpecF {
-  float lf[3], fl[3], V[3][3], d10, d21, d20;
-};
-
-MF_D bool ff_less(ffl a, ffl b) { return (a.hi < b.hi) | ((a.hi == b.hi) & (a.lo < b.lo)); }
-
-template <int KIND, bool LO>
-MF_D void smf_spectrum_f(const SmfInF &in, const SmfCoefF &C, SmfSpecF &Sp) {
-  SmfEigF E;
-  smf_eigsys_ff<KIND, LO>(in, E);
-  ffl lam[3] = {E.lam[0], E.lam[1], E.lam[2]}, xd[3] = {E.xd[0], E.xd[1], E.xd[2]};
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) Sp.V[i][j] = E.V[i][j];
-#pragma unroll
-  for (int st = 0; st < 3; st++) {  // sort ascending: a static order for every divided difference
-    const int a = st == 1 ? 1 : 0, b = a + 1;
-    bool sw = ff_less(lam[b], lam[a]);
-    ffl la = lam[a], lb = lam[b], xa = xd[a], xb = xd[b];
-    lam[a] = ff_sel(sw, lb, la); lam[b] = ff_sel(sw, la, lb);
-    xd[a] = ff_sel(sw, xb, xa); xd[b] = ff_sel(sw, xa, xb);
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-      float va = Sp.V[r][a], vb = Sp.V[r][b];
-      Sp.V[r][a] = self(sw, vb, va); Sp.V[r][b] = self(sw, va, vb);
-    }
-  }
-  if (KIND == POW || KIND == SQRT) {
-#pragma unroll
-    for (int i = 0; i < 3; i++) lam[i] = ff_sel(ff_less(ffl{0.f, 0.f}, lam[i]), lam[i], ffl{0.f, 0.f});
-  }
-#pragma unroll
-  for (int i = 0; i < 3; i++) Sp.lf[i] = lam[i].hi;
-  ffl t10 = ff_sub(lam[1], lam[0]), t21 = ff_sub(lam[2], lam[1]), t20 = ff_sub(lam[2], lam[0]);
-  Sp.d10 = t10.hi + t10.lo; Sp.d21 = t21.hi + t21.lo; Sp.d20 = t20.hi + t20.lo;
-#pragma unroll
-  for (int i = 0; i < 3; i++) Sp.fl[i] = fun_f<KIND>(Sp.lf[i], C.al);
-  if (KIND == LOG) {
-    float mf = E.m, lms = logf(mf);
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      float x = xd[i].hi + xd[i].lo;
-      Sp.fl[i] = self(fabsf(x) <= 0.5f * mf, lms + log1pf(x / mf), Sp.fl[i]);
-    }
-  }
-}
-
-// first divided differences D_ij = f[l_i, l_j] (D_ii = f'(l_i)) in FP32
-template <int KIND>
-MF_D void smf_dm_f(const SmfSpecF &Sp, const SmfCoefF &C, float Dm[3][3]) {
-  const float D01 = dd1s_f<KIND>(Sp.lf[0], Sp.lf[1], Sp.d10, Sp.fl[0], Sp.fl[1], C);
-  const float D02 = dd1s_f<KIND>(Sp.lf[0], Sp.lf[2], Sp.d20, Sp.fl[0], Sp.fl[2], C);
-  const float D12 = dd1s_f<KIND>(Sp.lf[1], Sp.lf[2], Sp.d21, Sp.fl[1], Sp.fl[2], C);
-  Dm[0][0] = deriv_f<KIND>(Sp.lf[0], Sp.fl[0], C); Dm[1][1] = deriv_f<KIND>(Sp.lf[1], Sp.fl[1], C);
-  Dm[2][2] = deriv_f<KIND>(Sp.lf[2], Sp.fl[2], C);
-  Dm[0][1] = Dm[1][0] = D01; Dm[0][2] = Dm[2][0] = D02; Dm[1][2] = Dm[2][1] = D12;
-}
-
-// second divided differences D2_ijl = f[l_i, l_j, l_l] (symmetric) in FP32
-template <int KIND>
-MF_D void smf_d2_f(const SmfSpecF &Sp, const float Dm[3][3], const SmfCoefF &C, float D2[3][3][3]) {
-  const float dd[3][3] = {{0.f, Sp.d10, Sp.d20}, {0.f, 0.f, Sp.d21}, {0.f, 0.f, 0.f}};
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = i; j < 3; j++)
-#pragma unroll
-      for (int l = j; l < 3; l++) {
-        const float d = (i == j && j == l)
-                            ? dd2_same_f<KIND>(Sp.lf[i], Sp.fl[i], Dm[i][i], C)
-                            : dd2s_f<KIND>(Sp.lf[j], Sp.lf[l], Sp.fl[j], Dm[i][j], Dm[j][l], dd[i][j], dd[j][l],
-                                           dd[i][l], C);
-        D2[i][j][l] = D2[i][l][j] = D2[j][i][l] = D2[j][l][i] = D2[l][i][j] = D2[l][j][i] = d;
-      }
-}
 
 constexpr int SMFX_TPB = 64;  // matrices per CTA of the standalone kernel
 
@@ -627,17 +205,6 @@ __global__ void __launch_bounds__(SMFX_TPB) smf_mixed_kernel(int64_t n, const fl
   __shared__ SmfxTileSmem<ORDER, MAT, SMFX_TPB> TS;
   const int64_t base = (int64_t)blockIdx.x * SMFX_TPB;
   smf_mixed_tile<KIND, ORDER, MAT, SMFX_TPB>(base, (int)min((int64_t)SMFX_TPB, n - base), x, F, J, H, C, TS);
-}
-
-inline void smf_coef_f(int kind, double al, SmfCoefF &C) {
-  SmfCoef D;
-  smf_coef(kind, al, D);
-  C.al = (float)al;
-  C.alm1 = (float)(al - 1.0);
-  C.zp1 = (float)D.zp1;
-  C.z2 = (float)D.z2;
-  C.tau = (float)D.tau;
-  for (int k = 0; k < DD2_TERMS; k++) C.c2[k] = (float)D.c2[k];
 }
 
 template <int KIND>

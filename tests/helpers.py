@@ -44,3 +44,19 @@ def voigt_to_matrix(v):
     A[..., 0, 2] = A[..., 2, 0] = v[..., 4]
     A[..., 1, 2] = A[..., 2, 1] = v[..., 5]
     return A
+
+
+def near_isotropic_f32():
+    """FP32 matrices within 2^-30 .. 2^-70 of a multiple of I: c (I + 2^-e S), S symmetric with zero diagonal (the
+    deviator exactly representable in FP32), and row 29913 of C0 (n = 65536, seed 4), whose FP32 eigenvectors came out
+    of the general path of smf_eigsys_ff 0.6 % from orthonormal on GB300 (F 3e-3 from the oracle)"""
+    from matfun_gb300 import workloads as w
+    rng = np.random.default_rng(29913)
+    parts = [w.c0_smf_spd(65536, seed=4, as_voigt=False)[29913:29914]]
+    for e in (30, 39, 41, 52, 60, 70):
+        c = np.exp(rng.uniform(-2, 2, 256))
+        S = rng.standard_normal((256, 3, 3))
+        S = S + S.transpose(0, 2, 1)
+        S[:, [0, 1, 2], [0, 1, 2]] = 0.0
+        parts.append(c[:, None, None] * (np.eye(3) + 2.0 ** -e * S))
+    return np.concatenate(parts).astype(np.float32)

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from tests import oracle_lib as ol
-from tests.helpers import maxrel
+from tests.helpers import maxrel, near_isotropic_f32
 
 pytestmark = pytest.mark.gpu
 KINDS = [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3"), (2, 0.7, "pow 0.7")]
@@ -73,22 +73,6 @@ def test_smf_mixed_c0_and_golden_inputs():
     sel = (g["kind"] == 1) & (np.abs(g["x"]).max(axis=1) < 1e30) & (np.abs(g["x"]).max(axis=1) > 1e-30)
     errs, _, _ = errors(False, 1, 0.0, g["x"][sel].astype(np.float32), 2)
     assert max(errs) <= 1e-5
-
-
-def near_isotropic_f32():
-    """FP32 matrices within 2^-30 .. 2^-70 of a multiple of I: c (I + 2^-e S), S symmetric with zero diagonal (the
-    deviator exactly representable in FP32), and row 29913 of C0 (n = 65536, seed 4), whose FP32 eigenvectors came out
-    of the general path of smf_eigsys_ff 0.6 % from orthonormal on GB300 (F 3e-3 from the oracle)"""
-    from matfun_gb300 import workloads as w
-    rng = np.random.default_rng(29913)
-    parts = [w.c0_smf_spd(65536, seed=4, as_voigt=False)[29913:29914]]
-    for e in (30, 39, 41, 52, 60, 70):
-        c = np.exp(rng.uniform(-2, 2, 256))
-        S = rng.standard_normal((256, 3, 3))
-        S = S + S.transpose(0, 2, 1)
-        S[:, [0, 1, 2], [0, 1, 2]] = 0.0
-        parts.append(c[:, None, None] * (np.eye(3) + 2.0 ** -e * S))
-    return np.concatenate(parts).astype(np.float32)
 
 
 @pytest.mark.xfail(strict=False, reason="the near-isotropic branch of smf_eigsys_ff has been checked on the CPU only")

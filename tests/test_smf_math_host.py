@@ -1,0 +1,115 @@
+"""The per-matrix math of the symmetric family, held against the oracle on the CPU.
+
+The eigensystem, f of the eigenvalues and the first / second divided differences that the smf kernels evaluate per
+thread (FP32 mixed form: matfun_gb300/csrc/smf_mixed_math.cuh; FP64 form: smf_device.cuh) are compiled for the host
+from the same headers with g++ (tests/host_math/smf_math_host.cc; host_intrinsics.h supplies the six CUDA intrinsics
+they use as exact host functions).  F, J and H are assembled from V, f(lambda), D and D2 in NumPy by the spectral
+(Daleckii-Krein) formulas and compared with the oracle's smf_eval_matrix:
+
+    F            = V diag(f) V^T
+    J[ij, kl]    = sum_ab V_ia V_jb D_ab Xt_kl,ab,                         Xt_kl = V^T (E_kl + E_lk) / 2 V
+    H[ij, kl, pq] = sum_abc V_ia V_jb D2_acb (Xt_kl,ac Xt_pq,cb + Xt_pq,ac Xt_kl,cb)
+
+This checks the math without a GPU (the device's own math library and the tile's FP32 assembly are checked by the
+GPU tests).  Bounds: 1e-6 for the FP32 form (max |x - ref| / max |ref| per array, as tests/test_mixed_gpu.py), 1e-12
+for the FP64 form (as tests/test_parity_gpu.py)."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests import oracle_lib as ol
+from tests.helpers import maxrel, near_isotropic_f32
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KINDS = [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3"), (2, 0.7, "pow 0.7")]
+P = ctypes.c_void_p
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    cxx = shutil.which("g++")
+    inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    if cxx is None or not os.path.exists(os.path.join(inc, "cuda_runtime.h")):
+        pytest.skip("g++ or the CUDA headers are missing")
+    out = str(tmp_path_factory.mktemp("host_math") / "libsmf_math_host.so")
+    src = os.path.join(HERE, "host_math", "smf_math_host.cc")
+    r = subprocess.run([cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-I" + inc, src, "-o", out],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    L = ctypes.CDLL(out)
+    L.smf_math_f32.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int64] + [P] * 6
+    L.smf_math_f64.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [P] * 6
+    L.smf_math_f32.restype = L.smf_math_f64.restype = ctypes.c_int
+    return L
+
+
+def spectra(L, kind, alpha, X, f32, mat=True):
+    n = len(X)
+    dt = np.float32 if f32 else np.float64
+    X = np.ascontiguousarray(X, dtype=dt)
+    lam, fl = np.empty((n, 3), dt), np.empty((n, 3), dt)
+    V, D, D2 = np.empty((n, 3, 3), dt), np.empty((n, 3, 3), dt), np.empty((n, 3, 3, 3), dt)
+    outs = [a.ctypes.data for a in (lam, fl, V, D, D2)]
+    if f32:
+        assert L.smf_math_f32(kind, alpha, int(mat), n, X.ctypes.data, *outs) == 0
+    else:
+        assert L.smf_math_f64(kind, alpha, n, X.ctypes.data, *outs) == 0
+    return [a.astype(np.float64) for a in (lam, fl, V, D, D2)]
+
+
+def assemble(fl, V, D, D2):
+    """F (n, 9), J (n, 81), H (n, 729) in the matrix layout of smf_eval_matrix"""
+    n = len(V)
+    F = np.einsum("nia,na,nja->nij", V, fl, V)
+    Xt = 0.5 * (np.einsum("nka,nlb->nklab", V, V) + np.einsum("nla,nkb->nklab", V, V)).reshape(n, 9, 3, 3)
+    J = np.einsum("nia,njb,nab,nKab->nijK", V, V, D, Xt, optimize=True)
+    M = np.einsum("nacb,nKac,nPcb->nKPab", D2, Xt, Xt, optimize=True)
+    H = np.einsum("nia,njb,nKPab->nijKP", V, V, M + M.transpose(0, 2, 1, 3, 4), optimize=True)
+    return F.reshape(n, 9), J.reshape(n, 81), H.reshape(n, 729)
+
+
+def voigt(A):
+    return np.stack([A[:, 0, 0], A[:, 1, 1], A[:, 2, 2], A[:, 0, 1], A[:, 0, 2], A[:, 1, 2]], axis=1)
+
+
+def inputs():
+    from matfun_gb300 import workloads as w
+    return {
+        "C2": w.c2_smf_spd(2000, seed=31, as_voigt=False),
+        "C0": w.c0_smf_spd(2000, seed=32, as_voigt=False),
+        "near-isotropic": near_isotropic_f32().astype(np.float64),
+    }
+
+
+@pytest.mark.parametrize("kind,alpha,name", KINDS)
+def test_fp32_math_against_oracle(lib, kind, alpha, name):
+    for case, A in inputs().items():
+        A32 = A.astype(np.float32)
+        ref = ol.call(ol.oracle(), "smf_eval_matrix", kind, alpha, A32.astype(np.float64).reshape(-1, 9), 2, 9)[1:]
+        for layout, X in (("matrix", A32.reshape(-1, 9)), ("Voigt", voigt(A32))):
+            _, fl, V, D, D2 = spectra(lib, kind, alpha, X, True, mat=layout == "matrix")
+            errs = [maxrel(g, r) for g, r in zip(assemble(fl, V, D, D2), ref)]
+            print(f"FP32 smf math, {name}, {case}, {layout}: max rel F J H {['%.1e' % e for e in errs]}")
+            assert max(errs) <= 1e-6, (case, layout, errs)
+
+
+def test_fp32_near_isotropic_row_is_isotropic(lib):
+    """C0 row 29913 (deviator 2^-54 |A|): the identity as eigenvectors and the equal diagonal entries as eigenvalues"""
+    A = near_isotropic_f32()[:1]
+    lam, _, V, _, _ = spectra(lib, 1, 0.0, A.reshape(1, 9), True)
+    assert np.array_equal(V[0], np.eye(3))
+    assert np.all(lam[0] == A[0, 0, 0])
+
+
+@pytest.mark.parametrize("kind,alpha,name", KINDS)
+def test_fp64_math_against_oracle(lib, kind, alpha, name):
+    for case, A in inputs().items():
+        ref = ol.call(ol.oracle(), "smf_eval_matrix", kind, alpha, A.reshape(-1, 9), 2, 9)[1:]
+        _, fl, V, D, D2 = spectra(lib, kind, alpha, voigt(A), False)
+        errs = [maxrel(g, r) for g, r in zip(assemble(fl, V, D, D2), ref)]
+        print(f"FP64 smf math, {name}, {case}: max rel F J H {['%.1e' % e for e in errs]}")
+        assert max(errs) <= 1e-12, (case, errs)
