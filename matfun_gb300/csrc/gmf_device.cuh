@@ -31,6 +31,37 @@ struct GmfCoef {
                           // that 4^j / j! stays in FP32's range; log, pow: 0)
 };
 
+// host: launch constants (series coefficients gmf_kernel.hpp:48-53; the binomial factors of the term bound by the
+// recurrence of gmf_kernel.hpp:84, as log2 values)
+inline void gmf_coef(int kind, double al, int order, GmfCoef &C) {
+  C.al = al;
+  C.rho_f = (kind == POW && 3.0 / al < G_RHO) ? 3.0 / al : G_RHO;
+  for (int k = 0; k < 3; k++) {
+    const double bh = al - k, bb = bh - al;
+    C.bh[k] = bh;
+    C.bl[k] = (al - (bh - bb)) + (-k - bb);
+  }
+  C.bt[0] = 1.0;
+  for (int j = 1; j < G_KMAX; j++)
+    C.bt[j] = kind == EXP ? C.bt[j - 1] / j : (kind == LOG ? (j % 2 ? 1.0 : -1.0) / j : C.bt[j - 1] * (al - j + 1) / j);
+  C.tsh = kind == EXP ? 2 : 0;
+  C.ffser = 1;
+  for (int j = 0; j < G_KMAX; j++) {
+    const double bs = std::ldexp(C.bt[j], C.tsh * j);
+    C.ffser &= std::fabs(bs) <= 0x1p100;  // (false for a NaN)
+    C.bth[j] = (float)bs;
+  }
+  for (int j = 0; j < G_KMAX; j++)
+    C.btl[j] = C.ffser ? (float)(std::ldexp(C.bt[j], C.tsh * j) - (double)C.bth[j]) : 0.f;
+  const int nn = 3 * (order + 1) - 1;
+  double c = 1.0;
+  for (int k = 0; k < G_KMAX; k++) {
+    const double t = nn + k < G_KMAX ? std::fabs(C.bt[nn + k]) * c : 0.0;
+    C.lterm[k] = t > 0 ? (float)std::log2(t) : -INFINITY;
+    c = c * (k + nn + 1) / (k + 1);
+  }
+}
+
 // the 19 divided differences f[x0^a x1^b x2^c], a >= b >= c, a >= 1, in lexicographic order of (a, b, c); each is
 // its parent with one node added (node 0 if a - 1 >= b, else node 1 if b - 1 >= c, else node 2)
 MF_D constexpr int gpos(int a, int b, int c) { return (a == 1 ? 0 : (a == 2 ? 3 : 9)) + b * (b + 1) / 2 + c; }

@@ -234,14 +234,7 @@ MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E) {
   for (int i = 0; i < 3; i++) kd = max(kd, __float_as_int(dv[i]) & 0x7FFFFFFF);
 #pragma unroll
   for (int k = 0; k < 3; k++) kd = max(kd, __float_as_int(o[k].hi) & 0x7FFFFFFF);
-  // A within 2^-40 of its largest entry (scaled into [1, 2)) of a multiple of I: its FP32 diagonal entries are then
-  // equal, and dropping the off-diagonal entries makes it isotropic (V = I, the diagonal as eigenvalues), which
-  // neglects less than 2^-40 |A| |f'| in F, far below FP32 output.  The rotation of the general path is not taken for
-  // these: on GB300 one such matrix (deviator 2^-54 |A|) came out of it with eigenvectors 0.6 % from orthonormal.
-  const bool flat = kd < ((127 - 40) << 23);
-#pragma unroll
-  for (int k = 0; k < 3; k++) o[k] = ff_sel(flat, ffl{0.f, 0.f}, o[k]);
-  const bool iso = flat | bad;
+  const bool iso = (kd == 0) | bad;
   const int ed = min(max((kd >> 23) & 0xFF, 1), 253);
   const float dsc = __int_as_float(ed << 23), ids = __int_as_float((254 - ed) << 23);
   float g0 = dv[0] * ids, g1 = dv[1] * ids, g2 = dv[2] * ids;
@@ -284,9 +277,20 @@ MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E) {
   const ffl qv = quad_ff<LO>(dg, o, v[0], v[1], v[2]), nv = dot_ff(v, v);
   const ffl b11 = quad_ff<LO>(dg, o, u[0], u[1], u[2]), b22 = quad_ff<LO>(dg, o, w[0], w[1], w[2]);
   const ffl b12 = bil_ff<LO>(dg, o, u, w);
-  // FP32 Jacobi rotation of the pair from the block (its entries are of the size of the pair's gap)
+  // FP32 Jacobi rotation of the pair from the block (its entries are of the size of the pair's gap).  The angle
+  // depends on jy / jx only, so both are scaled by a power of two into [1, 2) before they are squared: a gap below
+  // ~1e-19 of |A| would otherwise square into FP32's subnormal range, and the rounded jr would leave cos^2 + sin^2
+  // away from 1 by more than the Newton-Schulz step below repairs (1e-5 at a gap of 1e-22).  Where the squares are
+  // normal the scaling is exact and changes no bit of cos and sin.
   ffl jd = ff_sub(b11, b22);
-  float jx = jd.hi + jd.lo, jy = 2.f * (b12.hi + b12.lo), jr = sqrtf(jx * jx + jy * jy);
+  float jx = jd.hi + jd.lo, jy = 2.f * (b12.hi + b12.lo);
+  {
+    const int kj = max(__float_as_int(jx) & 0x7FFFFFFF, __float_as_int(jy) & 0x7FFFFFFF);
+    const float js = __int_as_float((254 - min(max((kj >> 23) & 0xFF, 1), 253)) << 23);
+    jx *= js;
+    jy *= js;
+  }
+  float jr = sqrtf(jx * jx + jy * jy);
   bool jz = !(jr > 0.f), jpos = jx >= 0.f;
   float jrs = self(jz, 1.f, jr);
   float big = sqrtf((jrs + fabsf(jx)) / (2.f * jrs)), sml = jy / (2.f * jrs * big);

@@ -48,11 +48,14 @@ def voigt_to_matrix(v):
 
 def near_isotropic_f32():
     """FP32 matrices within 2^-30 .. 2^-70 of a multiple of I: c (I + 2^-e S), S symmetric with zero diagonal (the
-    deviator exactly representable in FP32), and row 29913 of C0 (n = 65536, seed 4), whose FP32 eigenvectors came out
-    of the general path of smf_eigsys_ff 0.6 % from orthonormal on GB300 (F 3e-3 from the oracle)"""
+    deviator exactly representable in FP32); row 29913 of C0 (n = 65536, seed 4), whose FP32 eigenvectors came out of
+    smf_eigsys_ff 0.6 % from orthonormal on GB300 (F 3e-3 from the oracle); and row 31949 of C0 (n = 50000, seed 6),
+    a triple eigenvalue rounded to FP32, whose pair's Jacobi block squared into FP32's subnormal range before that
+    block was scaled (H 2e-2 from the oracle)"""
     from matfun_gb300 import workloads as w
     rng = np.random.default_rng(29913)
-    parts = [w.c0_smf_spd(65536, seed=4, as_voigt=False)[29913:29914]]
+    parts = [w.c0_smf_spd(65536, seed=4, as_voigt=False)[29913:29914],
+             w.c0_smf_spd(50000, seed=6, as_voigt=False)[31949:31950]]
     for e in (30, 39, 41, 52, 60, 70):
         c = np.exp(rng.uniform(-2, 2, 256))
         S = rng.standard_normal((256, 3, 3))

@@ -1,0 +1,124 @@
+"""Phase A of the gmf kernels, held against the oracle and the golden cases on the CPU.
+
+The per-matrix record of the general family (scaling, closed-form roots, pair refinement, branch-cut pair, groups, the
+confluent group series; F, the real basis r1, r2, the reduced divided differences D2', D3' and the factors sc1, sc2:
+matfun_gb300/csrc/gmf_device.cuh) is compiled for the host from the kernels' own header with g++
+(tests/host_math/gmf_math_host.cc; host_intrinsics.h supplies the CUDA intrinsics and a one-lane warp vote).  NumPy
+then contracts the record into J and H as phase B of the kernels does (r_0 = I, x, y, z = 3a + c):
+
+    J_abcd   = sc1 T4[ac, db],                          T4[x, y]    = sum_mn  r_m[x] D2'_mn r_n[y]
+    H_abcdef = sc2 (T6[ac, de, fb] + T6[ae, fc, db]),   T6[x, y, z] = sum_mnp r_m[x] r_n[y] r_p[z] D3'_mnp
+
+Bounds: the FP64 record within 1e-12 of the oracle (as tests/test_parity_gpu.py) and every golden case of the reference
+within its own tolerance; the float-float group series of the FP32-storage kernels within 1e-10, four orders of
+magnitude below FP32 rounding, on C1 and on the FP32-rounded golden inputs.  Phase B's own arithmetic, the CTA-local
+orderings and the device's math library are left to the GPU tests."""
+import ctypes
+import itertools
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests import oracle_lib as ol
+from tests.helpers import maxrel
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KINDS = [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3")]
+S2 = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
+S3 = [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 1), (0, 0, 2), (0, 1, 2), (1, 1, 2), (0, 2, 2), (1, 2, 2), (2, 2, 2)]
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    cxx = shutil.which("g++")
+    inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    if cxx is None or not os.path.exists(os.path.join(inc, "cuda_runtime.h")):
+        pytest.skip("g++ or the CUDA headers are missing")
+    out = str(tmp_path_factory.mktemp("host_math") / "libgmf_math_host.so")
+    src = os.path.join(HERE, "host_math", "gmf_math_host.cc")
+    r = subprocess.run([cxx, "-std=c++17", "-O1", "-fPIC", "-shared", "-I" + inc, src, "-o", out],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    L = ctypes.CDLL(out)
+    L.gmf_math.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int64] + \
+        [ctypes.c_void_p] * 6
+    L.gmf_math.restype = ctypes.c_int
+    return L
+
+
+def record(L, kind, alpha, order, ff, A):
+    n = len(A)
+    A = np.ascontiguousarray(A, dtype=np.float64).reshape(n, 9)
+    F, R12, D2, D3, sc = np.empty((n, 9)), np.empty((n, 18)), np.empty((n, 6)), np.empty((n, 10)), np.empty((n, 2))
+    assert L.gmf_math(kind, alpha, order, ff, n, *[x.ctypes.data for x in (A, F, R12, D2, D3, sc)]) == 0
+    return F, R12, D2, D3, sc
+
+
+def contract(order, F, R12, D2, D3, sc):
+    """F (n, 9), J (n, 81), H (n, 729) in the layout of gmf_eval, up to the order"""
+    n = len(F)
+    r = np.empty((n, 3, 3, 3))
+    r[:, 0] = np.eye(3)
+    r[:, 1], r[:, 2] = R12[:, :9].reshape(n, 3, 3), R12[:, 9:].reshape(n, 3, 3)
+    d2 = np.empty((n, 3, 3))
+    for k, (a, b) in enumerate(S2):
+        d2[:, a, b] = d2[:, b, a] = D2[:, k]
+    out = [F]
+    if order >= 1:
+        T4 = np.einsum("nmac,nmk,nkdb->nacdb", r, d2, r)
+        out.append(sc[:, :1] * np.einsum("nacdb->nabcd", T4).reshape(n, 81))
+    if order >= 2:
+        d3 = np.empty((n, 3, 3, 3))
+        for k, t in enumerate(S3):
+            for p in set(itertools.permutations(t)):
+                d3[:, p[0], p[1], p[2]] = D3[:, k]
+        T6 = np.einsum("nmac,nkde,npfb,nmkp->nacdefb", r, r, r, d3, optimize=True)
+        H = np.einsum("nacdefb->nabcdef", T6) + np.einsum("naefcdb->nabcdef", T6)
+        out.append(sc[:, 1:] * H.reshape(n, 729))
+    return out
+
+
+@pytest.mark.parametrize("kind,alpha,name", KINDS)
+@pytest.mark.parametrize("order", [0, 1, 2])
+def test_fp64_record_c1(lib, kind, alpha, name, order):
+    from matfun_gb300 import workloads as w
+    A = w.c1_gmf_groups(2000, seed=3 + order).reshape(-1, 9)
+    ref = ol.call(ol.oracle(), "gmf_eval", kind, alpha, A, order, 9)[1:order + 2]
+    got = contract(order, *record(lib, kind, alpha, order, 0, A))
+    errs = [maxrel(g, r) for g, r in zip(got, ref)]
+    print(f"gmf phase A on the host, {name}, order {order}: max rel F J H {['%.1e' % e for e in errs]}")
+    assert max(errs) <= 1e-12
+
+
+@pytest.mark.parametrize("kind,alpha,name", KINDS[1:])
+def test_ff_series_c1(lib, kind, alpha, name):
+    """the float-float group series (log and pow only: exp keeps its split FP64 series in every form)"""
+    from matfun_gb300 import workloads as w
+    A = w.c1_gmf_groups(2000, seed=9).reshape(-1, 9)
+    ref = ol.call(ol.oracle(), "gmf_eval", kind, alpha, A, 2, 9)[1:]
+    got = contract(2, *record(lib, kind, alpha, 2, 1, A))
+    errs = [maxrel(g, r) for g, r in zip(got, ref)]
+    print(f"gmf float-float series on the host, {name}: max rel F J H {['%.1e' % e for e in errs]}")
+    assert max(errs) <= 1e-10
+
+
+@pytest.mark.parametrize("fixture,ff,bound", [("cases_gmf.npz", 0, None), ("cases_gmf_f32.npz", 1, 1e-10)])
+def test_golden_cases(lib, fixture, ff, bound):
+    """every golden gmf case of the reference: the FP64 record within the case's tolerance; the float-float series on
+    the FP32-rounded inputs within 1e-10 of the oracle's results for those inputs"""
+    g = np.load(os.path.join(HERE, "golden", fixture))
+    worst = 0.0
+    for kind in np.unique(g["kind"]):
+        for alpha in np.unique(g["alpha"][g["kind"] == kind]):
+            sel = np.where((g["kind"] == kind) & (g["alpha"] == alpha))[0]
+            got = contract(2, *record(lib, int(kind), float(alpha), 2, ff, g["x"][sel].astype(np.float64)))
+            for row, i in enumerate(sel):
+                for arr, name in zip(got, "FJH"):
+                    e = maxrel(arr[row], g[name][i])
+                    tol = g["tol"][i] if bound is None else bound
+                    worst = max(worst, e / tol)
+                    assert e <= tol, f"case {i} (kind {kind}, alpha {alpha}) {name}: {e:.2e} > {tol:.0e}"
+    print(f"{fixture}, {'float-float' if ff else 'FP64'} series: worst {worst:.2f} of the bound")

@@ -75,7 +75,8 @@ def test_smf_mixed_c0_and_golden_inputs():
     assert max(errs) <= 1e-5
 
 
-@pytest.mark.xfail(strict=False, reason="the near-isotropic branch of smf_eigsys_ff has been checked on the CPU only")
+@pytest.mark.xfail(strict=False, reason="not yet run on a GPU since the Jacobi block of smf_eigsys_ff is scaled; "
+                   "C0 row 29913 failed on GB300 before, for a cause the host build does not reproduce")
 @pytest.mark.parametrize("kind,alpha,name", KINDS)
 def test_smf_mixed_near_isotropic(kind, alpha, name):
     A = near_isotropic_f32()
@@ -85,7 +86,8 @@ def test_smf_mixed_near_isotropic(kind, alpha, name):
     assert max(errs) <= TOL and max(row) <= TOL
 
 
-@pytest.mark.xfail(strict=False, reason="the near-isotropic branch of smf_eigsys_ff has been checked on the CPU only")
+@pytest.mark.xfail(strict=False, reason="not yet run on a GPU since the Jacobi block of smf_eigsys_ff is scaled; "
+                   "C0 row 29913 failed on GB300 before, for a cause the host build does not reproduce")
 def test_smf_mixed_adjoint_near_isotropic():
     """the FP32 VJP against the FP64 one on the same FP32 inputs (log: on a multiple of I, Abar = sym(W) / c)"""
     import torch
