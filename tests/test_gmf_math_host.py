@@ -122,3 +122,58 @@ def test_golden_cases(lib, fixture, ff, bound):
                     worst = max(worst, e / tol)
                     assert e <= tol, f"case {i} (kind {kind}, alpha {alpha}) {name}: {e:.2e} > {tol:.0e}"
     print(f"{fixture}, {'float-float' if ff else 'FP64'} series: worst {worst:.2f} of the bound")
+
+
+def stress_sets(n, seed=21):
+    """general matrices the workloads do not stress: Gaussian (real eigenvalues <= 0: NaN for log, sqrt, pow), Jordan
+    blocks of size 3 and 2 perturbed by 1e-4 .. 1e-15, complex pairs at angles up to 3.1415 from the positive axis
+    (next to the branch cut), near-singular matrices and matrices scaled by 2^-60 and 2^60; similarity transforms by
+    well-conditioned S = N(0, 1) + 3 I"""
+    rng = np.random.default_rng(seed)
+
+    def conj(M):
+        S = rng.standard_normal((len(M), 3, 3)) + 3 * np.eye(3)
+        return S @ M @ np.linalg.inv(S)
+
+    sets = {"gaussian": rng.standard_normal((n, 3, 3)), "gaussian + 3I": rng.standard_normal((n, 3, 3)) + 3 * np.eye(3)}
+    for eps in (1e-4, 1e-8, 1e-12, 1e-15):
+        c = np.exp(rng.uniform(-1, 1, n))
+        J = np.zeros((n, 3, 3))
+        J[:, [0, 1, 2], [0, 1, 2]] = c[:, None]
+        J[:, 0, 1] = J[:, 1, 2] = 1.0
+        sets[f"Jordan 3 + {eps:.0e}"] = conj(J + eps * rng.standard_normal((n, 3, 3)))
+        J2 = np.zeros((n, 3, 3))
+        J2[:, [0, 1], [0, 1]] = c[:, None]
+        J2[:, 0, 1] = 1.0
+        J2[:, 2, 2] = np.exp(rng.uniform(-1, 1, n))
+        sets[f"Jordan 2 + {eps:.0e}"] = conj(J2 + eps * rng.standard_normal((n, 3, 3)))
+    for th in (3.0, 3.14, 3.1415):
+        r, t = np.exp(rng.uniform(-1, 1, n)), th * rng.choice([-1.0, 1.0], n)
+        M = np.zeros((n, 3, 3))
+        M[:, 0, 0] = M[:, 1, 1] = r * np.cos(t)
+        M[:, 0, 1], M[:, 1, 0] = -r * np.sin(t), r * np.sin(t)
+        M[:, 2, 2] = np.exp(rng.uniform(-1, 1, n))
+        sets[f"pair angle {th}"] = conj(M)
+    for s in (1e-8, 1e-12):
+        D = np.exp(rng.uniform(-1, 1, (n, 3)))
+        D[:, 0] = s
+        sets[f"near-singular {s:.0e}"] = conj(np.einsum("na,ab->nab", D, np.eye(3)))
+    for k in (-60, 60):
+        sets[f"scale 2^{k}"] = (rng.standard_normal((n, 3, 3)) + 3 * np.eye(3)) * 2.0 ** k
+    return sets
+
+
+@pytest.mark.parametrize("kind,alpha,name", KINDS + [(2, 2.5, "pow 2.5")])
+def test_fp64_record_stress(lib, kind, alpha, name):
+    """the FP64 record on the stress sets: within 1e-12 of the oracle per set, NaN exactly where the oracle has NaN"""
+    for sname, A in stress_sets(300).items():
+        X = A.reshape(-1, 9)
+        ref = ol.call(ol.oracle(), "gmf_eval", kind, alpha, X, 2, 9)[1:]
+        got = contract(2, *record(lib, kind, alpha, 2, 0, X))
+        for g, r, out in zip(got, ref, "FJH"):
+            assert np.array_equal(np.isnan(g), np.isnan(r)), (sname, out)
+        if kind == 0 and sname == "scale 2^60":  # exp overflows there in any precision: the same entries overflow
+            assert all(np.array_equal(np.isinf(g), np.isinf(r)) for g, r in zip(got, ref)), sname
+            continue
+        errs = [maxrel(g, r) for g, r in zip(got, ref)]
+        assert max(errs) <= 1e-12, (sname, errs)

@@ -154,3 +154,37 @@ def test_golden_cases(lib, fixture, f32):
                     worst = max(worst, e / g["tol"][i])
                     assert e <= g["tol"][i], f"case {i} (kind {kind}, alpha {alpha}) {name}: {e:.2e}"
     print(f"{fixture}, {'FP32' if f32 else 'FP64'} math: worst {worst:.2f} of the case tolerance")
+
+
+def stress_sets_spd(n, seed=11):
+    """symmetric positive definite matrices the workloads do not stress: scaled by 2^-100 .. 2^100, pairs with relative
+    gaps 1e-4 .. 1e-30, triples spread by 1e-6 .. 1e-20, condition number 1e6 (random rotations)"""
+    rng = np.random.default_rng(seed)
+
+    def spd(lam):
+        Q, _ = np.linalg.qr(rng.standard_normal((len(lam), 3, 3)))
+        return np.einsum("nia,na,nja->nij", Q, lam, Q)
+
+    base = np.exp(rng.uniform(-1, 1, (n, 3)))
+    sets = {f"scale 2^{k}": spd(base) * 2.0 ** k for k in (-100, -60, -20, 20, 60, 100)}
+    for g in (1e-4, 1e-8, 1e-12, 1e-16, 1e-20, 1e-30):
+        c, d = np.exp(rng.uniform(-1, 1, n)), np.exp(rng.uniform(-1, 1, n))
+        sets[f"pair gap {g:.0e}"] = spd(np.stack([c, c * (1 + g), d], 1))
+    for g in (1e-6, 1e-10, 1e-20):
+        c = np.exp(rng.uniform(-1, 1, n))
+        sets[f"triple spread {g:.0e}"] = spd(np.stack([c, c * (1 + g), c * (1 + 2 * g)], 1))
+    sets["cond 1e6"] = spd(np.stack([np.ones(n), np.exp(rng.uniform(0, np.log(1e6), n)), 1e6 * np.ones(n)], 1))
+    return sets
+
+
+@pytest.mark.parametrize("kind,alpha,name", KINDS)
+def test_fp64_math_stress(lib, kind, alpha, name):
+    """the FP64 math on the stress sets within 1e-12 of the oracle (exp: only where exp of the spectrum is finite)"""
+    for sname, A in stress_sets_spd(200).items():
+        if kind == 0 and np.abs(A).max() > 80:  # exp overflows there in any precision
+            continue
+        A = 0.5 * (A + A.transpose(0, 2, 1))
+        ref = ol.call(ol.oracle(), "smf_eval_matrix", kind, alpha, A.reshape(-1, 9), 2, 9)[1:]
+        _, fl, V, D, D2 = spectra(lib, kind, alpha, voigt(A), False)
+        errs = [maxrel(g, r) for g, r in zip(assemble(fl, V, D, D2), ref)]
+        assert max(errs) <= 1e-12, (sname, errs)
