@@ -31,7 +31,6 @@ METRIC = "gmf log order-2 matrices/s (FP64)"
 # FP64 floating-point operations per matrix of one order-2 call on this workload (2 per DFMA): the ordered gmf_kernel
 # <LOG, 2> (DFMA 2355, DADD 1006, DMUL 723) plus gmf_key_kernel (the closed-form roots: 144, 64, 76), from the ncu
 # counters smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum at n = 262144
-# (profiles/gmf_kernel_log_o2_c1.md)
 FP64_FLOP_PER_MATRIX = {"log": 2 * (2355 + 144) + (1006 + 64) + (723 + 76)}
 # DRAM bytes per matrix of the ordered gmf_kernel<LOG, 2> launch from one ncu capture at n = 262144 on the same
 # workload (101.4 MB read + 1752.0 MB written for 259 584 matrices; the algorithmic bytes are 6624 per matrix, the
