@@ -179,6 +179,15 @@ int smf_xla_ffi_api_version(void);
  * in TFLOP/s, the bound of the FP64 kernels of this library.  Returns 0, or -1 / -2 like the entry points above. */
 int matfun_cuda_fp64_peak(double *tflops);
 
+/* Diagnostic (no counterpart in the reference): the FP32 symmetric eigensystem of smf_cuda_eval_f32 /
+ * smf_cuda_eval_matrix_f32 on n matrices (mat: 9-entry rows, else Voigt 6-vectors), 64 floats per matrix into out:
+ * its intermediate values (0-43: the normalised deviator g0..g5, p, q, r, the root, v, u, w, the shift, the 2x2
+ * block b11, b22, b12 as float-float, jx, jy, jr, cos, sin, the squared norms of v, r1, r2 as float-float, the Gram
+ * entries, the mean as float-float, the deviator's scale and its bit pattern) and results (44-49 eigenvalues as
+ * float-float, 50-58 V row-major, 59-61 the deviator's eigenvalues, 62 the mean), asynchronous on the stream.
+ * Returns 0, -1 (n < 0 or a NULL array with n > 0), -2 (CUDA error). */
+int matfun_cuda_smf_f32_probe(int mat, int64_t n, const float *x, float *out, void *stream);
+
 /* version string of this library (no counterpart in the reference's CUDA header; cf. smf_version, matfun.h:51) */
 const char *matfun_cuda_version(void);
 

@@ -63,3 +63,22 @@ def near_isotropic_f32():
         S[:, [0, 1, 2], [0, 1, 2]] = 0.0
         parts.append(c[:, None, None] * (np.eye(3) + 2.0 ** -e * S))
     return np.concatenate(parts).astype(np.float32)
+
+
+def build_host_math(src, out_dir, opt="-O2"):
+    """compile tests/host_math/<src> (kernel headers built for the host) into a shared library in out_dir with g++;
+    None where g++ or the CUDA headers are missing"""
+    import os
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    if cxx is None or not os.path.exists(os.path.join(inc, "cuda_runtime.h")):
+        return None
+    out = os.path.join(str(out_dir), os.path.splitext(src)[0] + ".so")
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "host_math", src)
+    r = subprocess.run([cxx, "-std=c++17", opt, "-fPIC", "-shared", "-I" + inc, path, "-o", out],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr)
+    return out

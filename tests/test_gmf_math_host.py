@@ -16,14 +16,12 @@ orderings and the device's math library are left to the GPU tests."""
 import ctypes
 import itertools
 import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
 from tests import oracle_lib as ol
-from tests.helpers import maxrel
+from tests.helpers import build_host_math, maxrel
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 KINDS = [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3")]
@@ -33,15 +31,9 @@ S3 = [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 1), (0, 0, 2), (0, 1, 2), (1, 1, 2
 
 @pytest.fixture(scope="module")
 def lib(tmp_path_factory):
-    cxx = shutil.which("g++")
-    inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
-    if cxx is None or not os.path.exists(os.path.join(inc, "cuda_runtime.h")):
+    out = build_host_math("gmf_math_host.cc", tmp_path_factory.mktemp("host_math"), "-O1")
+    if out is None:
         pytest.skip("g++ or the CUDA headers are missing")
-    out = str(tmp_path_factory.mktemp("host_math") / "libgmf_math_host.so")
-    src = os.path.join(HERE, "host_math", "gmf_math_host.cc")
-    r = subprocess.run([cxx, "-std=c++17", "-O1", "-fPIC", "-shared", "-I" + inc, src, "-o", out],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
     L = ctypes.CDLL(out)
     L.gmf_math.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int64] + \
         [ctypes.c_void_p] * 6

@@ -15,14 +15,12 @@ GPU tests).  Bounds: 1e-6 for the FP32 form (max |x - ref| / max |ref| per array
 for the FP64 form (as tests/test_parity_gpu.py)."""
 import ctypes
 import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
 from tests import oracle_lib as ol
-from tests.helpers import maxrel, near_isotropic_f32
+from tests.helpers import build_host_math, maxrel, near_isotropic_f32
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 KINDS = [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3"), (2, 0.7, "pow 0.7")]
@@ -31,15 +29,9 @@ P = ctypes.c_void_p
 
 @pytest.fixture(scope="module")
 def lib(tmp_path_factory):
-    cxx = shutil.which("g++")
-    inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
-    if cxx is None or not os.path.exists(os.path.join(inc, "cuda_runtime.h")):
+    out = build_host_math("smf_math_host.cc", tmp_path_factory.mktemp("host_math"), "-O2")
+    if out is None:
         pytest.skip("g++ or the CUDA headers are missing")
-    out = str(tmp_path_factory.mktemp("host_math") / "libsmf_math_host.so")
-    src = os.path.join(HERE, "host_math", "smf_math_host.cc")
-    r = subprocess.run([cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-I" + inc, src, "-o", out],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
     L = ctypes.CDLL(out)
     L.smf_math_f32.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int64] + [P] * 6
     L.smf_math_f64.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [P] * 6
