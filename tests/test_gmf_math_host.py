@@ -169,3 +169,17 @@ def test_fp64_record_stress(lib, kind, alpha, name):
             continue
         errs = [maxrel(g, r) for g, r in zip(got, ref)]
         assert max(errs) <= 1e-12, (sname, errs)
+
+
+@pytest.mark.parametrize("kind,alpha,name", KINDS[1:] + [(2, 2.5, "pow 2.5")])
+def test_ff_series_stress(lib, kind, alpha, name):
+    """the float-float group series of the FP32-storage kernels on the FP32-rounded stress sets: within 1e-10 of the
+    oracle's results for the same inputs, NaN exactly where the oracle has NaN"""
+    for sname, A in stress_sets(300).items():
+        X = A.astype(np.float32).astype(np.float64).reshape(-1, 9)
+        ref = ol.call(ol.oracle(), "gmf_eval", kind, alpha, X, 2, 9)[1:]
+        got = contract(2, *record(lib, kind, alpha, 2, 1, X))
+        for g, r, out in zip(got, ref, "FJH"):
+            assert np.array_equal(np.isnan(g), np.isnan(r)), (sname, out)
+        errs = [maxrel(g, r) for g, r in zip(got, ref)]
+        assert max(errs) <= 1e-10, (sname, errs)
