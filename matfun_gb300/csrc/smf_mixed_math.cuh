@@ -50,7 +50,9 @@ MF_D float dd1s_f(float a, float b, float dab, float fa, float fb, const SmfCoef
   if (KIND == LOG) {
     float s = 0.5f * (a + b), z = dab / (a + b), az = fabsf(z), z2 = z * z;
     if (az < 1e-3f) return (1.f + z2 / 3.f + z2 * z2 / 5.f + z2 * z2 * z2 / 7.f) / s;
-    if (az >= 0.5f) return (logf(b) - logf(a)) / dab;
+    // far pair: log(b / a) as log1p(dab / a), free of log |A| (whose ulp a difference of two logs would carry);
+    // a <= 0 keeps the difference of logs, with its infinities and NaNs
+    if (az >= 0.5f) return (a > 0.f ? log1pf(dab / a) : logf(b) - logf(a)) / dab;
     return atanhf(z) / z / s;
   }
   if (KIND == SQRT) return 1.f / (sqrtf(a) + sqrtf(b));

@@ -180,3 +180,19 @@ def test_fp64_math_stress(lib, kind, alpha, name):
         _, fl, V, D, D2 = spectra(lib, kind, alpha, voigt(A), False)
         errs = [maxrel(g, r) for g, r in zip(assemble(fl, V, D, D2), ref)]
         assert max(errs) <= 1e-12, (sname, errs)
+
+
+def test_fp32_log_jacobian_free_of_scale(lib):
+    """log J of the FP32 math per matrix (max error / max |J| of that matrix) within 6e-7 at |A| from 2^-60 to 2^60:
+    the far-pair divided difference is log1p((b - a) / a) / (b - a) (the difference of two logs it replaced lost
+    one ulp of log |A|: 1.3e-6 at 2^60)"""
+    from tests.helpers import maxrel_rows
+    for sname, A in stress_sets_spd(200).items():
+        if not sname.startswith("scale") or abs(int(sname.split("^")[1])) > 60:
+            continue
+        A32 = (0.5 * (A + A.transpose(0, 2, 1))).astype(np.float32)
+        ref = ol.call(ol.oracle(), "smf_eval_matrix", 1, 0.0, A32.astype(np.float64).reshape(-1, 9), 1, 9)
+        _, fl, V, D, D2 = spectra(lib, 1, 0.0, A32.reshape(-1, 9), True)
+        F, J, _ = assemble(fl, V, D, D2)
+        e = maxrel_rows(J, ref[2]).max()
+        assert e <= 6e-7, (sname, e)
