@@ -17,10 +17,15 @@
 
 namespace mf {
 
-// terms of the cluster series of the second divided difference in FP32: the offsets are at most tau = 0.25 of the
-// centre (exp: 1 in absolute terms, with factorial coefficients), so term k is below (k + 1) 0.25^k |c2[0]| and the
-// series is truncated below 1e-8 relative after 16 terms (the FP64 form keeps the reference's 30)
-constexpr int DD2_TERMS_F = 16;
+// terms of the cluster series of the second divided difference in FP32.  log: the offsets are at most tau = 0.25 of
+// the centre, so term k is below (k + 1) 0.25^k |c2[0]| and 16 terms reach 1e-8 relative (exp: offsets up to 1 in
+// absolute terms, factorial coefficients).  Powers (and sqrt) take tau = 0.5 (or 3 / alpha, below it) and 30 terms
+// (31 0.5^30 < 3e-8): outside the cluster the difference formula (D_jk - D_ij) / d subtracts first divided
+// differences that differ by (1 - alpha) d / l_j of their size, so their FP32 rounding is amplified by about
+// 1 / ((1 - alpha) tau); at tau = 0.25 that put H of pow 0.7 at 1.3e-6 .. 1.7e-6 of its maximum on near-double
+// eigenvalues.  The FP64 form keeps the reference's tau = 0.25 and 30 terms.
+constexpr int DD2_TERMS_F = 16, DD2_TERMS_F_POW = 30;
+constexpr double DD2_TAU_F_POW = 0.5;
 
 struct SmfCoefF {
   float al, alm1;   // exponent and exponent - 1
@@ -90,9 +95,10 @@ MF_D float dd2s_f(float lj, float lk, float fj, float Dij, float Djk, float dji,
       u = -dji / lj; w = dkj / lj;
       scale = (KIND == LOG ? 1.f : fj) / (lj * lj);
     }
+    constexpr int NT = (KIND == POW || KIND == SQRT) ? DD2_TERMS_F_POW : DD2_TERMS_F;
     float h = 1.f, wk = 1.f, sm = C.c2[0];
 #pragma unroll
-    for (int k = 1; k < DD2_TERMS_F; k++) {
+    for (int k = 1; k < NT; k++) {
       wk = wk * w;
       h = fmaf(u, h, wk);
       sm = fmaf(C.c2[k], h, sm);
@@ -477,7 +483,8 @@ inline void smf_coef_f(int kind, double al, SmfCoefF &C) {
   C.alm1 = (float)(al - 1.0);
   C.zp1 = (float)D.zp1;
   C.z2 = (float)D.z2;
-  C.tau = (float)D.tau;
+  const bool pw = kind == POW || kind == SQRT;
+  C.tau = (float)(pw ? (3.0 / al < DD2_TAU_F_POW ? 3.0 / al : DD2_TAU_F_POW) : D.tau);
   for (int k = 0; k < DD2_TERMS; k++) C.c2[k] = (float)D.c2[k];
 }
 

@@ -1,0 +1,202 @@
+// smf_mixed_tile.cuh -- one tile of the mixed-precision symmetric family: coalesced FP32 input, the eigensystem and
+// divided differences of smf_mixed_math.cuh per thread, the J / H forms of smf_tile.cuh in FP32, coalesced FP32
+// output; the code a CTA of the standalone kernel and of the batched persistent kernel runs.
+#pragma once
+
+#include "smf_mixed_math.cuh"
+#include "smf_tile.cuh"
+
+namespace mf {
+
+constexpr int SMFX_TPB = 64;  // matrices per CTA of the standalone kernel
+
+template <int ORDER, bool MAT, int TPB>
+struct SmfxTileSmem {
+  static constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6;
+  float sX[TPB * NIN];
+  float sF[TPB * NF];
+  float sK[ORDER >= 1 ? TPB * 21 : 1];
+  float sG[ORDER >= 2 ? TPB * 56 : 1];
+};
+
+template <int KIND, int ORDER, bool MAT, int SMFX_TPB>
+MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, float *__restrict__ F,
+                         float *__restrict__ J, float *__restrict__ H, const SmfCoefF &C,
+                         SmfxTileSmem<ORDER, MAT, SMFX_TPB> &TS) {
+  constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6, NJ = NF * NF, NH = NJ * NF;
+  float *sX = TS.sX, *sF = TS.sF, *sK = TS.sK, *sG = TS.sG;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < cnt * NIN; e += SMFX_TPB) sX[e] = x[base * NIN + e];
+  __syncthreads();
+  if (tid < cnt) {
+    const float *xi = sX + tid * NIN;
+    SmfInF in;
+    if (MAT) sym_in_f(xi, in);
+    else voigt_in_f(xi, in);
+    SmfSpecF Sp;
+    smf_spectrum_f<KIND, MAT>(in, C, Sp);
+    const float(&V)[3][3] = Sp.V;
+    const float *fl = Sp.fl;
+    float Fv[6];
+#pragma unroll
+    for (int s = 0; s < 6; s++) {
+      const int a = vk_(s), b = vl_(s);
+      Fv[s] = V[a][0] * fl[0] * V[b][0] + V[a][1] * fl[1] * V[b][1] + V[a][2] * fl[2] * V[b][2];
+    }
+    if (MAT) {
+#pragma unroll
+      for (int m = 0; m < 9; m++) sF[tid * 9 + m] = Fv[m % 4 == 0 ? m / 4 : (m == 1 || m == 3 ? 3 : (m == 2 || m == 6 ? 4 : 5))];
+    } else {
+#pragma unroll
+      for (int s = 0; s < 6; s++) sF[tid * 6 + s] = Fv[s];
+    }
+    if (ORDER >= 1) {
+      float Dm[3][3];
+      smf_dm_f<KIND>(Sp, C, Dm);
+      float P[6][3];
+#pragma unroll
+      for (int s6 = 0; s6 < 6; s6++)
+#pragma unroll
+        for (int a = 0; a < 3; a++) P[s6][a] = V[vk_(s6)][a] * V[vl_(s6)][a];
+      {
+        float Bv[21];
+#pragma unroll
+        for (int g = 0; g < 6; g++) {
+          float dy[3];
+#pragma unroll
+          for (int a = 0; a < 3; a++) dy[a] = Dm[a][0] * P[g][0] + Dm[a][1] * P[g][1] + Dm[a][2] * P[g][2];
+#pragma unroll
+          for (int b2 = 0; b2 <= g; b2++) Bv[sym2(b2, g)] = P[b2][0] * dy[0] + P[b2][1] * dy[1] + P[b2][2] * dy[2];
+        }
+        float *k_out = sK + tid * 21;
+#pragma unroll
+        for (int I = 0; I < 6; I++)
+#pragma unroll
+          for (int p = I; p < 6; p++) {
+            float acc = 0.f;
+            bool first = true;
+#pragma unroll
+            for (int u1 = 0; u1 < 2; u1++)
+#pragma unroll
+              for (int u2 = 0; u2 < 2; u2++) {
+                if ((u1 && vk_(I) == vl_(I)) || (u2 && vk_(p) == vl_(p))) continue;
+                const int s1 = u1 ? vl_(I) : vk_(I), t1 = u1 ? vk_(I) : vl_(I);
+                const int s2 = u2 ? vl_(p) : vk_(p), t2 = u2 ? vk_(p) : vl_(p);
+                const int pa = pidx(s1, s2), pb = pidx(t1, t2);
+                const float v2 = Bv[sym2(min(pa, pb), max(pa, pb))];
+                acc = first ? v2 : acc + v2;
+                first = false;
+              }
+            k_out[sym2(I, p)] = acc;
+          }
+      }
+      if (ORDER >= 2) {
+        float D2[3][3][3];
+        smf_d2_f<KIND>(Sp, Dm, C, D2);
+        float Tv[56];
+#pragma unroll
+        for (int g = 0; g < 6; g++) {
+          float M[3][3];
+#pragma unroll
+          for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int mm = a; mm < 3; mm++)
+              M[a][mm] = M[mm][a] = D2[a][mm][0] * P[g][0] + D2[a][mm][1] * P[g][1] + D2[a][mm][2] * P[g][2];
+#pragma unroll
+          for (int h = 0; h <= g; h++) {
+            float W[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) W[a] = M[a][0] * P[h][0] + M[a][1] * P[h][1] + M[a][2] * P[h][2];
+#pragma unroll
+            for (int f = 0; f <= h; f++) Tv[sym3(f, h, g)] = P[f][0] * W[0] + P[f][1] * W[1] + P[f][2] * W[2];
+          }
+        }
+        float *g_out = sG + tid * 56;
+#pragma unroll
+        for (int z = 0; z < 6; z++)
+#pragma unroll
+          for (int y = 0; y <= z; y++)
+#pragma unroll
+            for (int I = 0; I <= y; I++) {
+              float acc = 0.f;
+              bool first = true;
+#pragma unroll
+              for (int u1 = 0; u1 < 2; u1++)
+#pragma unroll
+                for (int u2 = 0; u2 < 2; u2++)
+#pragma unroll
+                  for (int u3 = 0; u3 < 2; u3++) {
+                    if ((u1 && vk_(I) == vl_(I)) || (u2 && vk_(y) == vl_(y)) || (u3 && vk_(z) == vl_(z))) continue;
+                    const int s1 = u1 ? vl_(I) : vk_(I), t1 = u1 ? vk_(I) : vl_(I);
+                    const int s2 = u2 ? vl_(y) : vk_(y), t2 = u2 ? vk_(y) : vl_(y);
+                    const int s3 = u3 ? vl_(z) : vk_(z), t3 = u3 ? vk_(z) : vl_(z);
+                    int a1 = pidx(s1, s2), a2 = pidx(t2, s3), a3 = pidx(t1, t3);
+                    sort3(a1, a2, a3);
+                    const float v3 = Tv[sym3(a1, a2, a3)];
+                    acc = first ? v3 : acc + v3;
+                    first = false;
+                  }
+              g_out[sym3(I, y, z)] = acc;
+            }
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < cnt * NF; e += SMFX_TPB) F[base * NF + e] = sF[e];
+  if (ORDER >= 1) {
+    constexpr int KJ = (NJ + SMFX_TPB - 1) / SMFX_TPB;
+    int jidx[KJ];
+    float jw[KJ];  // layout weight 2^ex (an FP32 multiplication by a power of two is exact)
+#pragma unroll
+    for (int k = 0; k < KJ; k++) {
+      const int w = min(tid + SMFX_TPB * k, NJ - 1);
+      int I, p, ex;
+      if (MAT) {
+        I = midx(w / 9); p = midx(w % 9);
+        ex = (I >= 3 ? -1 : 0) + mwt_log2(w % 9);
+      } else {
+        I = w / 6; p = w % 6;
+        ex = I >= 3 ? -1 : 0;
+      }
+      jidx[k] = sym2(min(I, p), max(I, p));
+      jw[k] = __int_as_float((127 + ex) << 23);
+    }
+    for (int mi = 0; mi < cnt; mi++) {
+      float *o = J + (base + mi) * NJ;
+      const float *s = sK + mi * 21;
+#pragma unroll
+      for (int k = 0; k < KJ; k++)
+        if (tid + SMFX_TPB * k < NJ) o[tid + SMFX_TPB * k] = s[jidx[k]] * jw[k];
+    }
+  }
+  if (ORDER >= 2) {
+    constexpr int KH = (NH + SMFX_TPB - 1) / SMFX_TPB;
+    int hidx[KH];
+    float hw[KH];
+#pragma unroll
+    for (int k = 0; k < KH; k++) {
+      const int w = min(tid + SMFX_TPB * k, NH - 1);
+      int I, p, q, ex;
+      if (MAT) {
+        const int m = w / 81, c = (w / 9) % 9, e = w % 9;
+        I = midx(m); p = midx(c); q = midx(e);
+        ex = 1 + (I >= 3 ? -1 : 0) + mwt_log2(c) + mwt_log2(e);
+      } else {
+        I = w / 36; p = (w / 6) % 6; q = w % 6;
+        ex = 1 + (I >= 3 ? -1 : 0);
+      }
+      sort3(I, p, q);
+      hidx[k] = sym3(I, p, q);
+      hw[k] = __int_as_float((127 + ex) << 23);
+    }
+    for (int mi = 0; mi < cnt; mi++) {
+      float *o = H + (base + mi) * NH;
+      const float *s = sG + mi * 56;
+#pragma unroll
+      for (int k = 0; k < KH; k++)
+        if (tid + SMFX_TPB * k < NH) o[tid + SMFX_TPB * k] = s[hidx[k]] * hw[k];
+    }
+  }
+}
+
+}  // namespace mf
