@@ -15,7 +15,7 @@
 //
 // Mixed precision (FP32 arrays, T = float): gmf keeps its FP64 record (spectral analysis, series, residues), folds the
 // scale factors into it in FP64 and rounds it to FP32 once for the contractions; smf takes the eigensystem and the
-// divided differences of the mixed smf kernel (smf_mixed.cuh) and contracts in FP32.
+// divided differences of the mixed smf kernel (smf_mixed_math.cuh) and contracts in FP32.
 #pragma once
 #include "gmf_kernels.cuh"
 #include "smf_kernels.cuh"
@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel(int64_t n, const 
   }
 }
 
-// mixed precision: FP32 arrays, the eigensystem and divided differences of smf_mixed.cuh, FP32 contractions
+// mixed precision: FP32 arrays, the eigensystem and divided differences of smf_mixed_math.cuh, FP32 contractions
 template <int KIND, int ORDER>
 __global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel_f32(int64_t n, const float *__restrict__ A,
                                                                    const float *__restrict__ W,

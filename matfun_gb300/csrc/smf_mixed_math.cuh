@@ -8,7 +8,7 @@
 //   * the differences of eigenvalues that feed the near-coalescent branches of the divided differences (z, u, w and
 //     the denominators of the difference formulas), taken from the float-float eigenvalues before rounding to FP32.
 // f(lambda), the first and second divided differences (stable forms, cluster series), the product vectors and the
-// J / H forms of smf_kernels.cuh run in FP32.  The kernel executes no FP64 instruction (the FP64 kernel: ~2.5k per
+// J / H forms of smf_tile.cuh run in FP32.  The kernel executes no FP64 instruction (the FP64 kernel: ~2.5k per
 // matrix, at 1/74 of the FP32 rate on GB300), so it moves towards the HBM roofline, and FP32 storage halves the bytes.
 // Accuracy against the FP64 oracle is stated per kind and order in the tests (<= 1e-6 relative, max-norm).
 #pragma once
