@@ -237,9 +237,12 @@ MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E, float *dbg = nullptr) {
   float q1 = s.hi / 3.f;
   float q2 = (fmaf(-q1, 3.f, s.hi) + s.lo) / 3.f;
   const ffl m = fast_two_sum(q1, q2);
-  float dv[3];  // deviator in FP32 (the input of the trigonometric root only)
+  // deviator in FP32 (the input of the trigonometric root only), from the float-float mean: a - m.hi is exact near
+  // the mean, and subtracting m.lo too leaves it traceless to FP32 rounding, as the root formula assumes (the
+  // trace residue 3 m.lo alone is a few percent of a deviator of 1e-6 |A|, and skews the root and its vector)
+  float dv[3];
 #pragma unroll
-  for (int i = 0; i < 3; i++) dv[i] = a[i] - m.hi;
+  for (int i = 0; i < 3; i++) dv[i] = (a[i] - m.hi) - m.lo;
   // FP32: normalised deviator, trigonometric root, eigenvector, complement
   int kd = 0;
 #pragma unroll
@@ -440,8 +443,14 @@ MF_D void smf_spectrum_f(const SmfInF &in, const SmfCoefF &C, SmfSpecF &Sp) {
     float mf = E.m, lms = logf(mf);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      float x = xd[i].hi + xd[i].lo;
-      Sp.fl[i] = self(fabsf(x) <= 0.5f * mf, lms + log1pf(x / mf), Sp.fl[i]);
+      // near 1 (the log strain of a small deformation): log1p of lambda - 1, taken in float-float from the
+      // float-float eigenvalue, keeps FP32 relative accuracy in log lambda, where log m + log1p(x / m) would lose
+      // the rounding of m to FP32 against a result of the size of the strain; one log1p serves both forms
+      const float x = xd[i].hi + xd[i].lo;
+      const float tt = (lam[i].hi - 1.f) + lam[i].lo;  // lam.hi - 1 is exact where |tt| <= 0.25 (Sterbenz)
+      const bool near1 = fabsf(tt) <= 0.25f, nearm = fabsf(x) <= 0.5f * mf;
+      const float l1 = log1pf(self(near1, tt, x / mf));
+      Sp.fl[i] = self(near1, l1, self(nearm, lms + l1, Sp.fl[i]));
     }
   }
 }
