@@ -3,7 +3,7 @@
 // input staging, the symmetric part of the matrix layout, the eigensystem, the divided differences, the product-vector
 // forms of J and H and their expansion into the output layouts with the layout weights -- against the oracle.  With
 // TPB = 1 every cooperative loop of a tile runs in its one thread and its barriers have nothing to wait for.  The test
-// builds this file with g++ (tests/test_smf_tile_host.py).
+// builds this file with g++ (tests/test_smf_tile_host.py).  The adjoint tiles (smf_adjoint_tile.cuh) run the same way.
 #include "host_intrinsics.h"
 
 struct HostDim3 {
@@ -17,6 +17,7 @@ inline int atomicAdd(int *p, int v) {
   return o;
 }
 
+#include "../../matfun_gb300/csrc/smf_adjoint_tile.cuh"
 #include "../../matfun_gb300/csrc/smf_mixed_tile.cuh"
 #include "../../matfun_gb300/csrc/smf_tile.cuh"
 
@@ -96,4 +97,64 @@ extern "C" int smf_tile_f32(int kind, double al, int order, int mat, int64_t n, 
                             float *H) {
   if (kind != 2) al = kind == 3 ? 0.5 : 0.0;
   return dispatch<float>(kind, order, mat, Run32{al, n, x, F, J, H});
+}
+
+namespace {
+
+template <int KIND, int ORDER>
+void adj64(double al, int64_t n, const double *A, const double *W, const double *V, double *F, double *Abar,
+           double *JV, double *HWV) {
+  SmfCoef C;
+  smf_coef(KIND, al, C);
+  SadjSmem<double, 1> S;
+  for (int64_t i = 0; i < n; i++) smf_adjoint_tile<KIND, ORDER, 1>(i, 1, A, W, V, F, Abar, JV, HWV, C, S);
+}
+
+template <int KIND, int ORDER>
+void adj32(double al, int64_t n, const float *A, const float *W, const float *V, float *F, float *Abar, float *JV,
+           float *HWV) {
+  SmfCoefF C;
+  smf_coef_f(KIND, al, C);
+  SadjSmem<float, 1> S;
+  for (int64_t i = 0; i < n; i++) smf_adjoint_tile_f32<KIND, ORDER, 1>(i, 1, A, W, V, F, Abar, JV, HWV, C, S);
+}
+
+template <typename T, typename Fn>
+int adj_dispatch(int kind, int order, Fn fn) {
+  switch (kind) {
+    case EXP: return order == 2 ? fn.template go<EXP, 2>() : fn.template go<EXP, 1>();
+    case LOG: return order == 2 ? fn.template go<LOG, 2>() : fn.template go<LOG, 1>();
+    case POW: return order == 2 ? fn.template go<POW, 2>() : fn.template go<POW, 1>();
+    case SQRT: return order == 2 ? fn.template go<SQRT, 2>() : fn.template go<SQRT, 1>();
+    default: return -1;
+  }
+}
+
+template <typename T>
+struct Adj {
+  double al;
+  int64_t n;
+  const T *A, *W, *V;
+  T *F, *Abar, *JV, *HWV;
+  template <int K, int O>
+  int go() const {
+    if constexpr (sizeof(T) == 8) adj64<K, O>(al, n, A, W, V, F, Abar, JV, HWV);
+    else adj32<K, O>(al, n, A, W, V, F, Abar, JV, HWV);
+    return 0;
+  }
+};
+
+}  // namespace
+
+// the adjoint tiles: order 2 when HWV is requested, else 1, as smf_cuda_adjoint picks it; outputs may be null
+extern "C" int smf_adjoint_f64(int kind, double al, int64_t n, const double *A, const double *W, const double *V,
+                               double *F, double *Abar, double *JV, double *HWV) {
+  if (kind != 2) al = kind == 3 ? 0.5 : 0.0;
+  return adj_dispatch<double>(kind, HWV ? 2 : 1, Adj<double>{al, n, A, W, V, F, Abar, JV, HWV});
+}
+
+extern "C" int smf_adjoint_f32(int kind, double al, int64_t n, const float *A, const float *W, const float *V,
+                               float *F, float *Abar, float *JV, float *HWV) {
+  if (kind != 2) al = kind == 3 ? 0.5 : 0.0;
+  return adj_dispatch<float>(kind, HWV ? 2 : 1, Adj<float>{al, n, A, W, V, F, Abar, JV, HWV});
 }

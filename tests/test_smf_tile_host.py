@@ -146,3 +146,39 @@ def test_fp32_log_small_strain(lib):
         got, _ = run(lib, True, 1, 0.0, 2, True, X)
         errs = [float(maxrel_rows(g, r).max()) for g, r in zip(got, ref)]
         assert max(errs) <= 1e-6, (strain, errs)
+
+
+@pytest.mark.parametrize("kind,alpha,name", [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3")])
+@pytest.mark.parametrize("f32", [False, True])
+def test_adjoint_tiles(lib, kind, alpha, name, f32):
+    """the adjoint tiles (smf_adjoint_tile.cuh) run on the CPU: F, Abar = J^T W, JV = J V and HWV = W.H.V against the
+    oracle's materialised J and H contracted in FP64, on C2, C0, the near-degenerate set and small strains (log),
+    within 1e-12 (FP64) and 1e-6 (FP32); the order-1 launch (no HWV) writes the same F, Abar, JV"""
+    from matfun_gb300 import workloads as w
+    for fn in (lib.smf_adjoint_f64, lib.smf_adjoint_f32):
+        fn.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [P] * 7
+        fn.restype = ctypes.c_int
+    rng = np.random.default_rng(61)
+    Q, _ = np.linalg.qr(rng.standard_normal((300, 3, 3)))
+    strain = np.einsum("nia,na,nja->nij", Q, 1 + 1e-4 * rng.uniform(-1, 1, (300, 3)), Q)
+    sets = [w.c2_smf_spd(500, seed=62, as_voigt=False), w.c0_smf_spd(500, seed=63, as_voigt=False),
+            near_isotropic_f32().astype(np.float64), strain]
+    dt = np.float32 if f32 else np.float64
+    fn = lib.smf_adjoint_f32 if f32 else lib.smf_adjoint_f64
+    for A in sets:
+        n = len(A)
+        Ac = np.ascontiguousarray(A.reshape(n, 9).astype(dt))
+        Wc, Vc = (np.ascontiguousarray(rng.standard_normal((n, 9)).astype(dt)) for _ in range(2))
+        _, F, J, H = ol.call(ol.oracle(), "smf_eval_matrix", kind, alpha, Ac.astype(np.float64), 2, 9)
+        J4, H5 = J.reshape(n, 9, 9), H.reshape(n, 9, 9, 9)
+        W64, V64 = Wc.astype(np.float64), Vc.astype(np.float64)
+        ref = [F, np.einsum("nm,nmc->nc", W64, J4), np.einsum("nmc,nc->nm", J4, V64),
+               np.einsum("nm,nmce,nc->ne", W64, H5, V64)]
+        out = [np.zeros((n, 9), dt) for _ in range(4)]
+        assert fn(kind, alpha, n, Ac.ctypes.data, Wc.ctypes.data, Vc.ctypes.data, *[o.ctypes.data for o in out]) == 0
+        errs = [maxrel(o, r) for o, r in zip(out, ref)]
+        assert max(errs) <= (1e-6 if f32 else 1e-12), errs
+        out1 = [np.zeros((n, 9), dt) for _ in range(3)]
+        assert fn(kind, alpha, n, Ac.ctypes.data, Wc.ctypes.data, Vc.ctypes.data, *[o.ctypes.data for o in out1],
+                  None) == 0
+        assert all(np.array_equal(a, b) for a, b in zip(out1, out[:3]))
