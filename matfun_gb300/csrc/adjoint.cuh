@@ -20,50 +20,17 @@
 #include "gmf_kernels.cuh"
 #include "smf_kernels.cuh"
 #include "smf_mixed.cuh"
+#include "gmf_adjoint_tile.cuh"
 #include "smf_adjoint_tile.cuh"
 
 namespace mf {
-
-template <typename T>
-MF_D void mm3(const T *X, const T *Y, T *Z) {  // Z = X Y
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) Z[3 * i + j] = X[3 * i] * Y[j] + X[3 * i + 1] * Y[3 + j] + X[3 * i + 2] * Y[6 + j];
-}
-template <typename T>
-MF_D void mmT3(const T *X, const T *Y, T *Z) {  // Z = X Y^T
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++)
-      Z[3 * i + j] = X[3 * i] * Y[3 * j] + X[3 * i + 1] * Y[3 * j + 1] + X[3 * i + 2] * Y[3 * j + 2];
-}
-template <typename T>
-MF_D void mTm3(const T *X, const T *Y, T *Z) {  // Z = X^T Y
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) Z[3 * i + j] = X[i] * Y[j] + X[3 + i] * Y[3 + j] + X[6 + i] * Y[6 + j];
-}
-
-// the output factor of a record, applied last as in the reference (NaN for a matrix outside the domain)
-template <typename T>
-MF_D T scale_out(T v, T sc) { return v * sc; }
 
 enum { ADJ_F = 1, ADJ_VJP = 2, ADJ_JVP = 4, ADJ_HVP = 8 };
 
 // ------------------------------------------------------------------------------------------------ general
 constexpr int GADJ_TPB = 128;
 
-struct GadjSmem {
-  double x[GADJ_TPB * 9], w[GADJ_TPB * 9], v[GADJ_TPB * 9];
-  double out[4][GADJ_TPB * 9];  // F, Abar, JV, HWV staging
-  GmfState state[GADJ_TPB];
-  unsigned key[GADJ_TPB];
-  int perm[GADJ_TPB];
-  long long gidx[GADJ_TPB];  // tile position -> matrix index (the ordered launch)
-};
+using GadjSmem = GadjSmemT<GADJ_TPB>;
 
 template <int KIND, int ORDER, typename T>
 __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const T *__restrict__ A,
@@ -73,182 +40,9 @@ __global__ void __launch_bounds__(GADJ_TPB) gmf_adjoint_kernel(int64_t n, const 
                                                                const GmfCoef C, const int *__restrict__ idx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GadjSmem &S = *reinterpret_cast<GadjSmem *>(smem_raw);
-  const int tid = threadIdx.x;
   const int64_t base = (int64_t)blockIdx.x * GADJ_TPB;
-  const int cnt = (int)min((int64_t)GADJ_TPB, n - base);
-  for (int e = tid; e < cnt * 9; e += GADJ_TPB) {  // (idx: position p holds matrix idx[base + p])
-    const int p = e / 9;
-    const long long g = idx ? (long long)idx[base + p] : base + p, ge = g * 9 + (e - 9 * p);
-    S.x[e] = A[ge];
-    if (W) S.w[e] = W[ge];
-    if (V) S.v[e] = V[ge];
-    if (e == 9 * p) S.gidx[p] = g;
-  }
-  __syncthreads();
-  unsigned key = 0xFFFFFFFFu;
-  if (tid < cnt) {
-    double a[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) a[k] = S.x[tid * 9 + k];
-    GmfState St;
-    gmf_classify<KIND, ORDER>(a, C, St);
-    S.state[tid] = St;
-    const unsigned cls = St.K == 0 ? 0u : ((St.flags & 1024) ? 1u : 2u);
-    key = (cls << 16) | ((unsigned)(255 - St.K) << 6) | (unsigned)((St.flags >> 3) & 63);
-  }
-  S.key[tid] = key;
-  __syncthreads();
-  {
-    int rank = 0;
-    for (int j = 0; j < GADJ_TPB; j++) {
-      const unsigned kj = S.key[j];
-      rank += (kj < key) | ((kj == key) & (j < tid));
-    }
-    S.perm[rank] = tid;
-  }
-  __syncthreads();
-  const int mine = S.perm[tid];
-  if (mine < cnt) {
-    GmfRec R;
-    gmf_finish<KIND, ORDER, sizeof(T) == 4>(S.state[mine], C, R);
-    // FP32: fold the scale factors into D2', D3' in FP64 when finite and nonzero, then round the record once
-    constexpr bool MIXED = sizeof(T) == 4;
-    const double rsc2 = ORDER >= 2 ? R.sc2 : 1.0;
-    const bool f1 = MIXED & isfinite(R.sc1) & (R.sc1 != 0.0), f2 = MIXED & isfinite(rsc2) & (rsc2 != 0.0);
-    const double s1 = sel(f1, R.sc1, 1.0), s2 = sel(f2, rsc2, 1.0);
-    const T sc1 = (T)sel(f1, 1.0, R.sc1), sc2 = (T)sel(f2, 1.0, rsc2);
-    T r[3][9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      r[0][k] = k % 4 == 0 ? T(1) : T(0);
-      r[1][k] = (T)R.r1[k];
-      r[2][k] = (T)R.r2[k];
-    }
-    T D2s[6], D3s[10];
-#pragma unroll
-    for (int k = 0; k < 6; k++) D2s[k] = (T)(R.D2[k] * s1);
-#pragma unroll
-    for (int k = 0; k < 10; k++) D3s[k] = ORDER >= 2 ? (T)(R.D3[k] * s2) : T(0);
-    const T D2m[3][3] = {{D2s[0], D2s[3], D2s[4]}, {D2s[3], D2s[1], D2s[5]}, {D2s[4], D2s[5], D2s[2]}};
-    if (F) {
-#pragma unroll
-      for (int k = 0; k < 9; k++) S.out[0][mine * 9 + k] = R.F[k];
-    }
-    const double *w = S.w + mine * 9, *v = S.v + mine * 9;
-    T Wl[9], Vl[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) { Wl[k] = W ? (T)w[k] : T(0); Vl[k] = V ? (T)v[k] : T(0); }
-    T Gw[3][9];  // W r_n^T
-    if (Abar || HWV) {
-#pragma unroll
-      for (int k = 0; k < 9; k++) Gw[0][k] = Wl[k];
-      mmT3(Wl, r[1], Gw[1]);
-      mmT3(Wl, r[2], Gw[2]);
-    }
-    if (Abar) {  // sc1 sum_m r_m^T (sum_n D2'_mn W r_n^T)
-      T acc[9];
-#pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] = T(0);
-#pragma unroll
-      for (int mm = 0; mm < 3; mm++) {
-        T Hm[9], Tm[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gw[0][k] + D2m[mm][1] * Gw[1][k] + D2m[mm][2] * Gw[2][k];
-        if (mm == 0) {
-#pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += Hm[k];
-        } else {
-          mTm3(r[mm], Hm, Tm);
-#pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += Tm[k];
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < 9; k++) S.out[1][mine * 9 + k] = scale_out(acc[k], sc1);
-    }
-    T Gv[3][9];  // V r_n
-    if (JV || HWV) {
-#pragma unroll
-      for (int k = 0; k < 9; k++) Gv[0][k] = Vl[k];
-      mm3(Vl, r[1], Gv[1]);
-      mm3(Vl, r[2], Gv[2]);
-    }
-    if (JV) {  // sc1 sum_m r_m (sum_n D2'_mn V r_n)
-      T acc[9];
-#pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] = T(0);
-#pragma unroll
-      for (int mm = 0; mm < 3; mm++) {
-        T Hm[9], Tm[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gv[0][k] + D2m[mm][1] * Gv[1][k] + D2m[mm][2] * Gv[2][k];
-        if (mm == 0) {
-#pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += Hm[k];
-        } else {
-          mm3(r[mm], Hm, Tm);
-#pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += Tm[k];
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < 9; k++) S.out[2][mine * 9 + k] = scale_out(acc[k], sc1);
-    }
-    if (ORDER >= 2 && HWV) {
-      // M_mn = r_m V r_n ; X_p = sum_mn D3'_mnp M_mn ; HWV = sc2 sum_p (X_p^T W r_p^T + r_p^T W X_p^T)
-      T X[3][9];
-#pragma unroll
-      for (int p = 0; p < 3; p++)
-#pragma unroll
-        for (int k = 0; k < 9; k++) X[p][k] = T(0);
-#pragma unroll
-      for (int mm = 0; mm < 3; mm++)
-#pragma unroll
-        for (int nn = 0; nn < 3; nn++) {
-          T M[9];
-          if (mm == 0) {
-#pragma unroll
-            for (int k = 0; k < 9; k++) M[k] = Gv[nn][k];
-          } else {
-            mm3(r[mm], Gv[nn], M);
-          }
-#pragma unroll
-          for (int p = 0; p < 3; p++) {
-            int i0 = mm, i1 = nn, i2 = p;
-            sort3(i0, i1, i2);
-            const T d = D3s[sym3(i0, i1, i2)];
-#pragma unroll
-            for (int k = 0; k < 9; k++) X[p][k] += d * M[k];
-          }
-        }
-      T acc[9];
-#pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] = T(0);
-#pragma unroll
-      for (int p = 0; p < 3; p++) {
-        T T1[9], T2[9], T3[9];
-        mTm3(X[p], Gw[p], T1);  // X_p^T (W r_p^T)
-        mmT3(Wl, X[p], T2);     // W X_p^T
-        if (p == 0) {
-#pragma unroll
-          for (int k = 0; k < 9; k++) T3[k] = T2[k];
-        } else {
-          mTm3(r[p], T2, T3);   // r_p^T W X_p^T
-        }
-#pragma unroll
-        for (int k = 0; k < 9; k++) acc[k] += T1[k] + T3[k];
-      }
-#pragma unroll
-      for (int k = 0; k < 9; k++) S.out[3][mine * 9 + k] = scale_out(acc[k], sc2);
-    }
-  }
-  __syncthreads();
-  T *dst[4] = {F, Abar, JV, HWV};
-#pragma unroll
-  for (int q = 0; q < 4; q++) {
-    if (!dst[q]) continue;
-    for (int e = tid; e < cnt * 9; e += GADJ_TPB) dst[q][S.gidx[e / 9] * 9 + e % 9] = (T)S.out[q][e];
-  }
+  gmf_adjoint_tile<KIND, ORDER, T, GADJ_TPB>(base, (int)min((int64_t)GADJ_TPB, n - base), A, W, V, F, Abar, JV, HWV,
+                                             C, idx, S);
 }
 
 // ------------------------------------------------------------------------------------------------ symmetric

@@ -28,6 +28,7 @@ inline double __longlong_as_double(long long i) {
   std::memcpy(&x, &i, sizeof x);
   return x;
 }
+using std::isfinite;  // a global function in device code
 inline float __fsqrt_rn(float x) { return std::sqrt(x); }
 inline float __fdiv_rn(float a, float b) { return a / b; }
 inline int min(int a, int b) { return a < b ? a : b; }

@@ -4,18 +4,8 @@
 // forms of J and H and their expansion into the output layouts with the layout weights -- against the oracle.  With
 // TPB = 1 every cooperative loop of a tile runs in its one thread and its barriers have nothing to wait for.  The test
 // builds this file with g++ (tests/test_smf_tile_host.py).  The adjoint tiles (smf_adjoint_tile.cuh) run the same way.
+#include "host_cta.h"
 #include "host_intrinsics.h"
-
-struct HostDim3 {
-  unsigned x = 0, y = 0, z = 0;
-};
-static HostDim3 threadIdx;  // thread 0 of a one-thread CTA
-inline void __syncthreads() {}
-inline int atomicAdd(int *p, int v) {
-  const int o = *p;
-  *p += v;
-  return o;
-}
 
 #include "../../matfun_gb300/csrc/smf_adjoint_tile.cuh"
 #include "../../matfun_gb300/csrc/smf_mixed_tile.cuh"

@@ -183,3 +183,54 @@ def test_ff_series_stress(lib, kind, alpha, name):
             assert np.array_equal(np.isnan(g), np.isnan(r)), (sname, out)
         errs = [maxrel(g, r) for g, r in zip(got, ref)]
         assert max(errs) <= 1e-10, (sname, errs)
+
+
+@pytest.fixture(scope="module")
+def adj(tmp_path_factory):
+    out = build_host_math("gmf_adjoint_host.cc", tmp_path_factory.mktemp("host_math"), "-O1")
+    if out is None:
+        pytest.skip("g++ or the CUDA headers are missing")
+    L = ctypes.CDLL(out)
+    for fn in (L.gmf_adjoint_f64, L.gmf_adjoint_f32):
+        fn.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int64] + [ctypes.c_void_p] * 7
+        fn.restype = ctypes.c_int
+    return L
+
+
+@pytest.mark.parametrize("kind,alpha,name", KINDS)
+@pytest.mark.parametrize("f32", [False, True])
+def test_adjoint_tile(adj, kind, alpha, name, f32):
+    """the general adjoint tile (gmf_adjoint_tile.cuh) run on the CPU: F, Abar = J^T W, JV = J V and HWV = W.H.V
+    against the oracle's J and H contracted in FP64, NaN exactly where the oracle has NaN.  FP64: within 1e-12 on C1
+    and every stress set (exp: where it is finite).  FP32 (the record folded and rounded once, FP32 contractions):
+    within 1e-6 on C1 and 2e-6 on the stress sets within FP32's range (a Jordan block perturbed by 1e-12 and pairs at
+    3.14 from the positive axis reach 1.1e-6 .. 1.2e-6); the order-1 launch writes the same F, Abar, JV"""
+    from matfun_gb300 import workloads as w
+    rng = np.random.default_rng(71)
+    sets = {"C1": w.c1_gmf_groups(1000, seed=71).reshape(-1, 9)}
+    sets.update({k: v.reshape(-1, 9) for k, v in stress_sets(100).items()})
+    dt = np.float32 if f32 else np.float64
+    fn = adj.gmf_adjoint_f32 if f32 else adj.gmf_adjoint_f64
+    for sname, A in sets.items():
+        if (kind == 0 and np.abs(A).max() > 60) or (f32 and sname.startswith("scale")):
+            continue
+        n = len(A)
+        Ac = np.ascontiguousarray(A.astype(dt))
+        Wc, Vc = (np.ascontiguousarray(rng.standard_normal((n, 9)).astype(dt)) for _ in range(2))
+        _, F, J, H = ol.call(ol.oracle(), "gmf_eval", kind, alpha, Ac.astype(np.float64), 2, 9)
+        J4, H5 = J.reshape(n, 9, 9), H.reshape(n, 9, 9, 9)
+        W64, V64 = Wc.astype(np.float64), Vc.astype(np.float64)
+        ref = [F, np.einsum("nm,nmc->nc", W64, J4), np.einsum("nmc,nc->nm", J4, V64),
+               np.einsum("nm,nmce,nc->ne", W64, H5, V64)]
+        out = [np.zeros((n, 9), dt) for _ in range(4)]
+        assert fn(kind, alpha, n, Ac.ctypes.data, Wc.ctypes.data, Vc.ctypes.data, *[o.ctypes.data for o in out]) == 0
+        for o, r in zip(out, ref):
+            assert np.array_equal(np.isnan(o), np.isnan(r)), sname
+        bound = (1e-6 if sname == "C1" else 2e-6) if f32 else 1e-12
+        errs = [maxrel(o, r) for o, r in zip(out, ref)]
+        assert max(errs) <= bound, (sname, errs)
+        out1 = [np.zeros((n, 9), dt) for _ in range(3)]
+        assert fn(kind, alpha, n, Ac.ctypes.data, Wc.ctypes.data, Vc.ctypes.data, *[o.ctypes.data for o in out1],
+                  None) == 0
+        for a, b in zip(out1, out[:3]):
+            assert maxrel(a, b) <= (1e-6 if f32 else 1e-13), sname
