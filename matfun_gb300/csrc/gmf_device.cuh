@@ -737,7 +737,7 @@ MF_D void gmf_classify_from(const double *a, const cx *xr, const GmfCoef &C, Gmf
   double rr = tmax(cabs_s(u[0]), tmax(cabs_s(u[1]), cabs_s(u[2])));
   double rq = sel((pk[0] | pk[1] | pk[2]) & (rr * fabs(iap) <= 1.0), rr * fabs(iap), 0.0);
   rr = sel(hasg & (rr <= G_R_EXP + 0.5), rr, 0.0);
-  int j1, j2;
+  int j1 = G_KMAX, j2 = G_KMAX;  // (no group: nterms is not called and the split points are not used)
   St.K = hasg ? nterms(C, 3 * (ORDER + 1) - 1, rr, rq, j1, j2) : 0;
   // the float-float / FP32 tail of the series: log and pow without a pole node, coefficients within FP32's range
   const bool tail = (C.ffser != 0) & !(pk[0] | pk[1] | pk[2]) & (rr <= 4.0);
