@@ -46,12 +46,12 @@ def voigt_to_matrix(v):
     return A
 
 
-def near_isotropic_f32():
-    """FP32 matrices within 2^-30 .. 2^-70 of a multiple of I: c (I + 2^-e S), S symmetric with zero diagonal (the
-    deviator exactly representable in FP32); row 29913 of C0 (n = 65536, seed 4), whose FP32 eigenvectors came out of
-    smf_eigsys_ff 0.6 % from orthonormal on GB300 (F 3e-3 from the oracle); and row 31949 of C0 (n = 50000, seed 6),
-    a triple eigenvalue rounded to FP32, whose pair's Jacobi block squared into FP32's subnormal range before that
-    block was scaled (H 2e-2 from the oracle)"""
+def near_degenerate_f32():
+    """the near-degenerate set: FP32 matrices within 2^-30 .. 2^-70 of a multiple of I, c (I + 2^-e S) with S
+    symmetric and of zero diagonal (the deviator exactly representable in FP32); row 29913 of C0 (n = 65536, seed 4),
+    whose FP32 eigenvectors came out of smf_eigsys_ff 0.6 % from orthonormal on GB300 (F 3e-3 from the oracle); and
+    row 31949 of C0 (n = 50000, seed 6), a triple eigenvalue rounded to FP32, whose pair's Jacobi block squared into
+    FP32's subnormal range before that block was scaled (H 2e-2 from the oracle)"""
     from matfun_gb300 import workloads as w
     rng = np.random.default_rng(29913)
     parts = [w.c0_smf_spd(65536, seed=4, as_voigt=False)[29913:29914],

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from tests import oracle_lib as ol
-from tests.helpers import maxrel, near_isotropic_f32
+from tests.helpers import maxrel, near_degenerate_f32
 
 pytestmark = pytest.mark.gpu
 KINDS = [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3"), (2, 0.7, "pow 0.7")]
@@ -79,7 +79,7 @@ def test_smf_mixed_c0_and_golden_inputs():
                    "C0 row 29913 failed on GB300 before, for a cause the host build does not reproduce")
 @pytest.mark.parametrize("kind,alpha,name", KINDS)
 def test_smf_mixed_near_isotropic(kind, alpha, name):
-    A = near_isotropic_f32()
+    A = near_degenerate_f32()
     errs, got, ref = errors(True, kind, alpha, A.reshape(-1, 9), 2)
     row = [maxrel(g[:1], r[:1]) for g, r in zip(got, ref[1:])]
     print(f"mixed smf near-isotropic {name}: max rel F J H {errs}; C0 row 29913 alone {row}")
@@ -94,7 +94,7 @@ def test_smf_mixed_adjoint_near_isotropic():
 
     import matfun_gb300
     lib = matfun_gb300.load()
-    A32 = torch.from_numpy(near_isotropic_f32()).cuda()
+    A32 = torch.from_numpy(near_degenerate_f32()).cuda()
     n = A32.shape[0]
     W32 = torch.from_numpy(np.random.default_rng(5).standard_normal((n, 3, 3)).astype(np.float32)).cuda()
     Ab32 = torch.empty_like(A32)
@@ -234,7 +234,7 @@ def test_smf_f32_probe_orthonormal(tmp_path):
     from matfun_gb300 import workloads as w
     from tests.helpers import build_host_math
     lib = matfun_gb300.load()
-    X = np.concatenate([near_isotropic_f32().reshape(-1, 9),
+    X = np.concatenate([near_degenerate_f32().reshape(-1, 9),
                         w.c2_smf_spd(2000, seed=41, as_voigt=False).astype(np.float32).reshape(-1, 9)])
     n = len(X)
     dX = torch.from_numpy(X).cuda()

@@ -20,7 +20,7 @@ import numpy as np
 import pytest
 
 from tests import oracle_lib as ol
-from tests.helpers import build_host_math, maxrel, near_isotropic_f32
+from tests.helpers import build_host_math, maxrel, near_degenerate_f32
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 KINDS = [(0, 0.0, "exp"), (1, 0.0, "log"), (3, 0.0, "sqrt"), (2, 0.3, "pow 0.3"), (2, 0.7, "pow 0.7")]
@@ -73,7 +73,7 @@ def inputs():
     return {
         "C2": w.c2_smf_spd(2000, seed=31, as_voigt=False),
         "C0": w.c0_smf_spd(2000, seed=32, as_voigt=False),
-        "near-isotropic": near_isotropic_f32().astype(np.float64),
+        "near-isotropic": near_degenerate_f32().astype(np.float64),
     }
 
 

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from tests import oracle_lib as ol
-from tests.helpers import build_host_math, maxrel, near_isotropic_f32, voigt_to_matrix
+from tests.helpers import build_host_math, maxrel, near_degenerate_f32, voigt_to_matrix
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 P = ctypes.c_void_p
@@ -59,7 +59,7 @@ def inputs():
     from matfun_gb300 import workloads as w
     from tests.test_smf_math_host import stress_sets_spd
     sets = {"C2": w.c2_smf_spd(1000, seed=51, as_voigt=False), "C0": w.c0_smf_spd(1000, seed=52, as_voigt=False),
-            "near-degenerate": near_isotropic_f32().astype(np.float64)}
+            "near-degenerate": near_degenerate_f32().astype(np.float64)}
     for name, A in stress_sets_spd(100, seed=53).items():
         sets[name] = 0.5 * (A + A.transpose(0, 2, 1))
     return sets
@@ -162,7 +162,7 @@ def test_adjoint_tiles(lib, kind, alpha, name, f32):
     Q, _ = np.linalg.qr(rng.standard_normal((300, 3, 3)))
     strain = np.einsum("nia,na,nja->nij", Q, 1 + 1e-4 * rng.uniform(-1, 1, (300, 3)), Q)
     sets = [w.c2_smf_spd(500, seed=62, as_voigt=False), w.c0_smf_spd(500, seed=63, as_voigt=False),
-            near_isotropic_f32().astype(np.float64), strain]
+            near_degenerate_f32().astype(np.float64), strain]
     dt = np.float32 if f32 else np.float64
     fn = lib.smf_adjoint_f32 if f32 else lib.smf_adjoint_f64
     for A in sets:
