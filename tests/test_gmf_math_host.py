@@ -234,3 +234,37 @@ def test_adjoint_tile(adj, kind, alpha, name, f32):
                   None) == 0
         for a, b in zip(out1, out[:3]):
             assert maxrel(a, b) <= (1e-6 if f32 else 1e-13), sname
+
+
+@pytest.mark.parametrize("kind,alpha,name", KINDS + [(2, 2.5, "pow 2.5")])
+def test_fp64_record_random(lib, kind, alpha, name):
+    """the FP64 record per matrix (max error / max |ref| of that matrix's F, J, H) on random general matrices:
+    diagonalisable with spectra over e^+-3, complex pairs at random angles, Jordan blocks perturbed by 1e-14 .. 1e-2
+    and I + 0.5 N, similarity transforms by S = N(0, 1) + U(0.5, 4) I; within 5e-12 per matrix (last-bit differences
+    amplified in H reach 2.5e-12 on 60 000 per kind), NaN exactly where the oracle has NaN"""
+    from tests.helpers import maxrel_rows
+    rng = np.random.default_rng(99)
+    n = 1500
+
+    def conj(M):
+        S = rng.standard_normal((len(M), 3, 3)) + rng.uniform(0.5, 4, (len(M), 1, 1)) * np.eye(3)
+        return S @ M @ np.linalg.inv(S)
+
+    D = np.zeros((n, 3, 3))
+    D[:, [0, 1, 2], [0, 1, 2]] = np.exp(rng.uniform(-3, 3, (n, 3)))
+    r, t = np.exp(rng.uniform(-2, 2, n)), rng.uniform(-3.14, 3.14, n)
+    M = np.zeros((n, 3, 3))
+    M[:, 0, 0] = M[:, 1, 1] = r * np.cos(t)
+    M[:, 0, 1], M[:, 1, 0] = -r * np.sin(t), r * np.sin(t)
+    M[:, 2, 2] = np.exp(rng.uniform(-2, 2, n))
+    J = np.zeros((n, 3, 3))
+    J[:, [0, 1, 2], [0, 1, 2]] = np.exp(rng.uniform(-2, 2, n))[:, None]
+    J[:, 0, 1], J[:, 1, 2] = rng.uniform(0, 2, n), rng.uniform(0, 2, n)
+    J += 10 ** rng.uniform(-14, -2, (n, 1, 1)) * rng.standard_normal((n, 3, 3))
+    X = np.concatenate([conj(D), conj(M), conj(J), np.eye(3) + 0.5 * rng.standard_normal((n, 3, 3))]).reshape(-1, 9)
+    ref = ol.call(ol.oracle(), "gmf_eval", kind, alpha, X, 2, 9)[1:]
+    got = contract(2, *record(lib, kind, alpha, 2, 0, X))
+    for g, r_ in zip(got, ref):
+        assert np.array_equal(np.isnan(g), np.isnan(r_))
+    e = np.max([np.nan_to_num(maxrel_rows(g, r_), nan=0.0) for g, r_ in zip(got, ref)], axis=0)
+    assert e.max() <= 5e-12, (name, float(e.max()))
