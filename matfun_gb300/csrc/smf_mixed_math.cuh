@@ -440,7 +440,7 @@ MF_D void smf_spectrum_f(const SmfInF &in, const SmfCoefF &C, SmfSpecF &Sp) {
 #pragma unroll
   for (int i = 0; i < 3; i++) Sp.fl[i] = fun_f<KIND>(Sp.lf[i], C.al);
   if (KIND == LOG) {
-    float mf = E.m, lms = logf(mf);
+    const float mf = E.m, lms = logf(mf), imf = 1.f / mf;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       // near 1 (the log strain of a small deformation): log1p of lambda - 1, taken in float-float from the
@@ -449,7 +449,7 @@ MF_D void smf_spectrum_f(const SmfInF &in, const SmfCoefF &C, SmfSpecF &Sp) {
       const float x = xd[i].hi + xd[i].lo;
       const float tt = (lam[i].hi - 1.f) + lam[i].lo;  // lam.hi - 1 is exact where |tt| <= 0.25 (Sterbenz)
       const bool near1 = fabsf(tt) <= 0.25f, nearm = fabsf(x) <= 0.5f * mf;
-      const float l1 = log1pf(self(near1, tt, x / mf));
+      const float l1 = log1pf(self(near1, tt, x * imf));
       Sp.fl[i] = self(near1, l1, self(nearm, lms + l1, Sp.fl[i]));
     }
   }
