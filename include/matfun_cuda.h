@@ -47,12 +47,13 @@ int smf_cuda_eval_matrix(int kind, double alpha, int64_t n, const double *A, dou
 int gmf_cuda_eval(int kind, double alpha, int64_t n, const double *A, double *F, double *J, double *H, void *stream);
 
 /* Mixed precision (no counterpart in the reference): FP32 arrays in and out, the bulk of the arithmetic in FP32.
- * smf: FP64 is kept for the deviator, the Rayleigh quotients that give the eigenvalues and the eigenvalue
- * differences of the near-coalescent divided-difference branches.  gmf: the spectral analysis (closed-form roots,
- * refinement, branch-cut pair, groups), the confluent series and the residues run in FP64; storage and the J / H
- * assembly in FP32.  Same layouts, kinds and return codes as smf_cuda_eval / smf_cuda_eval_matrix / gmf_cuda_eval.
- * Max relative error (max-norm per output array) against the FP64 results on the tested workloads: <= 1e-6 for smf;
- * gmf: see its tests (stated per kind and order). */
+ * smf: no FP64 arithmetic at all; the deviator, the Rayleigh quotients that give the eigenvalues and the eigenvalue
+ * differences of the near-coalescent divided-difference branches run in float-float (two FP32 words, about 48
+ * significant bits) on the FP32 pipe.  gmf: the spectral analysis (closed-form roots, refinement, branch-cut pair,
+ * groups) and the residues run in FP64, the confluent series in float-float; storage and the J / H assembly in FP32.
+ * Same layouts, kinds and return codes as smf_cuda_eval / smf_cuda_eval_matrix / gmf_cuda_eval.  Error against the
+ * FP64 results of the same FP32 input values, per matrix (max |x - ref| / max |ref| over each matrix's F, J or H),
+ * on the tested workloads: <= 1e-6 for every kind and order wherever the outputs fit FP32's range. */
 int smf_cuda_eval_f32(int kind, double alpha, int64_t n, const float *v, float *F, float *J, float *H, void *stream);
 int smf_cuda_eval_matrix_f32(int kind, double alpha, int64_t n, const float *A, float *F, float *J, float *H,
                              void *stream);
@@ -104,8 +105,9 @@ typedef struct mf_request {
 /* All requests queued on `stream` as one launch of the persistent kernel (the request table is uploaded on `stream`
  * first; gmf requests of log / pow at orders 1-2 with >= 2048 matrices are first ordered by spectral class, three
  * small kernels each, as the single gmf entry point orders large batches).  Returns 0, -1 when a request breaks the
- * rules of its single entry point (then nothing runs), -2 for a CUDA error.  Results equal those of the single entry
- * points to rounding (1e-13 relative, FP64). */
+ * rules of its single entry point or `stream` is being captured into a CUDA graph (then nothing runs: the table is
+ * uploaded from a host copy that lives only during the call; capture matfun_cuda_batched_run instead), -2 for a CUDA
+ * error.  Results equal those of the single entry points to rounding (1e-13 relative, FP64). */
 int matfun_cuda_batched(const mf_request *requests, int count, void *stream);
 /* The same as a plan: the table is validated and uploaded once (synchronously); matfun_cuda_batched_run then only
  * clears the tile cursor and launches, so it can be captured in a CUDA graph and replayed.  The arrays the requests
@@ -120,8 +122,10 @@ int matfun_cuda_batched_free(void *plan);
  * on first use.  The first call on a device looks up that array's device address (cudaGetSymbolAddress) with the
  * device current; make that first call before capturing a stream.  All calls share the array and it keeps the last
  * call's table: calls whose launches overlap on the GPU (different streams, no ordering between them) race and give
- * wrong results.  Returns 0, -1 (an invalid request), -2 (CUDA error), -4 (the table -- 72 bytes per request plus its
- * coefficients, about 2.5 KB for gmf and 0.3 KB for smf -- does not fit the 256 KiB). */
+ * wrong results.  Calls from several host threads on one stream are queued whole, one after the other (a lock covers
+ * the table copy and the launch).  Returns 0, -1 (an invalid request, or `stream` is being captured: the table is
+ * copied from a host copy that lives only during the call), -2 (CUDA error), -4 (the table -- 72 bytes per request
+ * plus its coefficients, about 2.5 KB for gmf and 0.3 KB for smf -- does not fit the 256 KiB). */
 int matfun_cuda_batched_noalloc(const mf_request *requests, int count, void *stream);
 
 /* Tuning of the persistent launch (set by the autotuner, matfun_gb300/autotune.py): CTAs per SM (1..8) and whether
@@ -178,15 +182,6 @@ int smf_xla_ffi_api_version(void);
 /* Diagnostic (no counterpart in the reference): the measured FP64 fused-multiply-add throughput of the current GPU
  * in TFLOP/s, the bound of the FP64 kernels of this library.  Returns 0, or -1 / -2 like the entry points above. */
 int matfun_cuda_fp64_peak(double *tflops);
-
-/* Diagnostic (no counterpart in the reference): the FP32 symmetric eigensystem of smf_cuda_eval_f32 /
- * smf_cuda_eval_matrix_f32 on n matrices (mat: 9-entry rows, else Voigt 6-vectors), 64 floats per matrix into out:
- * its intermediate values (0-43: the normalised deviator g0..g5, p, q, r, the root, v, u, w, the shift, the 2x2
- * block b11, b22, b12 as float-float, jx, jy, jr, cos, sin, the squared norms of v, r1, r2 as float-float, the Gram
- * entries, the mean as float-float, the deviator's scale and its bit pattern) and results (44-49 eigenvalues as
- * float-float, 50-58 V row-major, 59-61 the deviator's eigenvalues, 62 the mean), asynchronous on the stream.
- * Returns 0, -1 (n < 0 or a NULL array with n > 0), -2 (CUDA error). */
-int matfun_cuda_smf_f32_probe(int mat, int64_t n, const float *x, float *out, void *stream);
 
 /* version string of this library (no counterpart in the reference's CUDA header; cf. smf_version, matfun.h:51) */
 const char *matfun_cuda_version(void);

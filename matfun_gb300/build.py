@@ -123,22 +123,37 @@ def build_oracle():
     return lib
 
 
-REFERENCE_ROOT = "/root/reference"
+REF_OUT = os.path.join(ROOT, "oracle", "_ref")
+REF_ROOT_FILE = os.path.join(REF_OUT, "REFERENCE_ROOT")  # the tree the last build_reference_oracle used
+
+
+def _is_reference_tree(path):
+    return bool(path) and os.path.isdir(os.path.join(path, "c", "src"))
 
 
 def reference_root():
-    """the reference source tree, where it is present (the build host; not the GPU hosts)"""
-    return REFERENCE_ROOT if os.path.isdir(os.path.join(REFERENCE_ROOT, "c", "src")) else None
+    """the reference source tree, where it is present: the MATFUN_REFERENCE_ROOT environment variable, else the tree
+    the reference oracle was last built from (recorded by build_reference_oracle); None on hosts without it"""
+    cand = [os.environ.get("MATFUN_REFERENCE_ROOT")]
+    try:
+        with open(REF_ROOT_FILE) as f:
+            cand.append(f.read().strip())
+    except OSError:
+        pass
+    return next((c for c in cand if _is_reference_tree(c)), None)
 
 
-def build_reference_oracle(ref=REFERENCE_ROOT):
+def build_reference_oracle(ref):
     """the reference's own CPU library (oracle/_ref/libmatfun_ref.so) and its CUDA kernels as an sm_103a cubin
-    (oracle/_ref/matfun_cuda_ref.cubin), only where the reference sources are present"""
-    if not os.path.isdir(os.path.join(ref, "c", "src")):
+    (oracle/_ref/matfun_cuda_ref.cubin), built from the reference tree `ref` where it lies; None when `ref` is not
+    a reference tree"""
+    if not _is_reference_tree(ref):
         return None
     subprocess.run(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={ref}", "all"], cwd=ROOT,
                    check=True)
-    return os.path.join(ROOT, "oracle", "_ref", "libmatfun_ref.so")
+    with open(REF_ROOT_FILE, "w") as f:
+        f.write(os.path.abspath(ref) + "\n")
+    return os.path.join(REF_OUT, "libmatfun_ref.so")
 
 
 def build_ref_gpu_timer():

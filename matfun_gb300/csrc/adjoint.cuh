@@ -78,13 +78,9 @@ __global__ void __launch_bounds__(SADJ_TPB) smf_adjoint_kernel_f32(int64_t n, co
 template <int KIND, int ORDER, typename T>
 cudaError_t gmf_adjoint_one(unsigned blocks, int64_t n, const T *A, const T *W, const T *V, T *F, T *Abar, T *JV,
                             T *HWV, const GmfCoef &C, cudaStream_t st, const int *idx = nullptr) {
-  static bool attr = false;  // per instantiation (idempotent)
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(gmf_adjoint_kernel<KIND, ORDER, T>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GadjSmem));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};  // per instantiation, one bit per device
+  const cudaError_t e = smem_limit_per_device(gmf_adjoint_kernel<KIND, ORDER, T>, (int)sizeof(GadjSmem), attr);
+  if (e != cudaSuccess) return e;
   gmf_adjoint_kernel<KIND, ORDER, T><<<blocks, GADJ_TPB, sizeof(GadjSmem), st>>>(n, A, W, V, F, Abar, JV, HWV, C,
                                                                                   idx);
   return cudaGetLastError();

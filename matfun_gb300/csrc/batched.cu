@@ -253,12 +253,8 @@ cudaError_t launch_orders(const Table &T, unsigned char *ord_base, cudaStream_t 
 }
 
 cudaError_t prepare_kernel() {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  const cudaError_t e =
-      cudaFuncSetAttribute(batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
-  if (e == cudaSuccess) done = true;
-  return e;
+  static std::atomic<unsigned long long> done{0};  // one bit per device
+  return smem_limit_per_device(batched_kernel, (int)smem_bytes(), done);
 }
 
 cudaError_t launch_table(const unsigned char *dev_table, const Table &T, unsigned long long *cursor,
@@ -276,6 +272,14 @@ cudaError_t launch_table(const unsigned char *dev_table, const Table &T, unsigne
                                                      (const long long *)(dev_table + T.off_tiles), cursor,
                                                      dev_table + T.off_coef);
   return cudaGetLastError();
+}
+
+// true while `st` is being captured into a CUDA graph: the two batched entry points that take a request array
+// upload it from a host copy that lives only until they return (and matfun_cuda_batched may reallocate its buffer),
+// so they refuse a capturing stream; matfun_cuda_batched_plan / _run are the form to capture
+bool capturing(cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
 }
 
 struct Plan {
@@ -303,9 +307,10 @@ extern "C" int matfun_cuda_batched(const mf_request *requests, int count, void *
   if (T.count == 0) return 0;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -2;
+  const cudaStream_t st = (cudaStream_t)stream;
+  if (capturing(st)) return -1;
   Scratch &S = g_scratch[dev];
   std::lock_guard<std::mutex> lock(S.mu);
-  const cudaStream_t st = (cudaStream_t)stream;
   const size_t ord_at = align16(T.bytes.size()) + 16;  // order region after the table and the cursor
   const size_t need = ord_at + T.ord_bytes;
   if (S.size < need) {
@@ -400,17 +405,17 @@ extern "C" int matfun_cuda_batched_noalloc(const mf_request *requests, int count
   if (16 + T.bytes.size() > NOALLOC_BYTES) return -4;  // the table does not fit the fixed scratch array
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -2;
-  unsigned char *base = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {  // first call on this device: the device address of the array, with it current
-      void *p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return -2;
-      g_noalloc_addr[dev] = (unsigned char *)p;
-    }
-    base = g_noalloc_addr[dev];
-  }
   const cudaStream_t st = (cudaStream_t)stream;
+  if (capturing(st)) return -1;
+  // The lock covers the set-up and the queueing of the table copy and the launch, so that two host threads calling
+  // on the same stream queue copy A, launch A, copy B, launch B and never copy B before launch A.
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {  // first call on this device: the device address of the array, with it current
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return -2;
+    g_noalloc_addr[dev] = (unsigned char *)p;
+  }
+  unsigned char *base = g_noalloc_addr[dev];
   // the cursor (first 16 bytes) is cleared by launch_table; the table follows it
   cudaError_t e = cudaMemcpyAsync(base + 16, T.bytes.data(), T.bytes.size(), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = launch_table(base + 16, T, (unsigned long long *)base, st);

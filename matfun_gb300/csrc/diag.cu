@@ -1,13 +1,10 @@
-// diag.cu -- diagnostic entry points: the FP64 fused-multiply-add throughput of the current GPU, the denominator of
-// the FP64 roofline that bounds the FP64 kernels of this library (reported by the benchmark beside the HBM one); and
-// a probe of the FP32 symmetric eigensystem that returns its intermediate values per matrix, for comparison with a
-// host build of the same header.
+// diag.cu -- the FP64 fused-multiply-add throughput of the current GPU: the denominator of the FP64 roofline that
+// bounds the FP64 kernels of this library (reported by the benchmark beside the HBM one).
 #include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #include "../../include/matfun_cuda.h"
-#include "smf_mixed_math.cuh"
 
 namespace {
 constexpr int CHAINS = 8, ITER = 2048;
@@ -25,23 +22,7 @@ __global__ void dfma_chains(double *out, double a, double b) {
   for (int c = 0; c < CHAINS; c++) s += x[c];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
-template <bool MAT>
-__global__ void smf_f32_probe_kernel(int64_t n, const float *__restrict__ x, float *__restrict__ out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) mf::smf_f32_probe_one<MAT>(x + (MAT ? 9 : 6) * i, out + mf::SMF_F32_PROBE * i);
-}
 }  // namespace
-
-extern "C" int matfun_cuda_smf_f32_probe(int mat, int64_t n, const float *x, float *out, void *stream) {
-  if (n < 0 || (n > 0 && (!x || !out))) return -1;
-  if (n == 0) return 0;
-  if (n > (int64_t)INT_MAX * 128) return -2;
-  const unsigned blocks = (unsigned)((n + 127) / 128);
-  const cudaStream_t st = (cudaStream_t)stream;
-  if (mat) smf_f32_probe_kernel<true><<<blocks, 128, 0, st>>>(n, x, out);
-  else smf_f32_probe_kernel<false><<<blocks, 128, 0, st>>>(n, x, out);
-  return cudaGetLastError() == cudaSuccess ? 0 : -2;
-}
 
 extern "C" int matfun_cuda_fp64_peak(double *tflops) {
   if (!tflops) return -1;

@@ -443,13 +443,9 @@ template <int KIND, int ORDER, typename T>
 cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const T *A, T *F, T *J, T *H,
                            const GmfCoef &C, const int *idx = nullptr, const double *roots = nullptr,
                            const unsigned char *keys = nullptr) {
-  static bool attr = false;  // once per instantiation (idempotent; a racing second call sets the same value)
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(gmf_kernel<KIND, ORDER, T>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GmfSmem));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};  // per instantiation, one bit per device
+  const cudaError_t e = smem_limit_per_device(gmf_kernel<KIND, ORDER, T>, (int)sizeof(GmfSmem), attr);
+  if (e != cudaSuccess) return e;
   gmf_kernel<KIND, ORDER, T><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C, idx, roots, keys);
   return cudaGetLastError();
 }

@@ -2,10 +2,27 @@
 // (one per family and kind).  Arguments are validated and normalised by the caller: n > 0, the grid within limits,
 // sqrt of the general family arrives as pow with al = 0.5, al = 0.5 for smf sqrt and 0 for exp / log.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace mf {
+
+// Raises a kernel's dynamic shared memory limit to `bytes` on the current device, once per device.
+// cudaFuncSetAttribute acts on the current device's copy of the kernel only, so a process that launches the kernel
+// on several GPUs needs the call on each of them; `done` holds one bit per device (devices 0..63) and may be set by
+// several host threads at once.
+template <typename Kernel>
+cudaError_t smem_limit_per_device(Kernel kernel, int bytes, std::atomic<unsigned long long> &done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? 1ull << dev : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
 #define MF_SMF_DECL(k)                                                                                          \
   cudaError_t smf_launch_##k(double al, int64_t n, const double *x, bool mat, double *F, double *J, double *H, \
                              cudaStream_t st, int *asym = nullptr, bool reorder = true);

@@ -209,12 +209,8 @@ struct SmfEigF {
   float V[3][3];
 };
 
-// dbg (null in the kernels): the routine's intermediate values, SMF_F32_PROBE_EIG floats in the order of the record
-// at its end, for a probe that compares them with a host build of this header
-constexpr int SMF_F32_PROBE_EIG = 44, SMF_F32_PROBE = 64;
-
 template <int KIND, bool LO>
-MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E, float *dbg = nullptr) {
+MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E) {
   constexpr float SQRT6 = 2.4494897f, TWO_PI_3 = 2.0943951f;
   // power-of-two scaling from the largest magnitude (integer compare of the bit patterns: NaN sorts above Inf)
   int kb = 0;
@@ -341,13 +337,6 @@ MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E, float *dbg = nullptr) {
 #pragma unroll
     for (int i = 0; i < 3; i++) E.lam[i] = E.xd[i] = {nanv, nanv};
   }
-  if (dbg) {
-    const float rec[SMF_F32_PROBE_EIG] = {
-        g0, g1, g2, g3, g4, g5, p, q, r, sh, v[0], v[1], v[2], u[0], u[1], u[2], w[0], w[1], w[2], mu, b11.hi,
-        b11.lo, b22.hi, b22.lo, b12.hi, b12.lo, jx, jy, jr, cs, sn, nv.hi, nv.lo, n1.hi, n1.lo, n2.hi, n2.lo,
-        g01.hi + g01.lo, g02.hi + g02.lo, g12.hi + g12.lo, m.hi, m.lo, dsc, __int_as_float(kd)};
-    for (int k = 0; k < SMF_F32_PROBE_EIG; k++) dbg[k] = rec[k];
-  }
 }
 
 // Voigt input (FP32 values)
@@ -374,28 +363,6 @@ MF_D void sym_in_f(const float *xi, SmfInF &in) {
     ffl t = two_sum(xi[ia[k]], xi[ib[k]]);
     in.o[k] = {self(sym, 0.5f * t.hi, nanv), self(sym, 0.5f * t.lo, nanv)};
   }
-}
-
-// one matrix's probe record (SMF_F32_PROBE floats): the intermediate values of smf_eigsys_ff (0-43: g0..g5, p, q,
-// r, root, v, u, w, mu, the 2x2 block b11, b22, b12 as float-float, jx, jy, jr, cos, sin, the squared norms of v,
-// r1, r2 as float-float, the Gram entries v.r1, v.r2, r1.r2, the mean as float-float, the deviator's scale and the
-// bit pattern kd), then its results: eigenvalues as float-float (44-49), V row-major (50-58), the deviator's
-// eigenvalues (59-61), the mean (62)
-template <bool MAT>
-MF_D void smf_f32_probe_one(const float *xi, float *out) {
-  SmfInF in;
-  if (MAT) sym_in_f(xi, in);
-  else voigt_in_f(xi, in);
-  SmfEigF E;
-  smf_eigsys_ff<LOG, MAT>(in, E, out);
-  for (int i = 0; i < 3; i++) {
-    out[SMF_F32_PROBE_EIG + 2 * i] = E.lam[i].hi;
-    out[SMF_F32_PROBE_EIG + 2 * i + 1] = E.lam[i].lo;
-    for (int j = 0; j < 3; j++) out[SMF_F32_PROBE_EIG + 6 + 3 * i + j] = E.V[i][j];
-    out[SMF_F32_PROBE_EIG + 15 + i] = E.xd[i].hi;
-  }
-  out[SMF_F32_PROBE_EIG + 18] = E.m;
-  out[SMF_F32_PROBE_EIG + 19] = 0.f;
 }
 
 // the spectrum of the mixed path, eigenvalues sorted ascending: FP32 eigenvectors V (columns), eigenvalues lf,

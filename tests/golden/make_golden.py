@@ -1,6 +1,6 @@
 """Converts the reference's cross-language golden cases into compact fixtures for the parity tests.
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]     (default: /root/reference)
+    python tests/golden/make_golden.py REFERENCE_ROOT     (the reference source tree)
 
 Reads testdata/cases.txt (smf, Voigt layout: kind alpha tol v[6] F[6] J[36] H[216]) and testdata/cases_general.txt
 (gmf, matrix layout: kind alpha tol A[9] F[9] J[81] H[729]) of the reference -- F, J, H computed by the reference's
@@ -30,6 +30,8 @@ def convert(src, dst, nin, nf):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT")
+    ref = sys.argv[1]
     convert(os.path.join(ref, "testdata", "cases.txt"), os.path.join(HERE, "cases_smf.npz"), 6, 6)
     convert(os.path.join(ref, "testdata", "cases_general.txt"), os.path.join(HERE, "cases_gmf.npz"), 9, 9)

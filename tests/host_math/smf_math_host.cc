@@ -105,11 +105,3 @@ extern "C" int smf_math_f64(int kind, double al, int64_t n, const double *v6, do
   }
 }
 
-// the probe record of matfun_cuda_smf_f32_probe (SMF_F32_PROBE floats per matrix) from this host build
-extern "C" int smf_f32_probe(int mat, int64_t n, const float *x, float *out) {
-  for (int64_t i = 0; i < n; i++) {
-    if (mat) smf_f32_probe_one<true>(x + 9 * i, out + SMF_F32_PROBE * i);
-    else smf_f32_probe_one<false>(x + 6 * i, out + SMF_F32_PROBE * i);
-  }
-  return 0;
-}

@@ -39,6 +39,10 @@ def _requests(seed):
         if fam != "gmf" and i % 2:
             t = t.float()
         reqs.append(batched.request(fam, kind, t, order=i % 3, alpha=0.3 if kind == "pow" else None))
+    # a gmf log order-2 request large enough (>= 2048 matrices) that matfun_cuda_batched orders it by spectral class,
+    # which the no-allocation form, having no room for the permutation, evaluates in its given order
+    t = torch.from_numpy(w.c1_gmf_groups(3000, seed=seed)).cuda()
+    reqs.append(batched.request("gmf", "log", t, order=2))
     return reqs
 
 
@@ -74,6 +78,45 @@ def test_noalloc_matches_batched_on_two_calls(lib):
         for got, exp in zip(_outputs(reqs), expected):
             for a, b in zip(got, exp):
                 assert _close(a, b), f"call {call + 1}"
+
+
+def test_noalloc_allocates_no_device_memory(lib):
+    """after a first call on the device, further calls leave the device's free memory and torch's allocations as
+    they were"""
+    import torch
+
+    from matfun_gb300 import batched
+    reqs = _requests(13)
+    arr = batched._array(reqs)
+    assert lib.matfun_cuda_batched_noalloc(ctypes.cast(arr, ctypes.c_void_p), len(reqs), None) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    used0 = torch.cuda.memory_allocated()
+    for _ in range(3):
+        assert lib.matfun_cuda_batched_noalloc(ctypes.cast(arr, ctypes.c_void_p), len(reqs), None) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_allocated() == used0
+
+
+def test_noalloc_refuses_a_capturing_stream(lib):
+    """the table is copied from host memory that lives only during the call, so a stream being captured into a CUDA
+    graph is refused (-1) with nothing queued"""
+    import torch
+
+    from matfun_gb300 import batched
+    reqs = _requests(17)[:3]
+    arr = batched._array(reqs)
+    st = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(st):
+        with torch.cuda.graph(g, stream=st):
+            r = lib.matfun_cuda_batched_noalloc(ctypes.cast(arr, ctypes.c_void_p), len(reqs),
+                                                ctypes.c_void_p(st.cuda_stream))
+            torch.zeros(1, device="cuda")  # (a node, so that the graph is not empty)
+    assert r == -1
+    torch.cuda.synchronize()
 
 
 def test_noalloc_rejects_a_table_beyond_its_array(lib):
