@@ -179,9 +179,11 @@ void *GmfTangentCuda(void *call_frame);
 /* XLA FFI API version the handlers implement, major * 1000 + minor (reference: cuda/src/matfun_cuda.cu:265) */
 int smf_xla_ffi_api_version(void);
 
-/* Diagnostic (no counterpart in the reference): the measured FP64 fused-multiply-add throughput of the current GPU
- * in TFLOP/s, the bound of the FP64 kernels of this library.  Returns 0, or -1 / -2 like the entry points above. */
+/* Diagnostics (no counterpart in the reference): the measured FP64 / FP32 fused-multiply-add throughput of the
+ * current GPU in TFLOP/s (independent FMA chains on every SM), the pipe bounds of this library's kernels.
+ * Synchronous.  Return 0, or -1 / -2 like the entry points above. */
 int matfun_cuda_fp64_peak(double *tflops);
+int matfun_cuda_fp32_peak(double *tflops);
 
 /* version string of this library (no counterpart in the reference's CUDA header; cf. smf_version, matfun.h:51) */
 const char *matfun_cuda_version(void);

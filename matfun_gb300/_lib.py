@@ -37,6 +37,7 @@ SIGNATURES = {
     "smf_cuda_eval_matrix_host": (ctypes.c_int, _EVAL[:-1]),
     "gmf_cuda_eval_host": (ctypes.c_int, _EVAL[:-1]),
     "matfun_cuda_fp64_peak": (ctypes.c_int, [ctypes.c_void_p]),
+    "matfun_cuda_fp32_peak": (ctypes.c_int, [ctypes.c_void_p]),
     "matfun_cuda_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "matfun_cuda_batched_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "matfun_cuda_batched_plan": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
