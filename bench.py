@@ -53,7 +53,47 @@ def io_bytes(fam, order, elem=8):
 # matrices of each launch (profiles/pipe_counts_all_configs.md).  They turn the measured time of a configuration into
 # its FP64 / FP32 pipe fraction.  None: not counted.
 PIPE_FLOPS = {
-    "gmf/log/2/f64": {"fp64": 6867, "fp32": None},
+    "gmf/log/2/f64": {"fp64": 6739, "fp32": 12399},
+    "gmf/exp/2/f64": {"fp64": 5524, "fp32": 6257},
+    "gmf/sqrt/2/f64": {"fp64": 8719, "fp32": 12237},
+    "gmf/log/2/f32": {"fp64": 2507, "fp32": 40174},
+    "gmf/exp/2/f32": {"fp64": 3143, "fp32": 8193},
+    "gmf/sqrt/2/f32": {"fp64": 4517, "fp32": 39626},
+    "gmf/pow0.3/2/f32": {"fp64": 5178, "fp32": 39843},
+    "gmf/log/tangent/f64": {"fp64": 9034, "fp32": 12450},
+    "smf/log/2/f64/c0": {"fp64": 3009, "fp32": 66},
+    "smf/exp/0/f32": {"fp64": None, "fp32": 1517},
+    "smf/exp/0/f64": {"fp64": 709, "fp32": 14},
+    "smf/exp/1/f32": {"fp64": None, "fp32": 1950},
+    "smf/exp/1/f64": {"fp64": 1109, "fp32": 20},
+    "smf/exp/2/f32": {"fp64": None, "fp32": 3334},
+    "smf/exp/2/f64": {"fp64": 2868, "fp32": 208},
+    "smf/log/0/f32": {"fp64": None, "fp32": 1777},
+    "smf/log/0/f64": {"fp64": 998, "fp32": 22},
+    "smf/log/1/f32": {"fp64": None, "fp32": 2312},
+    "smf/log/1/f64": {"fp64": 1598, "fp32": 41},
+    "smf/log/2/f32": {"fp64": None, "fp32": 3622},
+    "smf/log/2/f64": {"fp64": 3210, "fp32": 242},
+    "smf/sqrt/0/f32": {"fp64": None, "fp32": 1505},
+    "smf/sqrt/0/f64": {"fp64": 661, "fp32": 14},
+    "smf/sqrt/1/f32": {"fp64": None, "fp32": 1854},
+    "smf/sqrt/1/f64": {"fp64": 1004, "fp32": 14},
+    "smf/sqrt/2/f32": {"fp64": None, "fp32": 3413},
+    "smf/sqrt/2/f64": {"fp64": 2640, "fp32": 226},
+    "smf/pow/0/f32": {"fp64": None, "fp32": 1664},
+    "smf/pow/0/f64": {"fp64": 986, "fp32": 14},
+    "smf/pow/1/f32": {"fp64": None, "fp32": 2433},
+    "smf/pow/1/f64": {"fp64": 2004, "fp32": 31},
+    "smf/pow/2/f32": {"fp64": None, "fp32": 3928},
+    "smf/pow/2/f64": {"fp64": 3641, "fp32": 242},
+    "smf/log/vjp/f64": {"fp64": 1518, "fp32": 49},
+    "smf/log/hvp/f64": {"fp64": 2306, "fp32": 66},
+    "smf/log/vjp/f32": {"fp64": None, "fp32": 2262},
+    "smf/log/hvp/f32": {"fp64": None, "fp32": 2790},
+    "gmf/pow0.3/vjp/f64": {"fp64": 5233, "fp32": 10693},
+    "gmf/pow0.3/hvp/f64": {"fp64": 10403, "fp32": 24383},
+    "gmf/pow0.3/vjp/f32": {"fp64": 3927, "fp32": 29029},
+    "gmf/pow0.3/hvp/f32": {"fp64": 5826, "fp32": 70819},
 }
 
 
@@ -339,11 +379,13 @@ def err_stats(got, ref):
     smax = s.max(dim=1).values
     rows = d.max(dim=1).values / smax.clamp_min(1e-300)
     fits = (smax <= 3.4028234663852886e38) & (smax >= 1.1754943508222875e-38)
+    nan_rows = nan_b.all(dim=1)  # matrices outside the domain: NaN in both
     rf = rows[fits]
     return {"batch": float(d.max() / s.max().clamp_min(1e-300)),
             "per_matrix_max": float(rf.max()) if rf.numel() else None,
             "per_matrix_p99_99": float(torch.quantile(rf[:1 << 20].float(), 0.9999)) if rf.numel() else None,
-            "rows_outside_fp32_range": int((~fits).sum()), "nan_mismatch_rows": int((nan_a != nan_b).any(1).sum())}
+            "nan_rows": int(nan_rows.sum()), "rows_outside_fp32_range": int((~fits & ~nan_rows).sum()),
+            "nan_mismatch_rows": int((nan_a != nan_b).any(1).sum())}
 
 
 def pair_f32_f64(fn32, fn64, x32, nf, kind, alpha, order, steps, dev, sample=65536):
@@ -794,16 +836,21 @@ def run_ours(args, rank, world, local):
         call = CpuCall("gmf_eval", kind, args.alpha, group_sample(X, args.cpu_sample), 2)
         out["cpu_baseline"] = cpu_log = cpu_baseline(call, args.cpu_budget,
                                                      f"gmf_eval {args.kind} order 2 on the C1 groups")
-    if rank == 0:
+    want = set(args.sections.split(",")) if args.sections else None
+    run = lambda name: rank == 0 and (want is None or name in want)
+    if run("c1_kinds"):
         section(out, "c1_kinds", lambda: c1_kinds(lib, args, dev, pk, X))
+    if run("smf_c0"):
         section(out, "smf_c0", lambda: smf_c0(lib, args, dev, pk))
-    if rank == 0 and not args.no_mixed:
+    if run("mixed") and not args.no_mixed:
         section(out, "mixed", lambda: mixed_sweep(lib, args, dev, pk))
+    if run("mixed_gmf") and not args.no_mixed:
         section(out, "mixed_gmf", lambda: mixed_gmf(lib, args, dev, pk, cpu_log))
-    if rank == 0 and not args.no_adjoint:
+    if run("adjoint") and not args.no_adjoint:
         section(out, "adjoint", lambda: adjoint_vs_materialised(lib, args, dev, pk))
+    if run("tangent") and not args.no_adjoint:
         section(out, "tangent", lambda: tangent_vs_materialised(lib, args, dev, pk, X))
-    if rank == 0 and not args.no_batched:
+    if run("batched") and not args.no_batched:
         section(out, "batched", lambda: batched_c3(lib, args, dev, pk))
     if rank == 0:
         out["pipe_peaks_tflops"] = {"fp64": pk.fp64, "fp32": pk.fp32}
@@ -926,6 +973,9 @@ def main():
     ap.add_argument("--mixed-steps", type=int, default=5)
     ap.add_argument("--gmf-mixed-n", type=int, default=1 << 20)
     ap.add_argument("--smf-n", type=int, default=1 << 16, help="matrices of the C0 section (smf log order 2)")
+    ap.add_argument("--sections", default="",
+                    help="comma-separated sections to run after the headline (default: all): c1_kinds, smf_c0, mixed, "
+                         "mixed_gmf, adjoint, tangent, batched")
     ap.add_argument("--count-pass", action="store_true",
                     help="one small launch per configuration (for ncu counters), no timing")
     args = ap.parse_args()

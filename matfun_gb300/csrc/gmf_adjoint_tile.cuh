@@ -35,6 +35,141 @@ MF_D void mTm3(const T *X, const T *Y, T *Z) {  // Z = X^T Y
 template <typename T>
 MF_D T scale_out(T v, T sc) { return v * sc; }
 
+// The contractions of one matrix's record (r_0 = I, r_1, r_2; D2' times s1, D3' times s2) with the directions, in the
+// compute type TC (the record and directions rounded to TC first), ABS: of the absolute values of record and
+// directions (the bound of the terms of each entry):
+//   o[0] = Abar / sc1 = sum_m r_m^T (sum_n D2'_mn W r_n^T)
+//   o[1] = JV / sc1   = sum_m r_m (sum_n D2'_mn V r_n)
+//   o[2] = HWV / sc2  = sum_p (X_p^T W r_p^T + r_p^T W X_p^T),  X_p = sum_mn D3'_mnp r_m V r_n
+// (only those asked for: dA, dJ, dH)
+template <int ORDER, typename TC, bool ABS>
+MF_D void gadj_contract(const GmfRec &R, double s1, double s2, const double *w, const double *v, bool dA, bool dJ,
+                        bool dH, TC o[3][9]) {
+  auto rd = [](double x) { return ABS ? (TC)fabs(x) : (TC)x; };
+  TC r[3][9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    r[0][k] = k % 4 == 0 ? TC(1) : TC(0);
+    r[1][k] = rd(R.r1[k]);
+    r[2][k] = rd(R.r2[k]);
+  }
+  TC D2s[6], D3s[10];
+#pragma unroll
+  for (int k = 0; k < 6; k++) D2s[k] = rd(R.D2[k] * s1);
+#pragma unroll
+  for (int k = 0; k < 10; k++) D3s[k] = ORDER >= 2 ? rd(R.D3[k] * s2) : TC(0);
+  const TC D2m[3][3] = {{D2s[0], D2s[3], D2s[4]}, {D2s[3], D2s[1], D2s[5]}, {D2s[4], D2s[5], D2s[2]}};
+  TC Wl[9], Vl[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) { Wl[k] = dA | dH ? rd(w[k]) : TC(0); Vl[k] = dJ | dH ? rd(v[k]) : TC(0); }
+  TC Gw[3][9];  // W r_n^T
+  if (dA || dH) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) Gw[0][k] = Wl[k];
+    mmT3(Wl, r[1], Gw[1]);
+    mmT3(Wl, r[2], Gw[2]);
+  }
+  if (dA) {
+    TC acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) acc[k] = TC(0);
+#pragma unroll
+    for (int mm = 0; mm < 3; mm++) {
+      TC Hm[9], Tm[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gw[0][k] + D2m[mm][1] * Gw[1][k] + D2m[mm][2] * Gw[2][k];
+      if (mm == 0) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[k] += Hm[k];
+      } else {
+        mTm3(r[mm], Hm, Tm);
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[k] += Tm[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) o[0][k] = acc[k];
+  }
+  TC Gv[3][9];  // V r_n
+  if (dJ || dH) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) Gv[0][k] = Vl[k];
+    mm3(Vl, r[1], Gv[1]);
+    mm3(Vl, r[2], Gv[2]);
+  }
+  if (dJ) {
+    TC acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) acc[k] = TC(0);
+#pragma unroll
+    for (int mm = 0; mm < 3; mm++) {
+      TC Hm[9], Tm[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gv[0][k] + D2m[mm][1] * Gv[1][k] + D2m[mm][2] * Gv[2][k];
+      if (mm == 0) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[k] += Hm[k];
+      } else {
+        mm3(r[mm], Hm, Tm);
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[k] += Tm[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) o[1][k] = acc[k];
+  }
+  if (ORDER >= 2 && dH) {
+    TC X[3][9];
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+      for (int k = 0; k < 9; k++) X[p][k] = TC(0);
+#pragma unroll
+    for (int mm = 0; mm < 3; mm++)
+#pragma unroll
+      for (int nn = 0; nn < 3; nn++) {
+        TC M[9];
+        if (mm == 0) {
+#pragma unroll
+          for (int k = 0; k < 9; k++) M[k] = Gv[nn][k];
+        } else {
+          mm3(r[mm], Gv[nn], M);
+        }
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+          int i0 = mm, i1 = nn, i2 = p;
+          sort3(i0, i1, i2);
+          const TC d = D3s[sym3(i0, i1, i2)];
+#pragma unroll
+          for (int k = 0; k < 9; k++) X[p][k] += d * M[k];
+        }
+      }
+    TC acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) acc[k] = TC(0);
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+      TC T1[9], T2[9], T3[9];
+      mTm3(X[p], Gw[p], T1);  // X_p^T (W r_p^T)
+      mmT3(Wl, X[p], T2);     // W X_p^T
+      if (p == 0) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) T3[k] = T2[k];
+      } else {
+        mTm3(r[p], T2, T3);   // r_p^T W X_p^T
+      }
+#pragma unroll
+      for (int k = 0; k < 9; k++) acc[k] += T1[k] + T3[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) o[2][k] = acc[k];
+  }
+}
+
+// FP32 adjoints: a matrix is recomputed from its FP64 record where an output's term bound exceeds this many times
+// its largest |entry| (cancellation amplifies the FP32 rounding of the record by that ratio)
+constexpr float GADJ_F32_AMP = 8.f;
+
 // shared memory of one tile
 template <int TPB>
 struct GadjSmemT {
@@ -95,129 +230,45 @@ MF_D void gmf_adjoint_tile(int64_t base, int cnt, const T *__restrict__ A, const
     const bool f1 = MIXED & isfinite(R.sc1) & (R.sc1 != 0.0), f2 = MIXED & isfinite(rsc2) & (rsc2 != 0.0);
     const double s1 = sel(f1, R.sc1, 1.0), s2 = sel(f2, rsc2, 1.0);
     const T sc1 = (T)sel(f1, 1.0, R.sc1), sc2 = (T)sel(f2, 1.0, rsc2);
-    T r[3][9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      r[0][k] = k % 4 == 0 ? T(1) : T(0);
-      r[1][k] = (T)R.r1[k];
-      r[2][k] = (T)R.r2[k];
-    }
-    T D2s[6], D3s[10];
-#pragma unroll
-    for (int k = 0; k < 6; k++) D2s[k] = (T)(R.D2[k] * s1);
-#pragma unroll
-    for (int k = 0; k < 10; k++) D3s[k] = ORDER >= 2 ? (T)(R.D3[k] * s2) : T(0);
-    const T D2m[3][3] = {{D2s[0], D2s[3], D2s[4]}, {D2s[3], D2s[1], D2s[5]}, {D2s[4], D2s[5], D2s[2]}};
     if (F) {
 #pragma unroll
       for (int k = 0; k < 9; k++) S.out[0][mine * 9 + k] = R.F[k];
     }
     const double *w = S.w + mine * 9, *v = S.v + mine * 9;
-    T Wl[9], Vl[9];
+    const bool dA = Abar != nullptr, dJ = JV != nullptr, dH = ORDER >= 2 && HWV != nullptr;
+    double o[3][9];
+    if constexpr (!MIXED) {
+      gadj_contract<ORDER, double, false>(R, s1, s2, w, v, dA, dJ, dH, o);
+    } else {
+      // FP32: the record rounded once and contracted in FP32, and the same contraction of the absolute values (the
+      // bound of the terms); an output whose bound exceeds GADJ_F32_AMP times its largest |entry| has cancelled, and
+      // the matrix is contracted again from its FP64 record (near-defective matrices: nearly dependent r_0, r_1, r_2
+      // against large divided differences)
+      float of[3][9], bf[3][9];
+      gadj_contract<ORDER, float, false>(R, s1, s2, w, v, dA, dJ, dH, of);
+      gadj_contract<ORDER, float, true>(R, s1, s2, w, v, dA, dJ, dH, bf);
+      bool wide = false;
 #pragma unroll
-    for (int k = 0; k < 9; k++) { Wl[k] = W ? (T)w[k] : T(0); Vl[k] = V ? (T)v[k] : T(0); }
-    T Gw[3][9];  // W r_n^T
-    if (Abar || HWV) {
+      for (int q = 0; q < 3; q++) {
+        float mo = 0.f, mb = 0.f;
 #pragma unroll
-      for (int k = 0; k < 9; k++) Gw[0][k] = Wl[k];
-      mmT3(Wl, r[1], Gw[1]);
-      mmT3(Wl, r[2], Gw[2]);
-    }
-    if (Abar) {  // sc1 sum_m r_m^T (sum_n D2'_mn W r_n^T)
-      T acc[9];
-#pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] = T(0);
-#pragma unroll
-      for (int mm = 0; mm < 3; mm++) {
-        T Hm[9], Tm[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gw[0][k] + D2m[mm][1] * Gw[1][k] + D2m[mm][2] * Gw[2][k];
-        if (mm == 0) {
-#pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += Hm[k];
-        } else {
-          mTm3(r[mm], Hm, Tm);
-#pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += Tm[k];
-        }
+        for (int k = 0; k < 9; k++) { mo = fmaxf(mo, fabsf(of[q][k])); mb = fmaxf(mb, bf[q][k]); }
+        wide = wide | (mb > GADJ_F32_AMP * mo);
       }
+      if (wide) {
+        gadj_contract<ORDER, double, false>(R, s1, s2, w, v, dA, dJ, dH, o);
+      } else {
 #pragma unroll
-      for (int k = 0; k < 9; k++) S.out[1][mine * 9 + k] = scale_out(acc[k], sc1);
-    }
-    T Gv[3][9];  // V r_n
-    if (JV || HWV) {
+        for (int q = 0; q < 3; q++)
 #pragma unroll
-      for (int k = 0; k < 9; k++) Gv[0][k] = Vl[k];
-      mm3(Vl, r[1], Gv[1]);
-      mm3(Vl, r[2], Gv[2]);
-    }
-    if (JV) {  // sc1 sum_m r_m (sum_n D2'_mn V r_n)
-      T acc[9];
-#pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] = T(0);
-#pragma unroll
-      for (int mm = 0; mm < 3; mm++) {
-        T Hm[9], Tm[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) Hm[k] = D2m[mm][0] * Gv[0][k] + D2m[mm][1] * Gv[1][k] + D2m[mm][2] * Gv[2][k];
-        if (mm == 0) {
-#pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += Hm[k];
-        } else {
-          mm3(r[mm], Hm, Tm);
-#pragma unroll
-          for (int k = 0; k < 9; k++) acc[k] += Tm[k];
-        }
+          for (int k = 0; k < 9; k++) o[q][k] = of[q][k];
       }
-#pragma unroll
-      for (int k = 0; k < 9; k++) S.out[2][mine * 9 + k] = scale_out(acc[k], sc1);
     }
-    if (ORDER >= 2 && HWV) {
-      // M_mn = r_m V r_n ; X_p = sum_mn D3'_mnp M_mn ; HWV = sc2 sum_p (X_p^T W r_p^T + r_p^T W X_p^T)
-      T X[3][9];
 #pragma unroll
-      for (int p = 0; p < 3; p++)
-#pragma unroll
-        for (int k = 0; k < 9; k++) X[p][k] = T(0);
-#pragma unroll
-      for (int mm = 0; mm < 3; mm++)
-#pragma unroll
-        for (int nn = 0; nn < 3; nn++) {
-          T M[9];
-          if (mm == 0) {
-#pragma unroll
-            for (int k = 0; k < 9; k++) M[k] = Gv[nn][k];
-          } else {
-            mm3(r[mm], Gv[nn], M);
-          }
-#pragma unroll
-          for (int p = 0; p < 3; p++) {
-            int i0 = mm, i1 = nn, i2 = p;
-            sort3(i0, i1, i2);
-            const T d = D3s[sym3(i0, i1, i2)];
-#pragma unroll
-            for (int k = 0; k < 9; k++) X[p][k] += d * M[k];
-          }
-        }
-      T acc[9];
-#pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] = T(0);
-#pragma unroll
-      for (int p = 0; p < 3; p++) {
-        T T1[9], T2[9], T3[9];
-        mTm3(X[p], Gw[p], T1);  // X_p^T (W r_p^T)
-        mmT3(Wl, X[p], T2);     // W X_p^T
-        if (p == 0) {
-#pragma unroll
-          for (int k = 0; k < 9; k++) T3[k] = T2[k];
-        } else {
-          mTm3(r[p], T2, T3);   // r_p^T W X_p^T
-        }
-#pragma unroll
-        for (int k = 0; k < 9; k++) acc[k] += T1[k] + T3[k];
-      }
-#pragma unroll
-      for (int k = 0; k < 9; k++) S.out[3][mine * 9 + k] = scale_out(acc[k], sc2);
+    for (int k = 0; k < 9; k++) {
+      if (dA) S.out[1][mine * 9 + k] = scale_out(o[0][k], (double)sc1);
+      if (dJ) S.out[2][mine * 9 + k] = scale_out(o[1][k], (double)sc1);
+      if (dH) S.out[3][mine * 9 + k] = scale_out(o[2][k], (double)sc2);
     }
   }
   __syncthreads();

@@ -38,6 +38,7 @@ namespace mf {
 constexpr int GMF_TPB = 128;
 constexpr int GMF_WARPS = GMF_TPB / 32;
 constexpr int GMF_REC = 36;  // r1 (9), r2 (9), D2' (6), D3' (10), sc1, sc2
+constexpr int GMF_RECF = 1100;  // float offset of the FP32 path's record copy in a warp's work area (past 570 floats)
 
 // shared memory layout of one CTA (doubles unless noted)
 struct GmfSmem {
@@ -153,6 +154,122 @@ MF_D void gmf_tangent_warp(const double *rc, const double *Fm, double *wk, int l
     G[lane] = sc1 == 1.0 ? s : sc1 * s;
   }
   __syncwarp();
+}
+
+// ---- phase B for one matrix by the 32 lanes of a warp, in the compute type TC (double: the FP64 path, and the
+// FP32 path's recomputation of a matrix whose contraction cancels; float: the FP32 path).  rc: the record (r1, r2,
+// D2', D3', then the factors sc1, sc2 left to apply); wk: the warp's work area.
+
+// J: Y2[y][m] = sum_n D2'_mn r_n[y] (27, at wk[0]), then T4[x, y] = sum_m r_m[x] Y2[y][m], x <= y (45, at wk[54])
+template <typename TC>
+MF_D void gmfb_t4(const TC *rc, TC *wk, int lane) {
+  const TC *r1 = rc, *r2 = rc + 9;
+  if (lane < 27) {
+    const int y = lane / 3, m = lane % 3;
+    const int i0 = m == 0 ? 0 : (m == 1 ? 3 : 4), i1 = m == 0 ? 3 : (m == 1 ? 1 : 5), i2 = m == 0 ? 4 : (m == 1 ? 5 : 2);
+    const TC d0 = rc[18 + i0], d1 = rc[18 + i1], d2 = rc[18 + i2];
+    wk[lane] = (y % 4 == 0 ? d0 : TC(0)) + d1 * r1[y] + d2 * r2[y];
+  }
+  __syncwarp();
+  for (int t = lane; t < 45; t += 32) {
+    int y = 0;
+    while (sym2(0, y + 1) <= t) y++;
+    const int x = t - sym2(0, y);
+    const TC *yv = wk + 3 * y;
+    wk[54 + t] = (x % 4 == 0 ? yv[0] : TC(0)) + r1[x] * yv[1] + r2[x] * yv[2];
+  }
+  __syncwarp();
+}
+
+// J_abcd = sc1 T4[ac, db] (81 entries, consecutive lanes on consecutive entries)
+template <typename TC, typename T>
+MF_D void gmfb_store_j(const TC *wk, TC sc1, T *o, int lane) {
+  const bool one1 = sc1 == TC(1);  // folded (the common case): no multiply per entry; uniform in the warp
+  for (int w = lane; w < 81; w += 32) {
+    const int a = w / 27, b = (w / 9) % 3, c = (w / 3) % 3, d = w % 3;
+    const int p1 = 3 * a + c, p2 = 3 * d + b;
+    const TC v = wk[54 + sym2(min(p1, p2), max(p1, p2))];
+    o[w] = (T)(one1 ? v : v * sc1);
+  }
+  __syncwarp();
+}
+
+// H: Z[z][mn] = sum_p D3'_mnp r_p[z] (54), Y[y, z][m] = sum_n Z[z][m, n] r_n[y] (135), T6[x, y, z] =
+// sum_m r_m[x] Y[y, z][m] (165, at wk[0]), then the 405 distinct H values T6 + T6 (at wk[165], over Z and Y)
+template <typename TC>
+MF_D void gmfb_u(const TC *rc, TC *wk, const GmfSmem &S, int lane) {
+  const TC *r1 = rc, *r2 = rc + 9, *d3 = rc + 24;
+  TC *T6 = wk, *Zs = wk + 165, *Ys = wk + 165 + 54, *U = wk + 165;
+  for (int t = lane; t < 54; t += 32) {  // (mn: 00 01 02 11 12 22)
+    const int z = t / 6, mn = t % 6;
+    const int mm = mn < 3 ? 0 : (mn < 5 ? 1 : 2), nn = mn < 3 ? mn : (mn < 5 ? mn - 2 : 2);
+    const int i0 = sym3(0, mm, nn);
+    const int i1 = nn <= 1 ? sym3(mm, nn, 1) : (mm <= 1 ? sym3(mm, 1, nn) : sym3(1, mm, nn));
+    const int i2 = sym3(mm, nn, 2);
+    Zs[t] = (z % 4 == 0 ? d3[i0] : TC(0)) + d3[i1] * r1[z] + d3[i2] * r2[z];
+  }
+  __syncwarp();
+  for (int t = lane; t < 135; t += 32) {
+    const unsigned short e = S.ymap[t];
+    const int y = e & 15, z = (e >> 4) & 15, m = e >> 8;
+    const TC *zz = Zs + 6 * z;
+    const int k0 = m == 0 ? 0 : (m == 1 ? 1 : 2), k1 = m == 0 ? 1 : (m == 1 ? 3 : 4), k2 = m == 0 ? 2 : (m == 1 ? 4 : 5);
+    Ys[t] = (y % 4 == 0 ? zz[k0] : TC(0)) + zz[k1] * r1[y] + zz[k2] * r2[y];
+  }
+  __syncwarp();
+  for (int t = lane; t < 165; t += 32) {
+    const unsigned short e = S.t6map[t];
+    const int x = e & 15, y = (e >> 4) & 15, z = e >> 8;
+    const TC *yv = Ys + 3 * sym2(y, z);
+    T6[t] = (x % 4 == 0 ? yv[0] : TC(0)) + r1[x] * yv[1] + r2[x] * yv[2];
+  }
+  __syncwarp();
+  for (int t = lane; t < 405; t += 32) {
+    const unsigned short e = S.umap[t];
+    U[t] = T6[e & 255] + T6[e >> 8];
+  }
+  __syncwarp();
+}
+
+// H_abcdef = sc2 U[hkey] (729 entries, consecutive lanes on consecutive entries)
+template <typename TC, typename T>
+MF_D void gmfb_store_h(const TC *wk, TC sc2, const GmfSmem &S, T *o, int lane) {
+  const TC *U = wk + 165;
+  if (sc2 == TC(1)) {
+    for (int w = lane; w < 729; w += 32) o[w] = (T)U[S.hkey[w]];
+  } else {
+    for (int w = lane; w < 729; w += 32) o[w] = (T)(U[S.hkey[w]] * sc2);
+  }
+  __syncwarp();
+}
+
+// The FP32 path rounds the record to FP32 and contracts it in FP32.  Where the terms of the contraction cancel
+// (near-defective matrices: large divided differences against nearly dependent r_0 = I, r_1, r_2), that rounding is
+// amplified by the ratio of the terms' bound to the result, and the matrix is recomputed from the FP64 record.  The
+// bound of the J entries is B_J = sum_mn |D2'_mn| rho_m rho_n, of the H entries 2 sum_mnp |D3'_mnp| rho_m rho_n rho_p
+// (rho_0 = 1, rho_m = max |r_m|); a matrix whose bound exceeds GMF_F32_AMP times the largest |entry| of its FP32
+// result is recomputed (about 0.5 % (J) and 6 % (H) of random general matrices, under 1 % of the benchmark's).
+constexpr float GMF_F32_AMP = 8.f;
+
+MF_D float warp_max_abs(float v) {  // max |v| over the warp (non-negative floats order as their bit patterns; NaN wins)
+  return __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fabsf(v))));
+}
+
+// the bounds B_J, B_H of a record (every lane computes them)
+MF_D void gmfb_bounds(const float *rc, float &bj, float &bh) {
+  float p1 = 0.f, p2 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 9; k++) { p1 = fmaxf(p1, fabsf(rc[k])); p2 = fmaxf(p2, fabsf(rc[9 + k])); }
+  const float *d2 = rc + 18, *d3 = rc + 24;
+  bj = fabsf(d2[0]) + p1 * (fabsf(d2[1]) * p1 + 2.f * fabsf(d2[3])) + p2 * (fabsf(d2[2]) * p2 + 2.f * fabsf(d2[4])) +
+       2.f * p1 * p2 * fabsf(d2[5]);
+  // sym3 order 000 001 011 111 002 012 112 022 122 222, with the number of index orderings of each
+  const float q[10] = {1.f, p1, p1 * p1, p1 * p1 * p1, p2, p1 * p2, p1 * p1 * p2, p2 * p2, p1 * p2 * p2, p2 * p2 * p2};
+  const float mult[10] = {1.f, 3.f, 3.f, 1.f, 3.f, 6.f, 3.f, 3.f, 3.f, 1.f};
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 10; k++) s += mult[k] * q[k] * fabsf(d3[k]);
+  bh = 2.f * s;
 }
 
 // one tile: matrices base .. base + cnt - 1 by a CTA of GMF_TPB threads (the standalone kernel and the batched
@@ -284,21 +401,22 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
     }
     if (OD >= 1) {
       // the scale factors sc1 / sc2 are folded into D2' / D3' when finite and nonzero; otherwise each output entry
-      // is multiplied by them (keeping the reference's NaN / Inf); rc[34] / rc[35] hold the factor left to apply
-      T *rc = reinterpret_cast<T *>(S.rec) + tid * GMF_REC;
+      // is multiplied by them (keeping the reference's NaN / Inf); rc[34] / rc[35] hold the factor left to apply.
+      // The record stays in FP64 for both storage types (the FP32 path rounds it in phase B).
+      double *rc = S.rec + tid * GMF_REC;
 #pragma unroll
-      for (int k = 0; k < 9; k++) { rc[k] = (T)R.r1[k]; rc[9 + k] = (T)R.r2[k]; }
+      for (int k = 0; k < 9; k++) { rc[k] = R.r1[k]; rc[9 + k] = R.r2[k]; }
       const bool f1 = isfinite(R.sc1) & (R.sc1 != 0.0);
       const double s1 = sel(f1, R.sc1, 1.0);
 #pragma unroll
-      for (int k = 0; k < 6; k++) rc[18 + k] = (T)(R.D2[k] * s1);
-      rc[34] = (T)sel(f1, 1.0, R.sc1);
+      for (int k = 0; k < 6; k++) rc[18 + k] = R.D2[k] * s1;
+      rc[34] = sel(f1, 1.0, R.sc1);
       if (OD >= 2) {
         const bool f2 = isfinite(R.sc2) & (R.sc2 != 0.0);
         const double s2 = sel(f2, R.sc2, 1.0);
 #pragma unroll
-        for (int k = 0; k < 10; k++) rc[24 + k] = (T)(R.D3[k] * s2);
-        rc[35] = (T)sel(f2, 1.0, R.sc2);
+        for (int k = 0; k < 10; k++) rc[24 + k] = R.D3[k] * s2;
+        rc[35] = sel(f2, 1.0, R.sc2);
       }
     }
   }
@@ -307,87 +425,55 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
 
   // ---- phase B: each warp assembles the matrices it finished (its 32 slots), so no CTA barrier separates the two
   // phases: a warp with short series assembles while the others still run theirs
-  T *wk = reinterpret_cast<T *>(S.work[warp]);
+  double *wkd = S.work[warp];
+  float *wkf = reinterpret_cast<float *>(S.work[warp]);
+  float *rcf = wkf + GMF_RECF;  // the FP32 path's copy of the record (past the FP32 work area)
   for (int sl = warp * 32; sl < warp * 32 + 32; sl++) {
     const int mi = S.perm[sl];
     if (mi >= cnt) break;  // the padding slots sort last
-    const T *rc = reinterpret_cast<const T *>(S.rec) + sl * GMF_REC;
-    const T *r1 = rc, *r2 = rc + 9;
+    const double *rcd = S.rec + sl * GMF_REC;
     if constexpr (ORDER == 3) {
-      gmf_tangent_warp(rc, reinterpret_cast<const T *>(S.x) + mi * 9, wk, lane, J ? J + S.gidx[mi] * 9 : nullptr,
-                       H + S.gidx[mi] * 81);
+      gmf_tangent_warp(rcd, S.x + mi * 9, wkd, lane, J ? J + S.gidx[mi] * 9 : nullptr, H + S.gidx[mi] * 81);
       continue;
     }
-    {
-      const T sc1 = rc[34];
-      if (lane < 27) {  // Y2[y][m] = sum_n D2'_mn r_n[y]
-        const int y = lane / 3, m = lane % 3;
-        const int i0 = m == 0 ? 0 : (m == 1 ? 3 : 4), i1 = m == 0 ? 3 : (m == 1 ? 1 : 5), i2 = m == 0 ? 4 : (m == 1 ? 5 : 2);
-        const T d0 = rc[18 + i0], d1 = rc[18 + i1], d2 = rc[18 + i2];
-        wk[lane] = (y % 4 == 0 ? d0 : T(0)) + d1 * r1[y] + d2 * r2[y];
+    T *oj = J + S.gidx[mi] * 81;
+    T *oh = ORDER >= 2 ? H + S.gidx[mi] * 729 : nullptr;
+    if constexpr (sizeof(T) == 8) {
+      gmfb_t4<double>(rcd, wkd, lane);
+      gmfb_store_j<double, T>(wkd, rcd[34], oj, lane);
+      if (ORDER >= 2) {
+        gmfb_u<double>(rcd, wkd, S, lane);
+        gmfb_store_h<double, T>(wkd, rcd[35], S, oh, lane);
       }
+    } else {
+      for (int k = lane; k < GMF_REC; k += 32) rcf[k] = (float)rcd[k];
       __syncwarp();
-      for (int t = lane; t < 45; t += 32) {  // T4[x, y] = sum_m r_m[x] Y2[y][m], x <= y
-        int y = 0;
-        while (sym2(0, y + 1) <= t) y++;
-        const int x = t - sym2(0, y);
-        const T *yv = wk + 3 * y;
-        wk[54 + t] = (x % 4 == 0 ? yv[0] : T(0)) + r1[x] * yv[1] + r2[x] * yv[2];
-      }
+      float bj, bh;
+      gmfb_bounds(rcf, bj, bh);
+      gmfb_t4<float>(rcf, wkf, lane);
+      float m = warp_max_abs(wkf[54 + lane]);
+      if (lane < 13) m = fmaxf(m, fabsf(wkf[54 + 32 + lane]));
+      m = warp_max_abs(m);
       __syncwarp();
-      T *o = J + S.gidx[mi] * 81;
-      const bool one1 = sc1 == T(1);  // folded (the common case): no multiply per entry; uniform in the warp
-      for (int w = lane; w < 81; w += 32) {
-        const int a = w / 27, b = (w / 9) % 3, c = (w / 3) % 3, d = w % 3;
-        const int p1 = 3 * a + c, p2 = 3 * d + b;
-        const T v = wk[54 + sym2(min(p1, p2), max(p1, p2))];
-        if (one1) o[w] = v;
-        else o[w] = v * sc1;
-      }
-      __syncwarp();
-    }
-    if (ORDER < 2) continue;
-    {
-      const T sc2 = rc[35];
-      const T *d3 = rc + 24;
-      T *T6 = wk, *Zs = wk + 165, *Ys = wk + 165 + 54, *U = wk + 165;
-      for (int t = lane; t < 54; t += 32) {  // Z[z][mn] = sum_p D3'_mnp r_p[z]  (mn: 00 01 02 11 12 22)
-        const int z = t / 6, mn = t % 6;
-        const int mm = mn < 3 ? 0 : (mn < 5 ? 1 : 2), nn = mn < 3 ? mn : (mn < 5 ? mn - 2 : 2);
-        const int i0 = sym3(0, mm, nn);
-        const int i1 = nn <= 1 ? sym3(mm, nn, 1) : (mm <= 1 ? sym3(mm, 1, nn) : sym3(1, mm, nn));
-        const int i2 = sym3(mm, nn, 2);
-        Zs[t] = (z % 4 == 0 ? d3[i0] : T(0)) + d3[i1] * r1[z] + d3[i2] * r2[z];
-      }
-      __syncwarp();
-      for (int t = lane; t < 135; t += 32) {  // Y[y, z][m] = sum_n Z[z][m, n] r_n[y]
-        const unsigned short e = S.ymap[t];
-        const int y = e & 15, z = (e >> 4) & 15, m = e >> 8;
-        const T *zz = Zs + 6 * z;
-        const int k0 = m == 0 ? 0 : (m == 1 ? 1 : 2), k1 = m == 0 ? 1 : (m == 1 ? 3 : 4), k2 = m == 0 ? 2 : (m == 1 ? 4 : 5);
-        Ys[t] = (y % 4 == 0 ? zz[k0] : T(0)) + zz[k1] * r1[y] + zz[k2] * r2[y];
-      }
-      __syncwarp();
-      for (int t = lane; t < 165; t += 32) {  // T6[x, y, z] = sum_m r_m[x] Y[y, z][m]
-        const unsigned short e = S.t6map[t];
-        const int x = e & 15, y = (e >> 4) & 15, z = e >> 8;
-        const T *yv = Ys + 3 * sym2(y, z);
-        T6[t] = (x % 4 == 0 ? yv[0] : T(0)) + r1[x] * yv[1] + r2[x] * yv[2];
-      }
-      __syncwarp();
-      // the 405 distinct H values (Z and Y are no longer needed: U takes their place), then the 729 stores
-      for (int t = lane; t < 405; t += 32) {
-        const unsigned short e = S.umap[t];
-        U[t] = T6[e & 255] + T6[e >> 8];
-      }
-      __syncwarp();
-      T *o = H + S.gidx[mi] * 729;
-      if (sc2 == T(1)) {
-        for (int w = lane; w < 729; w += 32) o[w] = U[S.hkey[w]];
+      if (bj > GMF_F32_AMP * m) {  // (uniform in the warp)
+        gmfb_t4<double>(rcd, wkd, lane);
+        gmfb_store_j<double, T>(wkd, rcd[34], oj, lane);
       } else {
-        for (int w = lane; w < 729; w += 32) o[w] = U[S.hkey[w]] * sc2;
+        gmfb_store_j<float, T>(wkf, rcf[34], oj, lane);
       }
-      __syncwarp();
+      if (ORDER >= 2) {
+        gmfb_u<float>(rcf, wkf, S, lane);
+        float mh = 0.f;
+        for (int t = lane; t < 405; t += 32) mh = fmaxf(mh, fabsf(wkf[165 + t]));
+        mh = warp_max_abs(mh);
+        __syncwarp();
+        if (bh > GMF_F32_AMP * mh) {  // (uniform; the FP64 work area covers the record copy, no longer read)
+          gmfb_u<double>(rcd, wkd, S, lane);
+          gmfb_store_h<double, T>(wkd, rcd[35], S, oh, lane);
+        } else {
+          gmfb_store_h<float, T>(wkf, rcf[35], S, oh, lane);
+        }
+      }
     }
   }
 }

@@ -29,6 +29,44 @@ def maxrel_rows(a, b):
     return np.max(d, axis=1) / np.maximum(s, 1e-300)
 
 
+FLT_MAX, FLT_MIN = 3.4028234663852886e38, 1.1754943508222875e-38
+
+
+def maxrel_rows_fp32(got, ref):
+    """per-matrix errors (max |x - ref| / max |ref| of each row) over the rows whose reference lies within FP32's
+    normal range (FP32 storage cannot hold the others) and is not all NaN; NaN positions must agree row by row"""
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    smax = np.max(np.abs(np.where(np.isnan(ref), 0.0, ref)), axis=1)
+    keep = (smax <= FLT_MAX) & (smax >= FLT_MIN) & ~np.isnan(ref).all(axis=1)
+    return maxrel_rows(got[keep], ref[keep])
+
+
+def random_general(n, seed=99):
+    """4 n general 3x3 matrices in four families: diagonalisable with spectra over e^+-3, complex pairs of modulus
+    e^+-2 at random angles beside a real eigenvalue, Jordan blocks (double and triple eigenvalues of modulus e^+-2
+    with unit-scale couplings) perturbed by 1e-14 .. 1e-2, each similarity-transformed by S = N(0, 1) + U(0.5, 4) I;
+    and I + 0.5 N(0, 1)"""
+    rng = np.random.default_rng(seed)
+
+    def conj(M):
+        S = rng.standard_normal((len(M), 3, 3)) + rng.uniform(0.5, 4, (len(M), 1, 1)) * np.eye(3)
+        return S @ M @ np.linalg.inv(S)
+
+    D = np.zeros((n, 3, 3))
+    D[:, [0, 1, 2], [0, 1, 2]] = np.exp(rng.uniform(-3, 3, (n, 3)))
+    r, t = np.exp(rng.uniform(-2, 2, n)), rng.uniform(-3.14, 3.14, n)
+    M = np.zeros((n, 3, 3))
+    M[:, 0, 0] = M[:, 1, 1] = r * np.cos(t)
+    M[:, 0, 1], M[:, 1, 0] = -r * np.sin(t), r * np.sin(t)
+    M[:, 2, 2] = np.exp(rng.uniform(-2, 2, n))
+    J = np.zeros((n, 3, 3))
+    J[:, [0, 1, 2], [0, 1, 2]] = np.exp(rng.uniform(-2, 2, n))[:, None]
+    J[:, 0, 1], J[:, 1, 2] = rng.uniform(0, 2, n), rng.uniform(0, 2, n)
+    J += 10 ** rng.uniform(-14, -2, (n, 1, 1)) * rng.standard_normal((n, 3, 3))
+    return np.concatenate([conj(D), conj(M), conj(J), np.eye(3) + 0.5 * rng.standard_normal((n, 3, 3))])
+
+
 def header_functions(path):
     """names of the functions an include/*.h declares"""
     src = open(path).read()

@@ -274,8 +274,9 @@ def test_fp64_record_random(lib, kind, alpha, name):
 def test_fp32_record_random(adj, kind, alpha, name):
     """the FP32 form (float-float series, record folded and rounded to FP32 once, FP32 contractions) per matrix on
     6000 random general matrices rounded to FP32 (the families of test_fp64_record_random), through the FP32 adjoint
-    tile: F and J^T W with median <= 2e-7 and 99.9th percentile <= 5e-6 per matrix, no matrix beyond 1e-3 (the
-    near-defective tail reaches 4.5e-4 on 60 000), NaN exactly where the oracle has NaN"""
+    tile: F and J^T W with median <= 2e-7 and no matrix beyond 1e-6, NaN exactly where the oracle has NaN.  The
+    near-defective matrices, whose contraction cancels (up to 4.5e-4 on 60 000 with the rounded record alone), are
+    recomputed from the FP64 record"""
     from tests.helpers import maxrel_rows
     rng = np.random.default_rng(99)
     n = 1500
@@ -307,4 +308,4 @@ def test_fp32_record_random(adj, kind, alpha, name):
     for o, r_ in zip(out, ref):
         assert np.array_equal(np.isnan(o), np.isnan(r_))
     e = np.max([np.nan_to_num(maxrel_rows(o.astype(np.float64), r_), nan=0.0) for o, r_ in zip(out, ref)], axis=0)
-    assert np.median(e) <= 2e-7 and np.quantile(e, 0.999) <= 5e-6 and e.max() <= 1e-3, (name, np.median(e), e.max())
+    assert np.median(e) <= 2e-7 and e.max() <= 1e-6, (name, np.median(e), e.max())
