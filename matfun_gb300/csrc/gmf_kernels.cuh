@@ -38,7 +38,6 @@ namespace mf {
 constexpr int GMF_TPB = 128;
 constexpr int GMF_WARPS = GMF_TPB / 32;
 constexpr int GMF_REC = 36;  // r1 (9), r2 (9), D2' (6), D3' (10), sc1, sc2
-constexpr int GMF_RECF = 1100;  // float offset of the FP32 path's record copy in a warp's work area (past 570 floats)
 
 // shared memory layout of one CTA (doubles unless noted)
 struct GmfSmem {
@@ -181,17 +180,25 @@ MF_D void gmfb_t4(const TC *rc, TC *wk, int lane) {
   __syncwarp();
 }
 
-// J_abcd = sc1 T4[ac, db] (81 entries, consecutive lanes on consecutive entries)
-template <typename TC, typename T>
-MF_D void gmfb_store_j(const TC *wk, TC sc1, T *o, int lane) {
+MF_D float warp_max_abs(float v) {  // max |v| over the warp (non-negative floats order as their bit patterns; NaN wins)
+  return __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fabsf(v))));
+}
+
+// J_abcd = sc1 T4[ac, db] (81 entries, consecutive lanes on consecutive entries); MAX: returns the largest |T4| of
+// the matrix (the same in every lane)
+template <typename TC, typename T, bool MAX = false>
+MF_D float gmfb_store_j(const TC *wk, TC sc1, T *o, int lane) {
   const bool one1 = sc1 == TC(1);  // folded (the common case): no multiply per entry; uniform in the warp
+  float mx = 0.f;
   for (int w = lane; w < 81; w += 32) {
     const int a = w / 27, b = (w / 9) % 3, c = (w / 3) % 3, d = w % 3;
     const int p1 = 3 * a + c, p2 = 3 * d + b;
     const TC v = wk[54 + sym2(min(p1, p2), max(p1, p2))];
     o[w] = (T)(one1 ? v : v * sc1);
+    if (MAX) mx = fmaxf(mx, fabsf((float)v));
   }
   __syncwarp();
+  return MAX ? warp_max_abs(mx) : 0.f;
 }
 
 // H: Z[z][mn] = sum_p D3'_mnp r_p[z] (54), Y[y, z][m] = sum_n Z[z][m, n] r_n[y] (135), T6[x, y, z] =
@@ -231,16 +238,27 @@ MF_D void gmfb_u(const TC *rc, TC *wk, const GmfSmem &S, int lane) {
   __syncwarp();
 }
 
-// H_abcdef = sc2 U[hkey] (729 entries, consecutive lanes on consecutive entries)
-template <typename TC, typename T>
-MF_D void gmfb_store_h(const TC *wk, TC sc2, const GmfSmem &S, T *o, int lane) {
+// H_abcdef = sc2 U[hkey] (729 entries, consecutive lanes on consecutive entries); MAX: returns the largest |U| of the
+// matrix (the same in every lane)
+template <typename TC, typename T, bool MAX = false>
+MF_D float gmfb_store_h(const TC *wk, TC sc2, const GmfSmem &S, T *o, int lane) {
   const TC *U = wk + 165;
+  float mx = 0.f;
   if (sc2 == TC(1)) {
-    for (int w = lane; w < 729; w += 32) o[w] = (T)U[S.hkey[w]];
+    for (int w = lane; w < 729; w += 32) {
+      const TC v = U[S.hkey[w]];
+      o[w] = (T)v;
+      if (MAX) mx = fmaxf(mx, fabsf((float)v));
+    }
   } else {
-    for (int w = lane; w < 729; w += 32) o[w] = (T)(U[S.hkey[w]] * sc2);
+    for (int w = lane; w < 729; w += 32) {
+      const TC v = U[S.hkey[w]];
+      o[w] = (T)(v * sc2);
+      if (MAX) mx = fmaxf(mx, fabsf((float)v));
+    }
   }
   __syncwarp();
+  return MAX ? warp_max_abs(mx) : 0.f;
 }
 
 // The FP32 path rounds the record to FP32 and contracts it in FP32.  Where the terms of the contraction cancel
@@ -248,14 +266,12 @@ MF_D void gmfb_store_h(const TC *wk, TC sc2, const GmfSmem &S, T *o, int lane) {
 // amplified by the ratio of the terms' bound to the result, and the matrix is recomputed from the FP64 record.  The
 // bound of the J entries is B_J = sum_mn |D2'_mn| rho_m rho_n, of the H entries 2 sum_mnp |D3'_mnp| rho_m rho_n rho_p
 // (rho_0 = 1, rho_m = max |r_m|); a matrix whose bound exceeds GMF_F32_AMP times the largest |entry| of its FP32
-// result is recomputed (about 0.5 % (J) and 6 % (H) of random general matrices, under 1 % of the benchmark's).
+// result is recomputed and its J (H) stored again (about 0.5 % (J) and 6 % (H) of random general matrices, under
+// 1 % of the benchmark's).
 constexpr float GMF_F32_AMP = 8.f;
+constexpr int GMF_RECF_BJ = GMF_REC, GMF_RECF_BH = GMF_REC + 1;  // the bounds after the FP32 record
 
-MF_D float warp_max_abs(float v) {  // max |v| over the warp (non-negative floats order as their bit patterns; NaN wins)
-  return __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fabsf(v))));
-}
-
-// the bounds B_J, B_H of a record (every lane computes them)
+// the bounds B_J, B_H of a record rounded to FP32
 MF_D void gmfb_bounds(const float *rc, float &bj, float &bh) {
   float p1 = 0.f, p2 = 0.f;
 #pragma unroll
@@ -291,6 +307,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
     if (e == 9 * p) S.gidx[p] = g;
   }
   static_assert(ORDER < 3 || sizeof(T) == 8, "the tangent form is FP64");
+  static_assert(sizeof(GmfState) >= (GMF_REC + 2) * sizeof(float), "the FP32 record and its bounds fit a state slot");
   constexpr int OD = ORDER == 3 ? 2 : ORDER;  // the order of the derivatives the record holds
   if (ORDER == 2) {  // index tables of phase B
     for (int t = tid; t < 405; t += GMF_TPB) {  // t = 45 (ab) + sym2(cd, ef), cd <= ef
@@ -418,6 +435,20 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
         for (int k = 0; k < 10; k++) rc[24 + k] = R.D3[k] * s2;
         rc[35] = sel(f2, 1.0, R.sc2);
       }
+      if constexpr (sizeof(T) == 4) {
+        // the FP32 path's record, rounded once, and the bounds of its contractions, in this matrix's state slot
+        // (free once gmf_finish has read it)
+        float *rf = reinterpret_cast<float *>(&S.state[mine]);
+#pragma unroll
+        for (int k = 0; k < (OD >= 2 ? GMF_REC : 24); k++) rf[k] = (float)rc[k];
+        rf[34] = (float)rc[34];
+        rf[35] = OD >= 2 ? (float)rc[35] : 1.f;
+        if (OD < 2) {
+#pragma unroll
+          for (int k = 24; k < 34; k++) rf[k] = 0.f;
+        }
+        gmfb_bounds(rf, rf[GMF_RECF_BJ], rf[GMF_RECF_BH]);
+      }
     }
   }
   if (ORDER < 1) return;
@@ -427,7 +458,6 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   // phases: a warp with short series assembles while the others still run theirs
   double *wkd = S.work[warp];
   float *wkf = reinterpret_cast<float *>(S.work[warp]);
-  float *rcf = wkf + GMF_RECF;  // the FP32 path's copy of the record (past the FP32 work area)
   for (int sl = warp * 32; sl < warp * 32 + 32; sl++) {
     const int mi = S.perm[sl];
     if (mi >= cnt) break;  // the padding slots sort last
@@ -446,32 +476,21 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
         gmfb_store_h<double, T>(wkd, rcd[35], S, oh, lane);
       }
     } else {
-      for (int k = lane; k < GMF_REC; k += 32) rcf[k] = (float)rcd[k];
-      __syncwarp();
-      float bj, bh;
-      gmfb_bounds(rcf, bj, bh);
+      // FP32: contract and store the rounded record; where its bound exceeds GMF_F32_AMP times the largest entry
+      // (uniform in the warp), contract the FP64 record and store the matrix's J (H) again
+      const float *rcf = reinterpret_cast<const float *>(&S.state[mi]);
       gmfb_t4<float>(rcf, wkf, lane);
-      float m = warp_max_abs(wkf[54 + lane]);
-      if (lane < 13) m = fmaxf(m, fabsf(wkf[54 + 32 + lane]));
-      m = warp_max_abs(m);
-      __syncwarp();
-      if (bj > GMF_F32_AMP * m) {  // (uniform in the warp)
+      const float mj = gmfb_store_j<float, T, true>(wkf, rcf[34], oj, lane);
+      if (rcf[GMF_RECF_BJ] > GMF_F32_AMP * mj) {
         gmfb_t4<double>(rcd, wkd, lane);
         gmfb_store_j<double, T>(wkd, rcd[34], oj, lane);
-      } else {
-        gmfb_store_j<float, T>(wkf, rcf[34], oj, lane);
       }
       if (ORDER >= 2) {
         gmfb_u<float>(rcf, wkf, S, lane);
-        float mh = 0.f;
-        for (int t = lane; t < 405; t += 32) mh = fmaxf(mh, fabsf(wkf[165 + t]));
-        mh = warp_max_abs(mh);
-        __syncwarp();
-        if (bh > GMF_F32_AMP * mh) {  // (uniform; the FP64 work area covers the record copy, no longer read)
+        const float mh = gmfb_store_h<float, T, true>(wkf, rcf[35], S, oh, lane);
+        if (rcf[GMF_RECF_BH] > GMF_F32_AMP * mh) {
           gmfb_u<double>(rcd, wkd, S, lane);
           gmfb_store_h<double, T>(wkd, rcd[35], S, oh, lane);
-        } else {
-          gmfb_store_h<float, T>(wkf, rcf[35], S, oh, lane);
         }
       }
     }
