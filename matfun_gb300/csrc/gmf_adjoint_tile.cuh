@@ -206,8 +206,7 @@ MF_D void gmf_adjoint_tile(int64_t base, int cnt, const T *__restrict__ A, const
     GmfState St;
     gmf_classify<KIND, ORDER>(a, C, St);
     S.state[tid] = St;
-    const unsigned cls = St.K == 0 ? 0u : ((St.flags & 1024) ? 1u : 2u);
-    key = (cls << 16) | ((unsigned)(255 - St.K) << 6) | (unsigned)((St.flags >> 3) & 63);
+    key = gmf_finish_key(St);
   }
   S.key[tid] = key;
   __syncthreads();

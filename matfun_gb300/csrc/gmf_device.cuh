@@ -1,15 +1,19 @@
-// gmf_device.cuh -- per-matrix device math of the general family (FP64, one thread per matrix).
-// Algorithm of c/include/matfun/gmf_kernel.hpp:251-692 (theory: confluent Newton-Hermite form over the eigenvalues):
-//   * eigenvalues of the deviator in closed form, refined against A itself where the closed form loses accuracy
-//     (Newton on det(A - mu I), a pair from det A and the principal minors, the branch-cut pair from the 2x2 block
-//     on the complement of the left eigenvector)
-//   * node order, groups (triple / closest pair / none), the 19 confluent divided differences by the streamed group
-//     series and the residues of single nodes
+// gmf_device.cuh -- per-matrix device math of the general family (FP64, one thread per matrix): F, J, H of f(A) for
+// a general real 3x3 A through the confluent Newton-Hermite form over its eigenvalues (the method of the reference's
+// c/include/matfun/gmf_kernel.hpp:251-692 and theory.md, "General matrices"):
+//   * the eigenvalues mu_i = m + x_i of A / sig (sig a power of two, m the shift), the x_i of the deviator in closed
+//     form, refined against A where the closed form loses accuracy (a pair from det A and the principal minors after
+//     Newton on the separated root; the pair near the branch cut from the 2x2 block on the complement of the left
+//     eigenvector; Newton on single real nodes far from m)
+//   * the nodes ordered and grouped (all three, the closest pair, or none); the 19 confluent divided differences
+//     f[x0^a x1^b x2^c]: a group's by its Taylor series streamed over the series index, a single node's beside a
+//     pair by its residue, and three single nodes by the Hermite recursion
 //   * the real basis r_0 = I, r_1, r_2 and T = I + iN, giving F and the real-reduced divided differences
 //     D2' = Re(T^T D T) (symmetric, 6 distinct) and D3' (T on all three indices; symmetric, 10 distinct).
-// Same branch thresholds and the same evaluation order of the series as the reference.  The kernels then contract
-// D2' and D3' with r into J and H through symmetric tensors (gmf_kernels.cu).
-// Written with sel() and non-short-circuit &, | (see mf_common.cuh) instead of long ?: / && chains.
+// The decisions and their thresholds are the method's (they define the result to which the parity tests hold this
+// code); the evaluation is this file's own: one thread per matrix takes only its branch, the CTA-local and batch-wide
+// orderings of the kernels give a warp's lanes the same branches.  The kernels then contract D2' and D3' with r into
+// J and H through symmetric tensors (gmf_kernels.cuh).
 #pragma once
 #include "ffloat.cuh"
 
@@ -83,120 +87,6 @@ MF_D constexpr int gpar(int t) {
 MF_D constexpr int gpos2(int j, int k) { return gpos(2, (j >= 1) + (k >= 1), (j >= 2) + (k >= 2)); }
 MF_D constexpr int gpos3(int j, int k, int l) {
   return gpos(3, (j >= 1) + (k >= 1) + (l >= 1), (j >= 2) + (k >= 2) + (l >= 2));
-}
-
-MF_D double det3(const double *M) {
-  return M[0] * (M[4] * M[8] - M[5] * M[7]) - M[1] * (M[3] * M[8] - M[5] * M[6]) + M[2] * (M[3] * M[7] - M[4] * M[6]);
-}
-
-// det by elimination with partial pivoting (gmf_kernel.hpp:138-159)
-MF_D double det_lu(const double *M) {
-  double a0 = fabs(M[0]), a1 = fabs(M[3]), a2 = fabs(M[6]);
-  bool p1 = (a1 > a0) & (a1 >= a2), p2 = (a2 > a0) & (a2 > a1);
-  double P[3], R1[3], R2[3];
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    P[c] = sel(p1, M[3 + c], sel(p2, M[6 + c], M[c]));
-    R1[c] = sel(p1 | p2, M[c], M[3 + c]);
-    R2[c] = sel(p2, M[3 + c], M[6 + c]);
-  }
-  double sgn = sel(p1, -1.0, 1.0);
-  double piv = sel(P[0] != 0, P[0], 1.0);
-  double l1 = R1[0] / piv, l2 = R2[0] / piv;
-  double b = R1[1] - l1 * P[1], c = R1[2] - l1 * P[2], d = R2[1] - l2 * P[1], e = R2[2] - l2 * P[2];
-  bool sw = fabs(d) > fabs(b);
-  double bb = sel(sw, d, b), cc = sel(sw, e, c), dd = sel(sw, b, d), ee = sel(sw, c, e);
-  sgn = sel(sw, -sgn, sgn);
-  double det = sgn * P[0] * bb * (ee - dd / sel(bb != 0, bb, 1.0) * cc);
-  return sel((P[0] != 0) & (bb != 0), det, 0.0);
-}
-
-MF_D double minors2(const double *M) {
-  return M[0] * M[4] - M[1] * M[3] + M[0] * M[8] - M[2] * M[6] + M[4] * M[8] - M[5] * M[7];
-}
-
-// eigenvalues of the deviator S (gmf_kernel.hpp:166-208)
-MF_D void roots3(const double *S, cx *x) {
-  constexpr double TWO_PI_3 = 2.0943951023931957;
-  double tau = (S[0] + S[4] + S[8]) / 3.0;
-  double Sp[9];
-#pragma unroll
-  for (int k = 0; k < 9; k++) Sp[k] = k % 4 == 0 ? S[k] - tau : S[k];
-  double s = fabs(Sp[0]);
-#pragma unroll
-  for (int k = 1; k < 9; k++) s = tmax(s, fabs(Sp[k]));
-  double t = pow2safe(s), it = 1.0 / t;
-#pragma unroll
-  for (int k = 0; k < 9; k++) Sp[k] = Sp[k] * it;
-  double P = 0.5 * (Sp[0] * Sp[0] + Sp[4] * Sp[4] + Sp[8] * Sp[8]) + Sp[1] * Sp[3] + Sp[2] * Sp[6] + Sp[5] * Sp[7];
-  double Q = det3(Sp);
-  double u = pow2safe(tmax(sqrt(fabs(P)), cbrt(fabs(Q)))), iu = 1.0 / u;
-  P = P * iu * iu;
-  Q = Q * iu * iu * iu;
-  t = t * u;
-  bool trig = (P > 0) & (4.0 * P * P * P >= 27.0 * Q * Q);
-  double s1;
-  if (trig) {
-    double p3 = P / 3.0;
-    double r = 0.5 * Q / (p3 * sqrt(p3));
-    r = sel(r > 1.0, 1.0, sel(r < -1.0, -1.0, r));
-    double ph = acos(r) / 3.0;
-    s1 = 2.0 * sqrt(p3) * cos(sel(r >= 0, ph, ph + TWO_PI_3));
-  } else {
-    double D = 0.25 * Q * Q - P * P * P / 27.0;
-    double uc = cbrt(0.5 * Q + copysgn(sqrt(sel(D > 0, D, 0.0)), Q));
-    s1 = uc + sel(uc != 0, P / (3.0 * sel(uc != 0, uc, 1.0)), 0.0);
-  }
-  double d = P - 0.75 * s1 * s1;
-  bool real = d >= 0;
-  double sq = sqrt(fabs(d));
-  double sa = -0.5 * s1 - copysgn(sq, s1);
-  double prod = sel(s1 != 0, Q / sel(s1 != 0, s1, 1.0), -P);
-  double sb = sel(sa != 0, prod / sel(sa != 0, sa, 1.0), 0.0);
-  double im = sel(real, 0.0, sq) * t;
-  x[0] = cmk(s1 * t + tau, 0.0 * t);
-  x[1] = cmk(sel(real, sa, -0.5 * s1) * t + tau, im);
-  x[2] = cmk(sel(real, sb, -0.5 * s1) * t + tau, -im);
-}
-
-// 3 Newton steps on det(A - mu_j I), derivative from the other nodes (gmf_kernel.hpp:210-226)
-template <int J>
-MF_D void newton(const double *As, cx *mu) {
-#pragma unroll
-  for (int it = 0; it < 3; it++) {
-    cx den = cmk(1.0, 0.0);
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-      if (k != J) den = cmul(den, csub(mu[k], mu[J]));
-    bool ok = (den.re != 0) | (den.im != 0);
-    double B[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) B[k] = k % 4 == 0 ? As[k] - mu[J].re : As[k];
-    double step = det_lu(B) * cinv_s(den).re;
-    mu[J].re = sel(ok, mu[J].re + step, mu[J].re);
-  }
-}
-
-// f of a node (k: output order; pow times sig^(al - k)) (gmf_kernel.hpp:228-248)
-template <int KIND>
-MF_D cx coef0(const GmfCoef &C, double sig, double m, cx x, cx mu, int k) {
-  if (KIND == EXP) {
-    double e = exp(x.re);
-    return cmk(e * cos(x.im), e * sin(x.im));
-  }
-  double th = atan2(mu.im, mu.re);
-  if (KIND == LOG) {
-    bool near = (m > 0) & (cabs_s(x) <= 0.5 * m);
-    double ms = sel(m > 0, m, 1.0), zr = x.re / ms, zi = x.im / ms;
-    double l1r = 0.5 * log1p(zr * (2.0 + zr) + zi * zi), l1i = atan2(zi, 1.0 + zr);
-    double lr = near ? log(sig * ms) + l1r : log(sig * cabs_s(mu));
-    return cmk(lr, sel(near, l1i, th));
-  }
-  double mag = pow_split(sig * cabs_s(mu), C.bh[k], C.bl[k]);
-  double ph = (C.al - k) * th;
-  cx out = cmk(mag * cos(ph), mag * sin(ph));
-  for (int i = 0; i < k; i++) out = cmul(out, mu);
-  return out;
 }
 
 // number of series terms (gmf_kernel.hpp:73-97): the group series needs terms until |b_(n+k)| C(k+n, n) r^k drops
@@ -483,275 +373,447 @@ struct GmfRec {
   double sc1, sc2;       // output factors of J and H (NaN for a matrix outside the domain)
 };
 
-// scaling by a power of two (exp: none), shift m, deviator S (gmf_kernel.hpp:262-275)
+MF_D void cross3(const double *a, const double *b, double *c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+MF_D double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+MF_D void matvec3(const double *M, const double *v, double *o) {
+#pragma unroll
+  for (int r = 0; r < 3; r++) o[r] = M[3 * r] * v[0] + M[3 * r + 1] * v[1] + M[3 * r + 2] * v[2];
+}
+
+// ------------------------------------------------------------------------------------------------ spectral analysis
+// One thread per matrix, and only the branch a matrix takes is evaluated (the CTA-local and batch-wide orderings of
+// the kernels give the lanes of a warp the same branches).  The decisions -- which roots are refined against A, the
+// branch-cut pair, the node order, the groups -- and their thresholds are those of the method (theory: confluent
+// Newton-Hermite form over the eigenvalues): they define the result, to which the parity tests hold this code.
+
+// det M by the cofactors of its first row
+MF_D double det_cof(const double *M) {
+  return M[0] * (M[4] * M[8] - M[5] * M[7]) + M[1] * (M[5] * M[6] - M[3] * M[8]) + M[2] * (M[3] * M[7] - M[4] * M[6]);
+}
+
+// det M by Gaussian elimination with partial pivoting (backward stable; exact pivots for a diagonal M), in the
+// textbook order: the pivot row P (the largest |M_i0|, the first of equal ones) above the other two rows R, Q, the
+// multipliers R_0 / P_0 and Q_0 / P_0, the 2 x 2 remainder [[b, c], [d, e]] eliminated the same way on its larger
+// first-column entry.  Newton on det(As - mu I) converges, for an ill-conditioned eigenvalue, to a point of the
+// rounding-noise band that this order of operations decides; the parity tests hold ill-conditioned matrices to the
+// oracle at 1e-12, so the plain expressions (no explicit fused forms) matter here.
+MF_D double det_elim(const double *M) {
+  const double a0 = fabs(M[0]), a1 = fabs(M[3]), a2 = fabs(M[6]);
+  const bool on1 = (a1 > a0) & (a1 >= a2), on2 = (a2 > a0) & (a2 > a1);
+  double P[3], R[3], Q[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    P[k] = on1 ? M[3 + k] : (on2 ? M[6 + k] : M[k]);
+    R[k] = (on1 | on2) ? M[k] : M[3 + k];
+    Q[k] = on2 ? M[3 + k] : M[6 + k];
+  }
+  if (P[0] == 0.0) return 0.0;  // the first column vanishes
+  const double lr = R[0] / P[0], lq = Q[0] / P[0];
+  const double b = R[1] - lr * P[1], c = R[2] - lr * P[2], d = Q[1] - lq * P[1], e = Q[2] - lq * P[2];
+  const bool sw = fabs(d) > fabs(b);  // the 2 x 2 pivot
+  const double p2 = sw ? d : b, o2 = sw ? c : e, s2 = sw ? b : d, t2 = sw ? e : c;
+  if (p2 == 0.0) return 0.0;
+  const double sgn = (on1 != sw) ? -1.0 : 1.0;  // parity of the row order
+  return sgn * P[0] * p2 * (o2 - s2 / p2 * t2);
+}
+
+// the sum of the principal 2 x 2 minors of M (the second invariant), its six products summed in order
+MF_D double minors_sum(const double *M) {
+  return M[0] * M[4] - M[1] * M[3] + M[0] * M[8] - M[2] * M[6] + M[4] * M[8] - M[5] * M[7];
+}
+
+// three Newton steps on p(mu) = det(As - mu I) for the real eigenvalue mu, the other two (a1 + i b1, a2 + i b2: both
+// real or a conjugate pair) held fixed: -p'(mu) = (a1 - mu + i b1)(a2 - mu + i b2) = (a1 - mu)(a2 - mu) - b1 b2, real;
+// the step p(mu) (1 / -p'(mu)); no step where p' vanishes
+MF_D double newton_real(const double *As, double mu, cx o1, cx o2) {
+#pragma unroll 1
+  for (int it = 0; it < 3; it++) {
+    const double d1 = o1.re - mu, d2 = o2.re - mu;
+    const double dp = d1 * d2 - o1.im * o2.im;
+    if (dp != 0.0) {
+      const double B[9] = {As[0] - mu, As[1], As[2], As[3], As[4] - mu, As[5], As[6], As[7], As[8] - mu};
+      mu = mu + det_elim(B) * (1.0 / dp);
+    }
+  }
+  return mu;
+}
+
+// The eigenvalues of the deviator S (traceless up to rounding) in closed form: x[0] the real root farthest from the
+// other two, x[1], x[2] the other two (a real pair, larger magnitude first, or a conjugate pair).  The rounding
+// residue tau = tr S / 3 is removed; the traceless d = S - tau I is scaled by a power of two s0 ~ max |d| and its
+// characteristic polynomial x^3 - p x - q (p = tr(d^2) / 2, q = det d) by s1 ~ max(sqrt |p|, cbrt |q|), so that p
+// and q are O(1).  Three real roots (p > 0, 4 p^3 >= 27 q^2): the trigonometric form, x = 2 sqrt(p / 3) cos(phi),
+// phi = acos(q (3 / p)^(3/2) / 2) / 3 (+ 2 pi / 3 for q < 0, the root farthest from the others); otherwise
+// Cardano's real root w + p / (3 w), w^3 = q / 2 + sign(q) sqrt(q^2 / 4 - p^3 / 27).  The other two solve
+// x^2 + r x + (r^2 - p) = 0: for a discriminant p - 3 r^2 / 4 >= 0 the larger one without cancellation and the other
+// from the product q / r, else the conjugate pair.
+MF_D void deviator_roots(const double *S, cx *x) {
+  constexpr double TWO_PI_3 = 2.0943951023931957;
+  const double tau = (S[0] + S[4] + S[8]) / 3.0;
+  double d[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) d[k] = k % 4 == 0 ? S[k] - tau : S[k];
+  double big = fabs(d[0]);
+#pragma unroll
+  for (int k = 1; k < 9; k++) big = tmax(big, fabs(d[k]));
+  const double s0 = pow2safe(big), i0 = 1.0 / s0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) d[k] *= i0;
+  double p = 0.5 * (d[0] * d[0] + d[4] * d[4] + d[8] * d[8]) + d[1] * d[3] + d[2] * d[6] + d[5] * d[7];
+  double q = det_cof(d);
+  const double s1 = pow2safe(tmax(sqrt(fabs(p)), cbrt(fabs(q)))), i1 = 1.0 / s1;
+  p *= i1 * i1;
+  q *= i1 * i1 * i1;
+  const double sc = s0 * s1;  // the roots of the cubic times sc are those of d
+  double r;
+  if ((p > 0) & (4.0 * p * p * p >= 27.0 * q * q)) {
+    const double p3 = p / 3.0, rt = sqrt(p3);
+    double c = 0.5 * q / (p3 * rt);
+    c = c > 1.0 ? 1.0 : (c < -1.0 ? -1.0 : c);
+    const double phi = acos(c) / 3.0;
+    r = 2.0 * rt * cos(c >= 0 ? phi : phi + TWO_PI_3);
+  } else {
+    const double disc = 0.25 * q * q - p * p * p / 27.0;
+    const double w = cbrt(0.5 * q + copysgn(sqrt(disc > 0 ? disc : 0.0), q));
+    r = w != 0 ? w + p / (3.0 * w) : 0.0;
+  }
+  const double dp = p - 0.75 * r * r, h = sqrt(fabs(dp));
+  x[0] = cmk(r * sc + tau, 0.0);
+  if (dp >= 0) {
+    const double a = -0.5 * r - copysgn(h, r);
+    const double prod = r != 0 ? q / r : -p;
+    const double b = a != 0 ? prod / a : 0.0;
+    x[1] = cmk(a * sc + tau, 0.0);
+    x[2] = cmk(b * sc + tau, 0.0);
+  } else {
+    const double c = -0.5 * r * sc + tau;
+    x[1] = cmk(c, h * sc);
+    x[2] = cmk(c, -h * sc);
+  }
+}
+
+// scaling by a power of two sig ~ max |a_ij| (exp: none), shift m = tr As / 3, deviator S = As - m I
 template <int KIND>
 MF_D void gmf_scale(const double *a, double &sig, double *As, double &m, double *S) {
   double amax = fabs(a[0]);
 #pragma unroll
   for (int k = 1; k < 9; k++) amax = tmax(amax, fabs(a[k]));
   sig = KIND == EXP ? 1.0 : pow2safe(amax);
-  const double isig = 1.0 / sig;
+  const double is = 1.0 / sig;
 #pragma unroll
-  for (int k = 0; k < 9; k++) As[k] = a[k] * isig;
+  for (int k = 0; k < 9; k++) As[k] = a[k] * is;
   m = (As[0] + As[4] + As[8]) / 3.0;
 #pragma unroll
   for (int k = 0; k < 9; k++) S[k] = k % 4 == 0 ? As[k] - m : As[k];
 }
 
-// the pair-refinement test (gmf_kernel.hpp:277-284)
-MF_D bool gmf_pair_check(const double *S, double m, const cx *mu, double &mid, double &Rp) {
+// The closed-form pair x[1], x[2] is replaced by one computed from A itself, after Newton on the separated root, when
+// the closed form is not the accurate one: the pair small against mu0 (|mid| + R <= mu0 / 4), or the deviator not
+// dominated by the shift with mu0 apart from the pair (|m| <= max |S|, R <= |mid - mu0| / 4); mid, R: the pair's
+// centre and half-distance.  A real pair's half-distance is half its difference, a conjugate pair's its |imaginary|.
+MF_D bool pair_from_A(const double *S, double m, double mu0, cx x1, cx x2, double &mid, double &R) {
   double smax = fabs(S[0]);
 #pragma unroll
   for (int k = 1; k < 9; k++) smax = tmax(smax, fabs(S[k]));
-  mid = 0.5 * (mu[1].re + mu[2].re);
-  Rp = 0.5 * cabs_s(csub(mu[1], mu[2]));
-  bool small = fabs(mid) + Rp <= 0.25 * fabs(mu[0].re);
-  bool aniso = (fabs(m) <= smax) & (Rp <= 0.25 * fabs(mid - mu[0].re));
-  return (mu[0].re != 0) & (small | aniso);
+  mid = 0.5 * ((m + x1.re) + (m + x2.re));
+  R = x1.im != 0 ? fabs(x1.im) : 0.5 * fabs((m + x1.re) - (m + x2.re));
+  const bool small = fabs(mid) + R <= 0.25 * fabs(mu0);
+  const bool apart = (fabs(m) <= smax) & (R <= 0.25 * fabs(mid - mu0));
+  return (mu0 != 0) & (small | apart);
 }
 
-// first part of the spectral analysis: the closed-form roots x of the deviator, and a key of the branches the rest
-// takes (complex pair, pair refinement, branch-cut pair), so that a CTA can order its matrices by it before the rest
+// the branches the spectral analysis of a matrix takes, from its closed-form roots: a key for ordering a batch or a
+// CTA so that neighbouring matrices take the same ones (complex pair, pair from A, branch-cut pair, and a 16-level
+// geometry bucket: the argument of the pair, or the spread of three real roots relative to their mean)
 template <int KIND>
 MF_D unsigned gmf_roots(const double *a, cx *x) {
   double sig, As[9], m, S[9];
   gmf_scale<KIND>(a, sig, As, m, S);
-  roots3(S, x);
-  cx mu[3];
-#pragma unroll
-  for (int i = 0; i < 3; i++) mu[i] = cmk(m + x[i].re, x[i].im);
-  double mid, Rp;
-  const bool pc = gmf_pair_check(S, m, mu, mid, Rp);
-  const bool cut = (KIND != EXP) & (mu[1].re + mu[2].re < 0);
-  const bool cplx = (x[0].im != 0) | (x[1].im != 0) | (x[2].im != 0);
-  // geometry bucket (16 levels): the argument of the complex pair, or the spread of three real roots relative to their
-  // mean; neighbours in it take the same groups, Newton steps and series lengths in the rest
-  const int ip = x[1].im != 0 ? 1 : (x[2].im != 0 ? 2 : 0);
-  const cx mp = mu[ip];
-  const float argp = fabsf(atan2f((float)mp.im, (float)mp.re)) * (16.0f / 3.1415927f);
+  deviator_roots(S, x);
+  double mid, R;
+  const bool pc = pair_from_A(S, m, m + x[0].re, x[1], x[2], mid, R);
+  const bool cut = (KIND != EXP) & ((m + x[1].re) + (m + x[2].re) < 0);
+  const bool cplx = x[1].im != 0;
+  const float argp = fabsf(atan2f((float)x[1].im, (float)(m + x[1].re))) * (16.0f / 3.1415927f);
   const float spread = (float)((tmax(tmax(x[0].re, x[1].re), x[2].re) - tmin(tmin(x[0].re, x[1].re), x[2].re)) /
                                tmax(fabs(m), 1e-300)) * 8.0f;
   const unsigned geo = (unsigned)fminf(cplx ? argp : spread, 15.0f);
   return (cplx ? 128u : 0u) | (pc ? 64u : 0u) | (cut ? 32u : 0u) | geo;
 }
 
-// the rest of the spectral analysis, from the roots x of gmf_roots
+// a node of the divided differences during the analysis
+struct GNode {
+  cx x;          // relative to the shift m
+  cx mu;         // the eigenvalue of As
+  bool refined;  // mu was computed from As itself: differences to this node are taken between the mu
+  bool pairpos;  // one of the closed form's deflated pair (positions 1, 2 before ordering)
+};
+
+MF_D void gswap(GNode &a, GNode &b) {
+  const GNode t = a;
+  a = b;
+  b = t;
+}
+
+// the rest of the spectral analysis, from the closed-form roots xr of gmf_roots: refinement against A, node order,
+// groups, offsets, series length
 template <int KIND, int ORDER>
 MF_D void gmf_classify_from(const double *a, const cx *xr, const GmfCoef &C, GmfState &St) {
   double sig, As[9], m, S[9];
   gmf_scale<KIND>(a, sig, As, m, S);
-  cx x[3], mu[3];
+  GNode nd[3];
 #pragma unroll
-  for (int i = 0; i < 3; i++) { x[i] = xr[i]; mu[i] = cmk(m + x[i].re, x[i].im); }
+  for (int i = 0; i < 3; i++) nd[i] = {xr[i], cmk(m + xr[i].re, xr[i].im), false, i > 0};
 
-  // ---- pair refinement (gmf_kernel.hpp:277-304)
+  // ---- the pair from det A and the principal minors, after Newton on the separated root
   double mid, Rp;
-  bool pc = gmf_pair_check(S, m, mu, mid, Rp);
-  double pcen = 0.0, ps = 0.0;
+  bool fromA = pair_from_A(S, m, nd[0].mu.re, nd[1].x, nd[2].x, mid, Rp);
+  double pcen = 0.0, ps = 0.0;  // centre and half-width of the pair computed from A
   bool preal = true;
-  if (pc) {
-    newton<0>(As, mu);
-    double m0 = mu[0].re;
-    bool big = fabs(m0) >= fabs(mid) + Rp;
-    double pid = det_lu(As) / m0, c2 = minors2(As);
-    double sgt = As[0] + As[4] + As[8] - m0;
-    double sg = sel(big, (c2 - pid) / m0, sgt), pi = sel(big, pid, c2 - m0 * sgt);
-    double disc = 0.25 * sg * sg - pi;
+  bool mu0_newton = false;
+  if (fromA) {
+    const double m0 = newton_real(As, nd[0].mu.re, nd[1].mu, nd[2].mu);
+    nd[0].mu.re = m0;
+    mu0_newton = true;
+    // product pi and sum sg of the pair: pi = det As / mu0, sg = (c2 - pi) / mu0 for mu0 the largest; otherwise
+    // sg = tr As - mu0, pi = c2 - mu0 sg
+    const double c2 = minors_sum(As);
+    double sg, pi;
+    if (fabs(m0) >= fabs(mid) + Rp) {
+      pi = det_elim(As) / m0;
+      sg = (c2 - pi) / m0;
+    } else {
+      sg = As[0] + As[4] + As[8] - m0;
+      pi = c2 - m0 * sg;
+    }
+    const double disc = 0.25 * sg * sg - pi;
     pcen = 0.5 * sg;
     ps = sqrt(fabs(disc));
     preal = disc >= 0;
-    double r1 = pcen + copysgn(ps, pcen);
-    double r2 = sel(r1 != 0, pi / sel(r1 != 0, r1, 1.0), pcen - copysgn(ps, pcen));
-    mu[1] = csel(preal, cmk(r1, 0.0), cmk(pcen, ps));
-    mu[2] = csel(preal, cmk(r2, 0.0), cmk(pcen, -ps));
-  }
-  // ---- branch-cut pair (log, pow) (gmf_kernel.hpp:305-367)
-  bool cut = (KIND != EXP) & (mu[1].re + mu[2].re < 0);
-  if (cut) {
-    if (!pc) newton<0>(As, mu);
-    double l0 = mu[0].re;
-    double Mc[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) Mc[k] = k % 4 == 0 ? As[k] - l0 : As[k];
-    double c01[3] = {Mc[3] * Mc[7] - Mc[6] * Mc[4], Mc[6] * Mc[1] - Mc[0] * Mc[7], Mc[0] * Mc[4] - Mc[3] * Mc[1]};
-    double c02[3] = {Mc[3] * Mc[8] - Mc[6] * Mc[5], Mc[6] * Mc[2] - Mc[0] * Mc[8], Mc[0] * Mc[5] - Mc[3] * Mc[2]};
-    double c12[3] = {Mc[4] * Mc[8] - Mc[7] * Mc[5], Mc[7] * Mc[2] - Mc[1] * Mc[8], Mc[1] * Mc[5] - Mc[4] * Mc[2]};
-    double n01 = c01[0] * c01[0] + c01[1] * c01[1] + c01[2] * c01[2];
-    double n02 = c02[0] * c02[0] + c02[1] * c02[1] + c02[2] * c02[2];
-    double n12 = c12[0] * c12[0] + c12[1] * c12[1] + c12[2] * c12[2];
-    bool s1 = n02 > n01;
-    double u[3], nn = sel(s1, n02, n01);
-#pragma unroll
-    for (int k = 0; k < 3; k++) u[k] = sel(s1, c02[k], c01[k]);
-    bool s2 = n12 > nn;
-#pragma unroll
-    for (int k = 0; k < 3; k++) u[k] = sel(s2, c12[k], u[k]);
-    nn = sel(s2, n12, nn);
-    bool okd = nn > 0;
-    double iu = 1.0 / sqrt(sel(okd, nn, 1.0));
-#pragma unroll
-    for (int k = 0; k < 3; k++) u[k] = u[k] * iu;
-    double au0 = fabs(u[0]), au1 = fabs(u[1]), au2 = fabs(u[2]);
-    bool k1 = au1 < au0, k2 = au2 < sel(k1, au1, au0);
-    double ex = sel(k1 | k2, 0.0, 1.0), ey = sel(k1 & !k2, 1.0, 0.0), ez = sel(k2, 1.0, 0.0);
-    double eu = ex * u[0] + ey * u[1] + ez * u[2];
-    double q1[3] = {ex - eu * u[0], ey - eu * u[1], ez - eu * u[2]};
-    double iq = 1.0 / sqrt(q1[0] * q1[0] + q1[1] * q1[1] + q1[2] * q1[2]);
-#pragma unroll
-    for (int k = 0; k < 3; k++) q1[k] = q1[k] * iq;
-    double q2[3] = {u[1] * q1[2] - u[2] * q1[1], u[2] * q1[0] - u[0] * q1[2], u[0] * q1[1] - u[1] * q1[0]};
-    double Sq1[3], Sq2[3];
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-      Sq1[r] = S[3 * r] * q1[0] + S[3 * r + 1] * q1[1] + S[3 * r + 2] * q1[2];
-      Sq2[r] = S[3 * r] * q2[0] + S[3 * r + 1] * q2[1] + S[3 * r + 2] * q2[2];
-    }
-    double b11 = q1[0] * Sq1[0] + q1[1] * Sq1[1] + q1[2] * Sq1[2];
-    double b12 = q1[0] * Sq2[0] + q1[1] * Sq2[1] + q1[2] * Sq2[2];
-    double b21 = q2[0] * Sq1[0] + q2[1] * Sq1[1] + q2[2] * Sq1[2];
-    double b22 = q2[0] * Sq2[0] + q2[1] * Sq2[1] + q2[2] * Sq2[2];
-    double dd = 0.5 * (b11 - b22), beta2 = -(dd * dd + b12 * b21), cc = m + 0.5 * (b11 + b22);
-    double bb = sqrt(fabs(beta2));
-    bool creal = beta2 <= 0;
-    mu[1] = csel(okd, csel(creal, cmk(cc + bb, 0.0), cmk(cc, bb)), mu[1]);
-    mu[2] = csel(okd, csel(creal, cmk(cc - bb, 0.0), cmk(cc, -bb)), mu[2]);
-    pcen = sel(okd, cc, pcen);
-    ps = sel(okd, bb, ps);
-    preal = (okd & creal) | (!okd & preal);
-    pc = pc | okd;
-  }
-  bool ab[3] = {pc, pc, pc};
-  double og[3] = {0.0, 1.0, 2.0};
-#pragma unroll
-  for (int i = 0; i < 3; i++) x[i] = csel(pc, cmk(mu[i].re - m, mu[i].im), x[i]);
-
-  // ---- node order (gmf_kernel.hpp:373-410)
-  {
-    auto key = [&](cx v) { return KIND == EXP ? v.re : -cabs_s(v); };
-    bool cplxp = x[1].im != 0;
-    if (cplxp) {
-      bool first = (key(mu[0]) <= key(mu[1])) | cut;
-      if (!first) {  // rotate to (pair, real node)
-        cx tx = x[0], tm = mu[0];
-        bool ta = ab[0];
-        double to = og[0];
-        x[0] = x[1]; mu[0] = mu[1]; ab[0] = ab[1]; og[0] = og[1];
-        x[1] = x[2]; mu[1] = mu[2]; ab[1] = ab[2]; og[1] = og[2];
-        x[2] = tx; mu[2] = tm; ab[2] = ta; og[2] = to;
-      }
+    if (preal) {
+      const double r1 = pcen + copysgn(ps, pcen);
+      nd[1].mu = cmk(r1, 0.0);
+      nd[2].mu = cmk(r1 != 0 ? pi / r1 : pcen - copysgn(ps, pcen), 0.0);
     } else {
+      nd[1].mu = cmk(pcen, ps);
+      nd[2].mu = cmk(pcen, -ps);
+    }
+  }
+  // ---- log, powers: a pair whose real parts sum below zero lies near the branch cut; f jumps between its nodes, so
+  // the result needs the pair's imaginary part beta itself: from the 2 x 2 block B = Q^T S Q of the deviator on the
+  // complement of mu0's left eigenvector u (u^T (As - mu0 I) = 0, the longest cross product of two columns),
+  // beta^2 = -(((b11 - b22) / 2)^2 + b12 b21), centre m + tr B / 2
+  const bool cut = (KIND != EXP) & (nd[1].mu.re + nd[2].mu.re < 0);
+  if (cut) {
+    if (!mu0_newton) nd[0].mu.re = newton_real(As, nd[0].mu.re, nd[1].mu, nd[2].mu);
+    const double l0 = nd[0].mu.re;
+    const double c0[3] = {As[0] - l0, As[3], As[6]}, c1[3] = {As[1], As[4] - l0, As[7]}, c2[3] = {As[2], As[5], As[8] - l0};
+    double u[3], nu;
+    {
+      double w01[3], w02[3], w12[3];
+      cross3(c0, c1, w01);
+      cross3(c0, c2, w02);
+      cross3(c1, c2, w12);
+      const double n01 = dot3(w01, w01), n02 = dot3(w02, w02), n12 = dot3(w12, w12);
+      const bool t02 = n02 > n01;
+      nu = t02 ? n02 : n01;
+      const bool t12 = n12 > nu;
+      nu = t12 ? n12 : nu;
 #pragma unroll
-      for (int s = 0; s < 3; s++) {
-        const int i = s == 1 ? 1 : 0, j = i + 1;
-        bool sw = key(mu[i]) > key(mu[j]);
-        cx tx = x[i], tm = mu[i];
-        bool ta = ab[i];
-        double to = og[i];
-        x[i] = csel(sw, x[j], x[i]); x[j] = csel(sw, tx, x[j]);
-        mu[i] = csel(sw, mu[j], mu[i]); mu[j] = csel(sw, tm, mu[j]);
-        ab[i] = (sw & ab[j]) | (!sw & ab[i]); ab[j] = (sw & ta) | (!sw & ab[j]);
-        og[i] = sel(sw, og[j], og[i]); og[j] = sel(sw, to, og[j]);
-      }
+      for (int k = 0; k < 3; k++) u[k] = t12 ? w12[k] : (t02 ? w02[k] : w01[k]);
+    }
+    if (nu > 0) {
+      const double iu = 1.0 / sqrt(nu);
+#pragma unroll
+      for (int k = 0; k < 3; k++) u[k] *= iu;
+      // q1: the coordinate axis least aligned with u, less its u component, normalised; q2 = u x q1
+      const double b0 = fabs(u[0]), b1 = fabs(u[1]), b2 = fabs(u[2]);
+      const bool y1 = b1 < b0, z2 = b2 < (y1 ? b1 : b0);
+      const int ax = z2 ? 2 : (y1 ? 1 : 0);
+      const double ua = ax == 0 ? u[0] : (ax == 1 ? u[1] : u[2]);
+      double q1[3] = {(ax == 0 ? 1.0 : 0.0) - ua * u[0], (ax == 1 ? 1.0 : 0.0) - ua * u[1],
+                      (ax == 2 ? 1.0 : 0.0) - ua * u[2]};
+      const double iq = 1.0 / sqrt(dot3(q1, q1));
+#pragma unroll
+      for (int k = 0; k < 3; k++) q1[k] *= iq;
+      double q2[3], Sq1[3], Sq2[3];
+      cross3(u, q1, q2);
+      matvec3(S, q1, Sq1);
+      matvec3(S, q2, Sq2);
+      const double b11 = dot3(q1, Sq1), b12 = dot3(q1, Sq2), b21 = dot3(q2, Sq1), b22 = dot3(q2, Sq2);
+      const double hd = 0.5 * (b11 - b22), beta2 = -(hd * hd + b12 * b21), cc = m + 0.5 * (b11 + b22);
+      const double bt = sqrt(fabs(beta2));
+      preal = beta2 <= 0;
+      nd[1].mu = preal ? cmk(cc + bt, 0.0) : cmk(cc, bt);
+      nd[2].mu = preal ? cmk(cc - bt, 0.0) : cmk(cc, -bt);
+      pcen = cc;
+      ps = bt;
+      fromA = true;
+    }
+  }
+  if (fromA) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      nd[i].refined = true;
+      nd[i].x = cmk(nd[i].mu.re - m, nd[i].mu.im);
     }
   }
 
-  // ---- groups (gmf_kernel.hpp:412-437)
-  auto okf = [&](double c, double R) -> bool {
+  // ---- node order: the node with the largest high derivatives last (exp: the largest real part; log, powers: the
+  // smallest modulus); a conjugate pair stays adjacent, the real node first when it comes first by that order or the
+  // pair lies near the cut (whose large divided differences then only multiply w_2), else last
+  auto key = [&](cx v) { return KIND == EXP ? v.re : (v.im == 0 ? -fabs(v.re) : -cabs_s(v)); };
+  if (nd[1].x.im != 0) {
+    if (!((key(nd[0].mu) <= key(nd[1].mu)) | cut)) {  // (real, pair) -> (pair, real)
+      gswap(nd[0], nd[1]);
+      gswap(nd[1], nd[2]);
+    }
+  } else {  // three real nodes: a stable sort
+    if (key(nd[0].mu) > key(nd[1].mu)) gswap(nd[0], nd[1]);
+    if (key(nd[1].mu) > key(nd[2].mu)) gswap(nd[1], nd[2]);
+    if (key(nd[0].mu) > key(nd[1].mu)) gswap(nd[0], nd[1]);
+  }
+
+  // ---- groups: all three nodes when their radius about the mean is within reach of the series (exp: radius <= 4;
+  // log, powers: radius <= rho (m + centre), centre right of the singularity), else the closest eligible pair (both
+  // real or conjugate) within reach whose radius is <= 0.6 of its distance to the third node (the series' pole), else
+  // none
+  auto reach = [&](double c, double R) -> bool {
     if (KIND == EXP) return R <= G_R_EXP;
     return (m + c > 0) & (R <= C.rho_f * (m + c));
   };
-  double cs3 = (x[0].re + x[1].re + x[2].re) / 3.0;
-  double R3 = tmax(tmax(cabs_s(cmk(x[0].re - cs3, x[0].im)), cabs_s(cmk(x[1].re - cs3, x[1].im))),
-                   cabs_s(cmk(x[2].re - cs3, x[2].im)));
-  bool triple = okf(cs3, R3);
-  bool psel[3] = {false, false, false};
-  double bestR = __longlong_as_double(0x7FF0000000000000ll);
-#pragma unroll
-  for (int p = 0; p < 3; p++) {
-    const int i = p == 2 ? 1 : 0, j = p == 0 ? 1 : 2, k = 3 - i - j;
-    bool elig = ((x[i].im == 0) & (x[j].im == 0)) | ((x[i].re == x[j].re) & (x[i].im == -x[j].im));
-    double c = 0.5 * (x[i].re + x[j].re), R = 0.5 * cabs_s(csub(x[i], x[j]));
-    bool okp = elig & okf(c, R) & (R <= G_RHO_POLE * cabs_s(cmk(c - x[k].re, -x[k].im))) & !triple;
-    bool better = okp & (R < bestR);
-    bestR = sel(better, R, bestR);
-#pragma unroll
-    for (int q = 0; q < p; q++) psel[q] = psel[q] & !better;
-    psel[p] = better;
+  const bool cplx = nd[1].x.im != 0 || nd[0].x.im != 0;
+  const double cs = (nd[0].x.re + nd[1].x.re + nd[2].x.re) / 3.0;
+  double R3;
+  if (!cplx) {
+    R3 = tmax(tmax(fabs(nd[0].x.re - cs), fabs(nd[1].x.re - cs)), fabs(nd[2].x.re - cs));
+  } else {
+    const bool real_first = nd[0].x.im == 0;  // the real node first (the pair at 1, 2) or last (the pair at 0, 1)
+    const cx xc = real_first ? nd[1].x : nd[0].x;
+    const double rc = cabs_s(cmk(xc.re - cs, xc.im));  // (the same for both members of the pair)
+    R3 = real_first ? tmax(tmax(fabs(nd[0].x.re - cs), rc), rc) : tmax(tmax(rc, rc), fabs(nd[2].x.re - cs));
   }
-  bool inG[3] = {bool(triple | psel[0] | psel[1]), bool(triple | psel[0] | psel[2]), bool(triple | psel[1] | psel[2])};
-  bool pk[3] = {psel[2], psel[1], psel[0]};
+  const bool triple = reach(cs, R3);
+  bool inG[3] = {triple, triple, triple}, pk[3] = {false, false, false};
+  if (!triple) {
+    double bestR = __longlong_as_double(0x7FF0000000000000ll);
+    int best = -1;
+#pragma unroll
+    for (int pr = 0; pr < 3; pr++) {  // pairs (0, 1), (0, 2), (1, 2); the third node k is the pole
+      const int i = pr == 2 ? 1 : 0, j = pr == 0 ? 1 : 2, k = 3 - i - j;
+      const cx xi = nd[i].x, xj = nd[j].x, xk = nd[k].x;
+      const bool both_real = (xi.im == 0) & (xj.im == 0);
+      if (!(both_real | ((xi.re == xj.re) & (xi.im == -xj.im)))) continue;
+      const double c = 0.5 * (xi.re + xj.re);
+      const double R = both_real ? 0.5 * fabs(xi.re - xj.re) : fabs(xi.im);
+      const double pole = xk.im == 0 ? fabs(c - xk.re) : cabs_s(cmk(c - xk.re, -xk.im));
+      if (reach(c, R) & (R <= G_RHO_POLE * pole) & (R < bestR)) {
+        bestR = R;
+        best = pr;
+      }
+    }
+    // pair (0, 1): pole node 2; (0, 2): node 1; (1, 2): node 0
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      pk[q] = best == 2 - q;
+      inG[q] = (best >= 0) & (best != 2 - q);
+    }
+  }
 
-  // ---- group centre and offsets (gmf_kernel.hpp:439-460)
-  double gsum = sel(inG[0], 1.0, 0.0) + sel(inG[1], 1.0, 0.0) + sel(inG[2], 1.0, 0.0);
-  double cxg = (sel(inG[0], x[0].re, 0.0) + sel(inG[1], x[1].re, 0.0) + sel(inG[2], x[2].re, 0.0)) /
-               sel(gsum > 0, gsum, 1.0);
+  // ---- group centre and offsets; the pair computed from A, when it is the group, keeps its own symmetric offsets
+  const int gn = (int)inG[0] + (int)inG[1] + (int)inG[2];
+  double cxg = gn > 0 ? ((inG[0] ? nd[0].x.re : 0.0) + (inG[1] ? nd[1].x.re : 0.0) + (inG[2] ? nd[2].x.re : 0.0)) /
+                            (double)gn : 0.0;
   double cmu = m + cxg;
-  bool is12[3] = {og[0] > 0.5, og[1] > 0.5, og[2] > 0.5};
-  bool ovr = pc & (gsum == 2.0) &
-             ((inG[0] & inG[1] & is12[0] & is12[1]) | (inG[0] & inG[2] & is12[0] & is12[2]) |
-              (inG[1] & inG[2] & is12[1] & is12[2]));
-  cxg = sel(ovr, pcen - m, cxg);
-  cmu = sel(ovr, pcen, cmu);
-  cx dpair = cmk(sel(preal, ps, 0.0), sel(preal, 0.0, ps));
+  const bool own_pair = fromA & (gn == 2) & ((!inG[0] | nd[0].pairpos) & (!inG[1] | nd[1].pairpos) &
+                                             (!inG[2] | nd[2].pairpos));
+  if (own_pair) {
+    cxg = pcen - m;
+    cmu = pcen;
+  }
   cx off[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    bool neg = (mu[i].re - pcen < 0) | (mu[i].im < 0);
-    cx di = csel(neg, cmk(-dpair.re, -dpair.im), dpair);
-    bool ovi = ovr & inG[i];
-    mu[i] = csel(ovi, cmk(pcen + di.re, di.im), mu[i]);
-    x[i] = csel(ovi, cmk(mu[i].re - m, mu[i].im), x[i]);
-    off[i] = csel(inG[i], csel(ovi, di, cmk(x[i].re - cxg, x[i].im)), cmk(0.0, 0.0));
+    off[i] = cmk(0.0, 0.0);
+    if (!inG[i]) continue;
+    if (own_pair) {  // +-ps (real pair) or +-i ps (conjugate pair) about pcen, in the nodes' own order
+      const bool lower = (nd[i].mu.re - pcen < 0) | (nd[i].mu.im < 0);
+      const double sgn = lower ? -1.0 : 1.0;
+      off[i] = preal ? cmk(sgn * ps, 0.0) : cmk(0.0, sgn * ps);
+      nd[i].mu = cmk(pcen + off[i].re, off[i].im);
+      nd[i].x = cmk(nd[i].mu.re - m, nd[i].mu.im);
+    } else {
+      off[i] = cmk(nd[i].x.re - cxg, nd[i].x.im);
+    }
   }
 
-  // ---- single real nodes far from m: Newton (gmf_kernel.hpp:462-476)
-#define MF_FAR_NEWTON(I)                                                                           \
-  {                                                                                                \
-    bool mask = !inG[I] & !ab[I] & (x[I].im == 0) & (fabs(x[I].re) > 0.5 * fabs(m));              \
-    if (mask) {                                                                                    \
-      newton<I>(As, mu);                                                                           \
-      ab[I] = true;                                                                                \
-      x[I] = cmk(mu[I].re - m, mu[I].im);                                                          \
-    }                                                                                              \
+  // ---- single real nodes far from the shift (|x| > |m| / 2): Newton on det(As - mu I)
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    if (inG[i] | nd[i].refined | (nd[i].x.im != 0) | !(fabs(nd[i].x.re) > 0.5 * fabs(m))) continue;
+    const int j = i == 0 ? 1 : 0, k = i == 2 ? 1 : 2;
+    nd[i].mu.re = newton_real(As, nd[i].mu.re, nd[j].mu, nd[k].mu);
+    nd[i].refined = true;
+    nd[i].x = cmk(nd[i].mu.re - m, nd[i].mu.im);
   }
-  MF_FAR_NEWTON(0)
-  MF_FAR_NEWTON(1)
-  MF_FAR_NEWTON(2)
-#undef MF_FAR_NEWTON
-  bool absc = (inG[0] & ab[0]) | (inG[1] & ab[1]) | (inG[2] & ab[2]);
+  // the series' pole: the outside node of a pair group, at its distance from the centre
+  const bool grp_refined = (inG[0] & nd[0].refined) | (inG[1] & nd[1].refined) | (inG[2] & nd[2].refined);
   double apole = 0.0;
 #pragma unroll
-  for (int k = 0; k < 3; k++) apole = sel(pk[k], sel(absc | ab[k], cmu - mu[k].re, cxg - x[k].re), apole);
-  double xshift = KIND == EXP ? tmax(tmax(x[0].re, x[1].re), x[2].re) : 0.0;
-  bool bad = KIND == EXP ? false
-                         : (((x[0].im == 0) & (mu[0].re <= 0)) | ((x[1].im == 0) & (mu[1].re <= 0)) |
-                            ((x[2].im == 0) & (mu[2].re <= 0)));
+  for (int k = 0; k < 3; k++)
+    if (pk[k]) apole = (grp_refined | nd[k].refined) ? cmu - nd[k].mu.re : cxg - nd[k].x.re;
+  const double xshift = KIND == EXP ? tmax(tmax(nd[0].x.re, nd[1].x.re), nd[2].x.re) : 0.0;
+  // log, powers: a real eigenvalue <= 0 lies outside the domain (NaN results)
+  bool bad = false;
+  if (KIND != EXP) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) bad = bad | ((nd[i].x.im == 0) & (nd[i].mu.re <= 0));
+  }
 
-  // ---- group series (gmf_kernel.hpp:478-533)
-  bool hasg = inG[0] | inG[1] | inG[2];
-  double L = KIND == EXP ? 1.0 : sel(hasg & (cmu > 0), cmu, 1.0), iL = 1.0 / L;
+  // ---- the series variable u = offset / L (L = the group centre for log and powers), its pole, the number of terms
+  const bool hasg = gn > 0;
+  const double L = KIND == EXP ? 1.0 : ((hasg & (cmu > 0)) ? cmu : 1.0), iL = 1.0 / L;
   cx u[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) u[i] = cscl(off[i], iL);
-  double ap = sel(fabs(apole) > 0, apole * iL, 1.0), iap = 1.0 / ap;
-  double rr = tmax(cabs_s(u[0]), tmax(cabs_s(u[1]), cabs_s(u[2])));
-  double rq = sel((pk[0] | pk[1] | pk[2]) & (rr * fabs(iap) <= 1.0), rr * fabs(iap), 0.0);
-  rr = sel(hasg & (rr <= G_R_EXP + 0.5), rr, 0.0);
-  int j1 = G_KMAX, j2 = G_KMAX;  // (no group: nterms is not called and the split points are not used)
+  const double ap = fabs(apole) > 0 ? apole * iL : 1.0, iap = 1.0 / ap;
+  double rr = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) rr = tmax(rr, u[i].im == 0 ? fabs(u[i].re) : cabs_s(u[i]));
+  const bool anypk = pk[0] | pk[1] | pk[2];
+  const double rq = (anypk & (rr * fabs(iap) <= 1.0)) ? rr * fabs(iap) : 0.0;
+  rr = (hasg & (rr <= G_R_EXP + 0.5)) ? rr : 0.0;
+  int j1 = G_KMAX, j2 = G_KMAX;
   St.K = hasg ? nterms(C, 3 * (ORDER + 1) - 1, rr, rq, j1, j2) : 0;
-  // the float-float / FP32 tail of the series: log and pow without a pole node, coefficients within FP32's range
-  const bool tail = (C.ffser != 0) & !(pk[0] | pk[1] | pk[2]) & (rr <= 4.0);
+  // the float-float / FP32 tail of the series: groups without a pole node, coefficients within FP32's range
+  const bool tail = (C.ffser != 0) & !anypk & (rr <= 4.0);
   j1 = tail ? j1 : G_KMAX;
   j2 = tail ? j2 : G_KMAX;
-  bool real = (u[0].im == 0) & (u[1].im == 0) & (u[2].im == 0);
+  const bool real = (u[0].im == 0) & (u[1].im == 0) & (u[2].im == 0);
 #pragma unroll
   for (int k = 0; k < 9; k++) St.As[k] = As[k];
   St.sig = sig; St.m = m; St.cxg = cxg; St.cmu = cmu; St.xshift = xshift; St.iap = iap; St.L = L; St.iL = iL;
+  int fl = (bad ? 512 : 0) | (real ? 1024 : 0) | (j1 << 12) | (j2 << 20);
 #pragma unroll
-  for (int i = 0; i < 3; i++) { St.x[i] = x[i]; St.mu[i] = mu[i]; St.u[i] = u[i]; }
-  St.flags = (ab[0] ? 1 : 0) | (ab[1] ? 2 : 0) | (ab[2] ? 4 : 0) | (inG[0] ? 8 : 0) | (inG[1] ? 16 : 0) |
-             (inG[2] ? 32 : 0) | (pk[0] ? 64 : 0) | (pk[1] ? 128 : 0) | (pk[2] ? 256 : 0) | (bad ? 512 : 0) |
-             (real ? 1024 : 0) | (j1 << 12) | (j2 << 20);
+  for (int i = 0; i < 3; i++) {
+    St.x[i] = nd[i].x;
+    St.mu[i] = nd[i].mu;
+    St.u[i] = u[i];
+    fl |= (nd[i].refined ? 1 << i : 0) | (inG[i] ? 8 << i : 0) | (pk[i] ? 64 << i : 0);
+  }
+  St.flags = fl;
+}
+
+// the key by which a CTA orders its matrices before gmf_finish, so that a warp's lanes do the same work: the class
+// (no group: real or complex nodes; real series; complex series), longer series first, then the group's node pattern
+MF_D unsigned gmf_finish_key(const GmfState &St) {
+  const bool allreal = (St.x[0].im == 0) & (St.x[1].im == 0) & (St.x[2].im == 0);
+  const unsigned cls = St.K == 0 ? (allreal ? 0u : 1u) : ((St.flags & 1024) ? 2u : 3u);
+  return (cls << 16) | ((unsigned)(255 - St.K) << 6) | (unsigned)((St.flags >> 3) & 63);
 }
 
 template <int KIND, int ORDER>
@@ -759,6 +821,164 @@ MF_D void gmf_classify(const double *a, const GmfCoef &C, GmfState &St) {
   cx x[3];
   gmf_roots<KIND>(a, x);
   gmf_classify_from<KIND, ORDER>(a, x, C, St);
+}
+
+// ---- single nodes.  The arithmetic is real where every node is real (V = double), complex otherwise (V = cx).
+MF_D double vsub(double a, double b) { return a - b; }
+MF_D cx vsub(cx a, cx b) { return csub(a, b); }
+MF_D double vadd(double a, double b) { return a + b; }
+MF_D cx vadd(cx a, cx b) { return cadd(a, b); }
+MF_D double vmul(double a, double b) { return a * b; }
+MF_D cx vmul(cx a, cx b) { return cmul(a, b); }
+MF_D double vscl(double a, double s) { return a * s; }
+MF_D cx vscl(cx a, double s) { return cscl(a, s); }
+MF_D double vinv(double a) { return 1.0 / a; }
+MF_D cx vinv(cx a) { return cinv_s(a); }
+MF_D void vset(double &v, cx a) { v = a.re; }
+MF_D void vset(cx &v, cx a) { v = a; }
+MF_D cx vcx(double a) { return cmk(a, 0.0); }
+MF_D cx vcx(cx a) { return a; }
+MF_D double vzero(double) { return 0.0; }
+MF_D cx vzero(cx) { return cmk(0.0, 0.0); }
+
+// Taylor coefficients t = (f, f', f''/2) at the node z (the eigenvalue of As; x = z - m, relative to the shift) of
+// the function whose divided differences the kernel forms: exp e^(x - xshift) (times e^(m + xshift) at the end); log
+// log(sig z), as log(sig m) + log1p(x / m) for |x| <= m / 2; powers (z / rho)^al, rho a power of two near the largest
+// |node| (the blocks of output order k are multiplied by (sig rho)^(al - k) rho^k afterwards).  Real z: real
+// arithmetic (z > 0 for log and powers; a real node <= 0 makes every result of the matrix NaN in any case).
+template <int KIND, typename V>
+MF_D void node_taylor(const GmfCoef &C, double sig, double m, double xshift, double rho, cx x, cx z, V *t) {
+  if (KIND == EXP) {
+    const double e = exp(x.re - xshift);
+    cx f0 = cmk(e, 0.0);
+    if (x.im != 0) f0 = cmk(e * cos(x.im), e * sin(x.im));
+    vset(t[0], f0);
+    t[1] = t[0];
+    t[2] = vscl(t[0], 0.5);
+    return;
+  }
+  V iz;
+  vset(iz, z.im == 0 ? cmk(1.0 / z.re, 0.0) : cinv_s(z));
+  if (KIND == LOG) {
+    const double ax = x.im == 0 ? fabs(x.re) : cabs_s(x);
+    cx f0;
+    if ((m > 0) & (ax <= 0.5 * m)) {  // near the shift: log(sig m) + log1p(x / m)
+      const double zr = x.re / m, zi = x.im / m;
+      f0 = cmk(log(sig * m) + 0.5 * log1p(zr * (2.0 + zr) + zi * zi), x.im == 0 ? 0.0 : atan2(zi, 1.0 + zr));
+    } else {
+      f0 = z.im == 0 ? cmk(log(sig * fabs(z.re)), atan2(0.0, z.re)) : cmk(log(sig * cabs_s(z)), atan2(z.im, z.re));
+    }
+    vset(t[0], f0);
+    t[1] = iz;
+    t[2] = vscl(vmul(iz, iz), -0.5);
+    return;
+  }
+  cx f0;
+  if (z.im == 0) {
+    f0 = cmk(pow_split(fabs(z.re) / rho, C.bh[0], C.bl[0]), 0.0);
+  } else {
+    const double mag = pow_split(cabs_s(z) / rho, C.bh[0], C.bl[0]), ph = C.al * atan2(z.im, z.re);
+    f0 = cmk(mag * cos(ph), mag * sin(ph));
+  }
+  vset(t[0], f0);
+  t[1] = vscl(vmul(t[0], iz), C.al);
+  t[2] = vscl(vmul(t[1], iz), 0.5 * (C.al - 1.0));
+}
+
+// the difference of nodes p and q: between the refined eigenvalues where either was refined against A, else between
+// the deviator's roots
+template <typename V>
+MF_D V node_diff(const cx *x, const cx *mu, const bool *ab, int p, int q) {
+  V d;
+  vset(d, (ab[p] | ab[q]) ? csub(mu[p], mu[q]) : csub(x[p], x[q]));
+  return d;
+}
+
+// No group (three single nodes, pairwise apart): the divided differences over multiplicity vectors (a, b, c), each at
+// most ORDER + 1, by the Hermite recursion
+//   f[z0^a z1^b z2^c] = (f[N - z_q] - f[N - z_p]) / (z_p - z_q),   p < q the first two nodes with nonzero multiplicity
+// from f[z^k] = f^(k-1)(z) / (k-1)!: 54 steps of one difference and one product at order 2.
+template <int KIND, int ORDER, typename V>
+MF_D void dd_three_single(const GmfCoef &C, double sig, double m, double xshift, double rho, const cx *x,
+                          const cx *mu, const bool *ab, const double *bs, cx *D) {
+  constexpr int M = ORDER + 1, ND = ORDER == 0 ? 3 : (ORDER == 1 ? 9 : 19);
+  V t[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) node_taylor<KIND, V>(C, sig, m, xshift, rho, x[i], mu[i], t[i]);
+  const V i01 = vinv(node_diff<V>(x, mu, ab, 0, 1)), i02 = vinv(node_diff<V>(x, mu, ab, 0, 2)),
+          i12 = vinv(node_diff<V>(x, mu, ab, 1, 2));
+  V G[M + 1][M + 1][M + 1];
+#pragma unroll
+  for (int k = 1; k <= M; k++) {
+    G[k][0][0] = t[0][k - 1];
+    G[0][k][0] = t[1][k - 1];
+    G[0][0][k] = t[2][k - 1];
+  }
+#pragma unroll
+  for (int s = 2; s <= 3 * M; s++)
+#pragma unroll
+    for (int a = 0; a <= M; a++)
+#pragma unroll
+      for (int b = 0; b <= M; b++) {
+        const int c = s - a - b;
+        if (c < 0 || c > M || (int)(a > 0) + (int)(b > 0) + (int)(c > 0) < 2) continue;
+        if (a > 0 && b > 0) {         // nodes 0, 1
+          G[a][b][c] = vmul(vsub(G[a][b - 1][c], G[a - 1][b][c]), i01);
+        } else if (a > 0) {           // nodes 0, 2
+          G[a][b][c] = vmul(vsub(G[a][b][c - 1], G[a - 1][b][c]), i02);
+        } else {                      // nodes 1, 2
+          G[a][b][c] = vmul(vsub(G[a][b][c - 1], G[a][b - 1][c]), i12);
+        }
+      }
+#pragma unroll
+  for (int e = 0; e < ND; e++) D[e] = cscl(vcx(G[gms(e, 0)][gms(e, 1)][gms(e, 2)]), bs[gms(e, 0) - 1]);
+}
+
+// Beside a pair group: the residue of the single node I, the coefficient of tau^(m_I - 1) in
+// f(z_I + tau) prod_(z != I) (z_I - z + tau)^(-m_z), with (d + tau)^(-n) = d^(-n) (1 - n tau / d + n (n+1) / 2 tau^2 / d^2
+// - ...), added to each entry with m_I > 0
+template <int KIND, int ORDER, typename V, int I>
+MF_D void dd_residue(const GmfCoef &C, double sig, double m, double xshift, double rho, const cx *x, const cx *mu,
+                     const bool *ab, const double *bs, cx *D) {
+  constexpr int ND = ORDER == 0 ? 3 : (ORDER == 1 ? 9 : 19);
+  constexpr int A = I == 0 ? 1 : 0, B = I == 2 ? 1 : 2;  // the other two nodes
+  V t[3];
+  node_taylor<KIND, V>(C, sig, m, xshift, rho, x[I], mu[I], t);
+  V wa[ORDER + 4], wb[ORDER + 4];  // powers 0 .. ORDER + 3 of 1 / (z_I - z_A), 1 / (z_I - z_B)
+  wa[1] = vinv(node_diff<V>(x, mu, ab, I, A));
+  wb[1] = vinv(node_diff<V>(x, mu, ab, I, B));
+  vset(wa[0], cmk(1.0, 0.0));
+  wb[0] = wa[0];
+#pragma unroll
+  for (int e = 2; e < ORDER + 4; e++) { wa[e] = vmul(wa[e - 1], wa[1]); wb[e] = vmul(wb[e - 1], wb[1]); }
+#pragma unroll
+  for (int e = 0; e < ND; e++) {
+    const int mi = gms(e, I), ma = gms(e, A), mb = gms(e, B);
+    if (mi == 0) continue;
+    // coefficients of the two expansions up to tau^(mi - 1)
+    V pa[3], pb[3];
+#pragma unroll
+    for (int k = 0; k < mi; k++) {
+      const double ca = k == 0 ? 1.0 : (k == 1 ? -(double)ma : 0.5 * ma * (ma + 1));
+      const double cb = k == 0 ? 1.0 : (k == 1 ? -(double)mb : 0.5 * mb * (mb + 1));
+      pa[k] = ma == 0 ? (k == 0 ? wa[0] : vzero(wa[0])) : vscl(wa[ma + k], ca);
+      pb[k] = mb == 0 ? (k == 0 ? wb[0] : vzero(wb[0])) : vscl(wb[mb + k], cb);
+    }
+    V r = vzero(t[0]);
+#pragma unroll
+    for (int j = 0; j < mi; j++) {  // t_j * (pa pb)_(mi - 1 - j)
+      const int d = mi - 1 - j;
+      V q = vzero(t[0]);
+#pragma unroll
+      for (int k = 0; k <= d; k++) {
+        if (ma == 0 && k > 0) continue;
+        if (mb == 0 && d - k > 0) continue;
+        q = vadd(q, ma == 0 ? pb[d - k] : (mb == 0 ? pa[k] : vmul(pa[k], pb[d - k])));
+      }
+      r = vadd(r, vmul(t[j], q));
+    }
+    D[e] = cadd(D[e], cscl(vcx(r), bs[gms(e, 0) - 1]));
+  }
 }
 
 // the second half: divided differences (series, residues), real basis, F and the reduced D2', D3'
@@ -818,64 +1038,28 @@ MF_D void gmf_finish(const GmfState &St, const GmfCoef &C, GmfRec &R) {
       D[c] = cscl(D[c], fac);
     }
   }
-  // ---- residues of the single nodes (gmf_kernel.hpp:534-576)
+  // ---- single nodes: with no group the divided differences of all three by the Hermite recursion, beside a pair
+  // group the residue of the one outside node; powers rescaled per output order (node_taylor)
+  const double rho = KIND == POW ? pow2safe(tmax(tmax(cabs_s(mu[0]), cabs_s(mu[1])), cabs_s(mu[2]))) : 1.0;
+  double bs[3] = {1.0, 1.0, 1.0};  // the scale of each output order's block
+  if (KIND == POW) {
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
-    if (inG[i]) continue;
-    cx xs = KIND == EXP ? cmk(x[i].re - xshift, x[i].im) : x[i];
-    cx f0[3];
-    f0[0] = coef0<KIND>(C, sig, m, xs, mu[i], 0);
-    if (KIND == POW && ORDER >= 1) f0[1] = coef0<KIND>(C, sig, m, xs, mu[i], 1);
-    if (KIND == POW && ORDER >= 2) f0[2] = coef0<KIND>(C, sig, m, xs, mu[i], 2);
-    cx imu = cinv_s(mu[i]);
-    // powers w_z^e (e = 1..5) of 1 / (mu_i - mu_z) for the two other nodes z: the Taylor coefficients of
-    // 1 / (t - mu_z)^mz at mu_i are (w^mz, -mz w^(mz+1), mz (mz+1)/2 w^(mz+2))
-    const int za = i == 0 ? 1 : 0, zb = i == 2 ? 1 : 2;
-    cx wa[6], wb[6];
-    wa[0] = cmk(1.0, 0.0);
-    wb[0] = cmk(1.0, 0.0);
-    wa[1] = cinv_s(csel(ab[i] | ab[za], csub(mu[i], mu[za]), csub(x[i], x[za])));
-    wb[1] = cinv_s(csel(ab[i] | ab[zb], csub(mu[i], mu[zb]), csub(x[i], x[zb])));
-#pragma unroll
-    for (int e = 2; e < 6; e++) { wa[e] = cmul(wa[e - 1], wa[1]); wb[e] = cmul(wb[e - 1], wb[1]); }
-#pragma unroll
-    for (int c = 0; c < ND; c++) {
-      const int mi = gms(c, i);
-      if (mi == 0) continue;
-      const int k = gms(c, 0) - 1, ma = gms(c, za), mb = gms(c, zb);
-      cx fb = KIND == POW ? f0[k] : f0[0], ser[3];
-      if (KIND == EXP) {
-        ser[0] = fb; ser[1] = fb; ser[2] = cscl(fb, 0.5);
-      } else if (KIND == LOG) {
-        ser[0] = fb; ser[1] = imu; ser[2] = cscl(cmul(imu, imu), -0.5);
-      } else {
-        ser[0] = fb;
-        ser[1] = cscl(cmul(fb, imu), C.al);
-        ser[2] = cscl(cmul(ser[1], imu), (C.al - 1.0) / 2.0);
-      }
-      // coefficient mi - 1 of ser * Pa * Pb (truncated products, only the terms that are needed)
-      cx pa[3], pb[3];
-      pa[0] = wa[ma];
-      pb[0] = wb[mb];
-      if (mi >= 2) {
-        pa[1] = ma ? cscl(wa[ma + 1], (double)-ma) : cmk(0.0, 0.0);
-        pb[1] = mb ? cscl(wb[mb + 1], (double)-mb) : cmk(0.0, 0.0);
-      }
-      if (mi >= 3) {
-        pa[2] = ma ? cscl(wa[ma + 2], ma * (ma + 1) / 2.0) : cmk(0.0, 0.0);
-        pb[2] = mb ? cscl(wb[mb + 2], mb * (mb + 1) / 2.0) : cmk(0.0, 0.0);
-      }
-      cx q[3];
-      q[0] = ma ? (mb ? cmul(pa[0], pb[0]) : pa[0]) : pb[0];
-      if (mi >= 2) q[1] = cadd(ma ? (mb ? cmul(pa[0], pb[1]) : cmk(0.0, 0.0)) : pb[1],
-                               mb ? (ma ? cmul(pa[1], pb[0]) : cmk(0.0, 0.0)) : pa[1]);
-      if (mi >= 3) q[2] = cadd(cadd(ma ? (mb ? cmul(pa[0], pb[2]) : cmk(0.0, 0.0)) : pb[2],
-                                    (ma && mb) ? cmul(pa[1], pb[1]) : cmk(0.0, 0.0)),
-                               mb ? (ma ? cmul(pa[2], pb[0]) : cmk(0.0, 0.0)) : pa[2]);
-      cx r = cmul(ser[0], q[mi - 1]);
-      if (mi >= 2) r = cadd(r, cmul(ser[1], q[mi - 2]));
-      if (mi >= 3) r = cadd(r, cmul(ser[2], q[0]));
-      D[c] = cadd(D[c], r);
+    for (int k = 0; k <= ORDER; k++) bs[k] = pow_split(sig * rho, C.bh[k], C.bl[k]) * (k == 0 ? 1.0 : (k == 1 ? rho : rho * rho));
+  }
+  const bool allreal = (x[0].im == 0) & (x[1].im == 0) & (x[2].im == 0);
+  if (!hasg) {
+    if (allreal) dd_three_single<KIND, ORDER, double>(C, sig, m, xshift, rho, x, mu, ab, bs, D);
+    else dd_three_single<KIND, ORDER, cx>(C, sig, m, xshift, rho, x, mu, ab, bs, D);
+  } else {
+    // (a pair group leaves one single node)
+    if (allreal) {
+      if (!inG[0]) dd_residue<KIND, ORDER, double, 0>(C, sig, m, xshift, rho, x, mu, ab, bs, D);
+      else if (!inG[1]) dd_residue<KIND, ORDER, double, 1>(C, sig, m, xshift, rho, x, mu, ab, bs, D);
+      else if (!inG[2]) dd_residue<KIND, ORDER, double, 2>(C, sig, m, xshift, rho, x, mu, ab, bs, D);
+    } else {
+      if (!inG[0]) dd_residue<KIND, ORDER, cx, 0>(C, sig, m, xshift, rho, x, mu, ab, bs, D);
+      else if (!inG[1]) dd_residue<KIND, ORDER, cx, 1>(C, sig, m, xshift, rho, x, mu, ab, bs, D);
+      else if (!inG[2]) dd_residue<KIND, ORDER, cx, 2>(C, sig, m, xshift, rho, x, mu, ab, bs, D);
     }
   }
 

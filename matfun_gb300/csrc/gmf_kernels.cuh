@@ -385,8 +385,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
       GmfState St;
       gmf_classify_from<KIND, OD>(a, x, C, St);
       S.state[mi] = St;
-      const unsigned cls = St.K == 0 ? 0u : ((St.flags & 1024) ? 1u : 2u);
-      key2 = (cls << 16) | ((unsigned)(255 - St.K) << 6) | (unsigned)((St.flags >> 3) & 63);
+      key2 = gmf_finish_key(St);
     }
     S.key[mi] = key2;  // (every thread finished reading the first keys before the last barrier)
   }
