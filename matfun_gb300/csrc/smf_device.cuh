@@ -1,15 +1,19 @@
-// smf_device.cuh -- per-matrix device math of the symmetric family (FP64, one thread per matrix):
-//   * closed-form eigensystem of a symmetric 3x3 matrix (deviator + Smith's trigonometric formula, cross-product
-//     eigenvector, Jacobi rotation by half-angle formulas) -- c/include/matfun/smf_kernel.hpp:200-280
-//   * f of the eigenvalues with the log1p form near the mean -- smf_kernel.hpp:75-82, 281-290
-//   * stable first / second divided differences -- smf_kernel.hpp:84-192
+// smf_device.cuh -- per-matrix device math of the symmetric family (FP64, one thread per matrix), the method of the
+// reference's c/include/matfun/smf_kernel.hpp (Daleckii-Krein forms over a closed-form eigensystem):
+//   * the eigensystem of a symmetric 3x3 matrix: its deviator's eigenvalue farthest from the other two by the
+//     trigonometric formula (Smith), that eigenvalue's eigenvector as the longest cross product of two rows of the
+//     shifted deviator, an orthonormal complement, and the remaining pair by a Jacobi rotation of the 2x2 block;
+//     eigenvalues as Rayleigh quotients of A (and of the deviator, for log near the mean)
+//   * f of the eigenvalues (log through log1p near the mean)
+//   * the first and second divided differences f[a, b], f[x, y, z] with their stable forms for close arguments
 // and the eigen-basis quantities the kernels contract into J and H:
 //   Et_p = V^T E_p V for the six Voigt basis matrices E_p,
 //   J_{I,p}   = w_I  K(I, p),       K(X, Y)    = sum_ab D_ab X_ab Y_ab                       (21 distinct)
 //   H_{I,p,q} = w_I  G'(I, p, q),   G'(X, Y, Z) = 2 sum_amb D2_amb X_ab Y_am Z_mb           (56 distinct)
 // with w_I = 1 for a diagonal and 1/2 for an off-diagonal Voigt index I.  K and G' are symmetric in all their
 // arguments (D and D2 are symmetric, the Et are symmetric matrices), so only the sorted index tuples are computed;
-// the reference assembles all 36 / 126 entries (smf_kernel.hpp:297-381).  Same branch thresholds as the reference.
+// the reference assembles all 36 / 126 entries (smf_kernel.hpp:297-381).  The branch thresholds of the divided
+// differences and of the eigensystem are the method's (they define the result the parity tests hold this code to).
 #pragma once
 #include "mf_common.cuh"
 
@@ -63,87 +67,121 @@ struct SmfEig {
   double lam[3], V[3][3], xd[3], m, sig;
 };
 
+// y = M x for the symmetric M with diagonal (d0, d1, d2) and off-diagonal (o01, o02, o12)
+MF_D void symv3(double d0, double d1, double d2, double o01, double o02, double o12, const double *x, double *y) {
+  y[0] = d0 * x[0] + o01 * x[1] + o02 * x[2];
+  y[1] = o01 * x[0] + d1 * x[1] + o12 * x[2];
+  y[2] = o02 * x[0] + o12 * x[1] + d2 * x[2];
+}
+MF_D double sdot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+MF_D void scross3(const double *a, const double *b, double *c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
 template <int KIND>
 MF_D void smf_eigsys(const double *v, SmfEig &E) {
   constexpr double SQRT6 = 2.449489742783178, TWO_PI_3 = 2.0943951023931957;
-  // power-of-two scale sig ~ max|v| (exact; the pairwise select tree keeps the reference's NaN behaviour)
-  double s01 = tmax(fabs(v[0]), fabs(v[1])), s23 = tmax(fabs(v[2]), fabs(v[3]));
-  double s45 = tmax(fabs(v[4]), fabs(v[5]));
-  double sig = pow2floor(tmax(tmax(s01, s23), s45) + 1e-300), isig = 1.0 / sig;
-  double a0 = v[0] * isig, a1 = v[1] * isig, a2 = v[2] * isig, a3 = v[3] * isig, a4 = v[4] * isig,
-               a5 = v[5] * isig;
-  // deviator, its trace residue removed, normalised by a power of two
-  double m = (a0 + a1 + a2) / 3.0, d0 = a0 - m, d1 = a1 - m, d2 = a2 - m;
-  double tr3 = (d0 + d1 + d2) / 3.0, e0 = d0 - tr3, e1 = d1 - tr3, e2 = d2 - tr3;
-  double z01 = tmax(fabs(e0), fabs(e1)), z23 = tmax(fabs(e2), fabs(a3)), z45 = tmax(fabs(a4), fabs(a5));
-  double dmax = tmax(tmax(z01, z23), z45);
-  bool iso = dmax <= 1e-300;
-  double ids = 1.0 / sel(iso, 1.0, pow2floor(dmax));
-  double g0 = e0 * ids, g1 = e1 * ids, g2 = e2 * ids, g3 = a3 * ids, g4 = a4 * ids, g5 = a5 * ids;
-  // the eigenvalue farthest from the other two (Smith)
+  // 1. an exact power-of-two scale sig ~ max |v| (products up to |A|^4 below then neither overflow nor underflow)
+  const double sig = pow2floor(tmax(tmax(tmax(fabs(v[0]), fabs(v[1])), tmax(fabs(v[2]), fabs(v[3]))),
+                                    tmax(fabs(v[4]), fabs(v[5]))) + 1e-300);
+  const double is = 1.0 / sig;
+  double a[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) a[k] = v[k] * is;
+  // 2. the deviator d = A - m I, and its traceless part (the rounding residue of m removed) normalised by a power of
+  //    two: g = (d - tr(d) / 3 I) / 2^k, so that the closed form sees a traceless matrix of magnitude ~1
+  const double m = (a[0] + a[1] + a[2]) / 3.0;
+  const double d[3] = {a[0] - m, a[1] - m, a[2] - m};
+  const double res = (d[0] + d[1] + d[2]) / 3.0;
+  const double e[3] = {d[0] - res, d[1] - res, d[2] - res};
+  const double dmax = tmax(tmax(tmax(fabs(e[0]), fabs(e[1])), tmax(fabs(e[2]), fabs(a[3]))),
+                           tmax(fabs(a[4]), fabs(a[5])));
+  const bool iso = dmax <= 1e-300;  // A = m I: every vector is an eigenvector
+  const double ig = iso ? 1.0 : 1.0 / pow2floor(dmax);
+  const double g0 = e[0] * ig, g1 = e[1] * ig, g2 = e[2] * ig, g3 = a[3] * ig, g4 = a[4] * ig, g5 = a[5] * ig;
+  // 3. the root of the normalised deviator farthest from the other two: with p = tr g^2, q = det g, cos(3 phi) =
+  //    3 sqrt(6) q / p^(3/2), root = sqrt(2 p / 3) cos(phi) (phi + 2 pi / 3 for a negative cosine)
   double p = g0 * g0 + g1 * g1 + g2 * g2 + 2.0 * (g3 * g3 + g4 * g4 + g5 * g5);
   double q = g0 * (g1 * g2 - g5 * g5) - g3 * (g3 * g2 - g5 * g4) + g4 * (g3 * g5 - g1 * g4);
-  double pg = sel(iso, 1.0, p), qg = sel(iso, 0.0, q);
-  double r = 3.0 * SQRT6 * qg / (pg * sqrt(pg));
-  r = sel(r > 1.0, 1.0, sel(r < -1.0, -1.0, r));
-  double t = sqrt(2.0 * pg / 3.0), ph = acos(r) / 3.0;
-  double sh = t * cos(sel(r >= 0, ph, ph + TWO_PI_3));
-  // its eigenvector: the longest cross product of two rows of the shifted deviator
-  double m00 = g0 - sh, m11 = g1 - sh, m22 = g2 - sh;
-  double cxv = g3 * g5 - g4 * m11, cyv = g4 * g3 - m00 * g5, czv = m00 * m11 - g3 * g3;
-  double nn = cxv * cxv + cyv * cyv + czv * czv;
-  {
-    double bx = g3 * m22 - g4 * g5, by = g4 * g4 - m00 * m22, bz = m00 * g5 - g3 * g4;
-    double nb = bx * bx + by * by + bz * bz;
-    bool s1 = nb > nn;
-    cxv = sel(s1, bx, cxv); cyv = sel(s1, by, cyv); czv = sel(s1, bz, czv); nn = sel(s1, nb, nn);
-    double ex = m11 * m22 - g5 * g5, ey = g5 * g4 - g3 * m22, ez = g3 * g5 - m11 * g4;
-    double ne = ex * ex + ey * ey + ez * ez;
-    bool s2 = ne > nn;
-    cxv = sel(s2, ex, cxv); cyv = sel(s2, ey, cyv); czv = sel(s2, ez, czv); nn = sel(s2, ne, nn);
+  if (iso) { p = 1.0; q = 0.0; }
+  double c3 = 3.0 * SQRT6 * q / (p * sqrt(p));
+  c3 = c3 > 1.0 ? 1.0 : (c3 < -1.0 ? -1.0 : c3);
+  const double phi = acos(c3) / 3.0;
+  const double root = sqrt(2.0 * p / 3.0) * cos(c3 >= 0 ? phi : phi + TWO_PI_3);
+  // 4. its eigenvector: the longest cross product of two rows of g - root I
+  const double r0[3] = {g0 - root, g3, g4}, r1[3] = {g3, g1 - root, g5}, r2[3] = {g4, g5, g2 - root};
+  double c[3][3];
+  scross3(r0, r1, c[0]);
+  scross3(r0, r2, c[1]);
+  scross3(r1, r2, c[2]);
+  double vv[3] = {c[0][0], c[0][1], c[0][2]}, nn = sdot3(c[0], c[0]);
+#pragma unroll
+  for (int t = 1; t < 3; t++) {
+    const double nt = sdot3(c[t], c[t]);
+    if (nt > nn) {
+      nn = nt;
+      vv[0] = c[t][0]; vv[1] = c[t][1]; vv[2] = c[t][2];
+    }
   }
-  double nrm = sqrt(nn);
-  bool ok = (nrm > 1e-300) & !iso;
-  double inv = 1.0 / sel(ok, nrm, 1.0);
-  double vx = sel(ok, cxv * inv, 1.0), vy = sel(ok, cyv * inv, 0.0), vz = sel(ok, czv * inv, 0.0);
-  // orthonormal complement (u, w)
-  double ax = fabs(vx), ay = fabs(vy), az = fabs(vz);
-  bool k1 = ay < ax, k2 = az < sel(k1, ay, ax);
-  double ex = sel(k1 | k2, 0.0, 1.0), ey = sel(k1 & !k2, 1.0, 0.0), ez = sel(k2, 1.0, 0.0);
-  double vk = ex * vx + ey * vy + ez * vz;
-  double ux = ex - vk * vx, uy = ey - vk * vy, uz = ez - vk * vz;
-  double nu = sqrt(ux * ux + uy * uy + uz * uz);
-  bool oku = nu > 1e-300;
-  double iu = 1.0 / sel(oku, nu, 1.0);
-  ux = sel(oku, ux * iu, 0.0); uy = sel(oku, uy * iu, 0.0); uz = sel(oku, uz * iu, 0.0);
-  double wx = vy * uz - vz * uy, wy = vz * ux - vx * uz, wz = vx * uy - vy * ux;
-  // Rayleigh quotients of A (eigenvalues) and of the deviator (rotation angle; log near m)
-  double Aux = a0 * ux + a3 * uy + a4 * uz, Auy = a3 * ux + a1 * uy + a5 * uz, Auz = a4 * ux + a5 * uy + a2 * uz;
-  double Awx = a0 * wx + a3 * wy + a4 * wz, Awy = a3 * wx + a1 * wy + a5 * wz, Awz = a4 * wx + a5 * wy + a2 * wz;
-  double Avx = a0 * vx + a3 * vy + a4 * vz, Avy = a3 * vx + a1 * vy + a5 * vz, Avz = a4 * vx + a5 * vy + a2 * vz;
-  double a11 = ux * Aux + uy * Auy + uz * Auz, a12 = ux * Awx + uy * Awy + uz * Awz;
-  double a22 = wx * Awx + wy * Awy + wz * Awz, lv = vx * Avx + vy * Avy + vz * Avz;
-  double Dux = d0 * ux + a3 * uy + a4 * uz, Duy = a3 * ux + d1 * uy + a5 * uz, Duz = a4 * ux + a5 * uy + d2 * uz;
-  double Dwx = d0 * wx + a3 * wy + a4 * wz, Dwy = a3 * wx + d1 * wy + a5 * wz, Dwz = a4 * wx + a5 * wy + d2 * wz;
-  double b11 = ux * Dux + uy * Duy + uz * Duz, b12 = ux * Dwx + uy * Dwy + uz * Dwz;
-  double b22 = wx * Dwx + wy * Dwy + wz * Dwz;
-  // Jacobi rotation (cos, sin of half the angle atan2(2 b12, b11 - b22))
-  double jx = b11 - b22, jy = 2.0 * b12, jr = sqrt(jx * jx + jy * jy);
-  bool jz = jr == 0, jpos = jx >= 0;
-  double jrs = sel(jz, 1.0, jr);
-  double big = sqrt((jrs + fabs(jx)) / (2.0 * jrs)), sml = jy / (2.0 * jrs * big);
-  double sgn = sel((jy > 0) | ((jy == 0) & (__double_as_longlong(jy) >= 0)), 1.0, -1.0);
-  double cs = sel(jz, 1.0, sel(jpos, big, sgn * sml)), sn = sel(jz, 0.0, sel(jpos, sml, sgn * big));
+  const double nrm = sqrt(nn);
+  double vx[3] = {1.0, 0.0, 0.0};
+  if ((nrm > 1e-300) & !iso) {
+    const double in = 1.0 / nrm;
+    vx[0] = vv[0] * in; vx[1] = vv[1] * in; vx[2] = vv[2] * in;
+  }
+  // 5. an orthonormal complement: u from the coordinate axis least aligned with v (less its v component), w = v x u
+  const double b0 = fabs(vx[0]), b1 = fabs(vx[1]), b2 = fabs(vx[2]);
+  const bool ay = b1 < b0, az = b2 < (ay ? b1 : b0);
+  const int ax = az ? 2 : (ay ? 1 : 0);
+  const double va = ax == 0 ? vx[0] : (ax == 1 ? vx[1] : vx[2]);
+  double u[3] = {(ax == 0 ? 1.0 : 0.0) - va * vx[0], (ax == 1 ? 1.0 : 0.0) - va * vx[1],
+                 (ax == 2 ? 1.0 : 0.0) - va * vx[2]};
+  const double nu = sqrt(sdot3(u, u));
+  if (nu > 1e-300) {
+    const double in = 1.0 / nu;
+    u[0] *= in; u[1] *= in; u[2] *= in;
+  } else {
+    u[0] = u[1] = u[2] = 0.0;
+  }
+  double w[3];
+  scross3(vx, u, w);
+  // 6. Rayleigh quotients: of A (the eigenvalues, accurate over spectra of many orders of magnitude) and of the
+  //    deviator d (its 2x2 block gives the Jacobi angle without the cancellation of A's near I)
+  double Au[3], Aw[3], Av[3], Du[3], Dw[3];
+  symv3(a[0], a[1], a[2], a[3], a[4], a[5], u, Au);
+  symv3(a[0], a[1], a[2], a[3], a[4], a[5], w, Aw);
+  symv3(a[0], a[1], a[2], a[3], a[4], a[5], vx, Av);
+  symv3(d[0], d[1], d[2], a[3], a[4], a[5], u, Du);
+  symv3(d[0], d[1], d[2], a[3], a[4], a[5], w, Dw);
+  const double a11 = sdot3(u, Au), a12 = sdot3(u, Aw), a22 = sdot3(w, Aw), lv = sdot3(vx, Av);
+  const double b11 = sdot3(u, Du), b12 = sdot3(u, Dw), b22 = sdot3(w, Dw);
+  // 7. the Jacobi rotation (cos, sin of half the angle atan2(2 b12, b11 - b22)) by the half-angle formulas, the larger
+  //    eigenvalue of the block first
+  const double jx = b11 - b22, jy = 2.0 * b12, jr = sqrt(jx * jx + jy * jy);
+  double cs = 1.0, sn = 0.0;
+  if (jr != 0) {
+    const double big = sqrt((jr + fabs(jx)) / (2.0 * jr)), sml = jy / (2.0 * jr * big);
+    const double sg = ((jy > 0) | ((jy == 0) & (__double_as_longlong(jy) >= 0))) ? 1.0 : -1.0;
+    if (jx >= 0) { cs = big; sn = sml; }
+    else { cs = sg * sml; sn = sg * big; }
+  }
   E.lam[0] = lv * sig;
   E.lam[1] = (cs * cs * a11 + 2.0 * cs * sn * a12 + sn * sn * a22) * sig;
   E.lam[2] = (sn * sn * a11 - 2.0 * cs * sn * a12 + cs * cs * a22) * sig;
-  E.V[0][0] = vx; E.V[0][1] = cs * ux + sn * wx; E.V[0][2] = cs * wx - sn * ux;
-  E.V[1][0] = vy; E.V[1][1] = cs * uy + sn * wy; E.V[1][2] = cs * wy - sn * uy;
-  E.V[2][0] = vz; E.V[2][1] = cs * uz + sn * wz; E.V[2][2] = cs * wz - sn * uz;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    E.V[k][0] = vx[k];
+    E.V[k][1] = cs * u[k] + sn * w[k];
+    E.V[k][2] = cs * w[k] - sn * u[k];
+  }
   E.m = m;
   E.sig = sig;
   if (KIND == LOG) {
-    E.xd[0] = vx * (d0 * vx + a3 * vy + a4 * vz) + vy * (a3 * vx + d1 * vy + a5 * vz) + vz * (a4 * vx + a5 * vy + d2 * vz);
+    double Dv[3];
+    symv3(d[0], d[1], d[2], a[3], a[4], a[5], vx, Dv);
+    E.xd[0] = sdot3(vx, Dv);
     E.xd[1] = cs * cs * b11 + 2.0 * cs * sn * b12 + sn * sn * b22;
     E.xd[2] = sn * sn * b11 - 2.0 * cs * sn * b12 + cs * cs * b22;
   }
@@ -169,97 +207,105 @@ MF_D void smf_eigen(const double *v, double al, double lam[3], double fl[3], dou
   }
 }
 
-// first divided difference f[a, b] (smf_kernel.hpp:84-115)
+// ---- first divided differences f[a, b] (f[a, a] = f'(a)) in forms stable for close arguments
+// exp: e^max(a, b) (1 - e^-d) / d, d = |a - b| (no overflow, no cancellation)
+// log: with s = (a + b) / 2, z = (a - b) / (a + b): log a - log b = 2 atanh z, so f[a, b] = atanh(z) / (z s); its
+//      series (1 + z^2/3 + z^4/5 + z^6/7) / s for |z| < 1e-3, and the plain quotient for |z| >= 0.5
+// sqrt: 1 / (sqrt a + sqrt b) (arguments clamped at 0: PSD round-off)
+// powers: with s the mean and z = (a - b) / (2 s): a^al - b^al = s^al ((1 + z)^al - (1 - z)^al), so
+//      f[a, b] = s^(al - 1) (expm1(al log1p z) - expm1(al log1p(-z))) / (2 z) for 0 < |z| < 0.5, al s^(al - 1) at
+//      z = 0, the plain quotient beyond
 template <int KIND>
 MF_D double smf_dd1(double a, double b, double fa, double fb, const SmfCoef &C) {
   if (KIND == EXP) {
-    double d = fabs(a - b);
-    return sel(a > b, fa, fb) * sel(d > 0, -expm1(-d) / d, 1.0);
+    const double d = fabs(a - b);
+    const double fmax = a > b ? fa : fb;
+    return d > 0 ? fmax * (-expm1(-d) / d) : fmax;
   }
   if (KIND == LOG) {
-    double s = 0.5 * (a + b), z = (a - b) / (a + b), az = fabs(z), z2 = z * z;
-    if (az < 1e-3) return (1.0 + z2 / 3.0 + z2 * z2 / 5.0 + z2 * z2 * z2 / 7.0) / s;
+    const double s = 0.5 * (a + b), z = (a - b) / (a + b), az = fabs(z);
     if (az >= 0.5) return (log(a) - log(b)) / (a - b);
+    if (az < 1e-3) {
+      const double z2 = z * z;
+      return (1.0 + z2 / 3.0 + z2 * z2 / 5.0 + z2 * z2 * z2 / 7.0) / s;
+    }
     return atanh(z) / z / s;
   }
-  a = sel(a > 0, a, 0.0);
-  b = sel(b > 0, b, 0.0);
+  a = a > 0 ? a : 0.0;
+  b = b > 0 ? b : 0.0;
   if (KIND == SQRT) return 1.0 / (sqrt(a) + sqrt(b));
-  double s = 0.5 * (a + b), ss = sel(s > 0, s, 1.0);
-  double z = (a - b) / (2.0 * ss), az = fabs(z);
-  bool zero = az == 0, near = !zero & (az < 0.5);
-  if (!zero & !near) return (fa - fb) / (a - b);
-  double al = C.al;
-  double g = zero ? al : (expm1(al * log1p(z)) - expm1(al * log1p(-z))) / (2.0 * z);
-  return (s > 0 ? pow_split(ss, C.bh1, C.bl1) : C.zp1) * g;
+  const double s = 0.5 * (a + b), sp = s > 0 ? s : 1.0;
+  const double z = (a - b) / (2.0 * sp), az = fabs(z);
+  if (az >= 0.5) return (fa - fb) / (a - b);
+  const double g = az == 0 ? C.al : (expm1(C.al * log1p(z)) - expm1(C.al * log1p(-z))) / (2.0 * z);
+  return (s > 0 ? pow_split(sp, C.bh1, C.bl1) : C.zp1) * g;
 }
 
-// f'(x) (smf_kernel.hpp:117-126)
+// f'(x) = f[x, x]
 template <int KIND>
 MF_D double smf_deriv(double x, double fx, const SmfCoef &C) {
   if (KIND == EXP) return fx;
   if (KIND == LOG) return 1.0 / x;
-  x = sel(x > 0, x, 0.0);
+  x = x > 0 ? x : 0.0;
   if (KIND == SQRT) return 1.0 / (2.0 * sqrt(x));
-  return x > 0 ? C.al * pow_split(x, C.bh1, C.bl1) : C.al * C.zp1;
+  return C.al * (x > 0 ? pow_split(x, C.bh1, C.bl1) : C.zp1);
 }
 
-// second divided difference f[li, lj, lk] (smf_kernel.hpp:148-192)
+// ---- second divided differences f[x, y, z] (symmetric; f[x, x, x] = f''(x) / 2).  With the three points sorted,
+// lo <= md <= hi: a cluster (exp: hi - lo <= 1; log, powers: lo and hi within tau md of md > 0) by the Taylor series
+// about md, f[x, y, z] = sum_k f^(k+2)(md) / (k+2)! h_k(lo - md, hi - md), h_k(u, w) = sum_i u^i w^(k-i) (30 terms:
+// the coefficients c2 without their md-dependent factor e^md, 1 / md^2 or md^(al - 2) = f(md) / md^2); otherwise the
+// difference over the most distant pair, (f[md, hi] - f[lo, md]) / (hi - lo).  Powers: arguments clamped at 0, and
+// f''(0) / 2 where all three are 0.
 template <int KIND>
 MF_D double smf_dd2(double li, double lj, double lk, double fi, double fj, double fk, double Dij, double Dik,
                     double Djk, const SmfCoef &C) {
   if (KIND == POW || KIND == SQRT) {
-    li = sel(li > 0, li, 0.0); lj = sel(lj > 0, lj, 0.0); lk = sel(lk > 0, lk, 0.0);
+    li = li > 0 ? li : 0.0; lj = lj > 0 ? lj : 0.0; lk = lk > 0 ? lk : 0.0;
   }
-  double dA = lk - li, dB = lj - li, dC = lk - lj, aA = fabs(dA), aB = fabs(dB), aC = fabs(dC);
-  bool useA = (aA >= aB) & (aA >= aC), useB = !useA & (aB >= aC);
-  double num = sel(useA, Djk - Dij, sel(useB, Djk - Dik, Dik - Dij));
-  double den = sel(useA, dA, sel(useB, dB, dC));
-  double mn = sel(li < lj, li, lj), mx = sel(li < lj, lj, li);
-  double lo = sel(mn < lk, mn, lk), hi = sel(mx > lk, mx, lk), t = sel(mx < lk, mx, lk), mid = sel(mn > t, mn, t);
+  // sort (i, j, k) into (lo, md, hi), carrying f and the first differences of the pairs
+  double x0 = li, x1 = lj, x2 = lk, f0 = fi, f1 = fj, f2 = fk, d01 = Dij, d02 = Dik, d12 = Djk, t;
+  if (x1 < x0) { t = x0; x0 = x1; x1 = t; t = f0; f0 = f1; f1 = t; t = d02; d02 = d12; d12 = t; }
+  if (x2 < x1) { t = x1; x1 = x2; x2 = t; t = f1; f1 = f2; f2 = t; t = d01; d01 = d02; d02 = t; }
+  if (x1 < x0) { t = x0; x0 = x1; x1 = t; t = f0; f0 = f1; f1 = t; t = d02; d02 = d12; d12 = t; }
+  const double lo = x0, md = x1, hi = x2;
   bool cluster;
+  double u, w, scale;
   if (KIND == EXP) {
-    cluster = (hi - lo) <= 1.0;
+    cluster = hi - lo <= 1.0;
+    u = lo - md; w = hi - md; scale = f1;
   } else {
-    cluster = (mid > 0) & (mid - lo <= C.tau * mid) & (hi - mid <= C.tau * mid);
+    cluster = (md > 0) & (md - lo <= C.tau * md) & (hi - md <= C.tau * md);
+    u = (lo - md) / md; w = (hi - md) / md;
+    scale = (KIND == LOG ? 1.0 : f1) / (md * md);
   }
   double out;
   if (cluster) {
-    double fm = sel(mid == li, fi, sel(mid == lj, fj, fk));
-    double u, w, scale;
-    if (KIND == EXP) {
-      u = lo - mid; w = hi - mid; scale = fm;
-    } else {
-      u = (lo - mid) / mid; w = (hi - mid) / mid;
-      scale = (KIND == LOG ? 1.0 : fm) / (mid * mid);
-    }
-    double h = 1.0, wk = 1.0, s = C.c2[0];
+    double h = 1.0, wk = 1.0, acc = C.c2[0];
 #pragma unroll
-    for (int k = 1; k < DD2_TERMS; k++) {
+    for (int k = 1; k < DD2_TERMS; k++) {  // h_k = u h_(k-1) + w^k
       wk = wk * w;
       h = u * h + wk;
-      s = s + C.c2[k] * h;
+      acc = acc + C.c2[k] * h;
     }
-    out = scale * s;
+    out = scale * acc;
   } else {
-    out = num / sel(den != 0, den, 1.0);
+    const double span = hi - lo;
+    out = (d12 - d01) / (span != 0 ? span : 1.0);
   }
-  if (KIND == POW || KIND == SQRT) out = sel(hi > 0, out, C.z2);
+  if (KIND == POW || KIND == SQRT) out = hi > 0 ? out : C.z2;
   return out;
 }
 
-// f[l, l, l] = f''(l) / 2: the reference's cluster series at u = w = 0 is exactly scale * c2[0]; outside the
-// cluster its difference formula gives (D_ll - D_ll) / 1 (smf_kernel.hpp:148-192, specialised to three equal points)
+// f[l, l, l] = f''(l) / 2: the cluster series at u = w = 0 is its first coefficient times the scale; where l lies
+// outside the cluster test (log, powers at l <= 0) the difference form gives (D_ll - D_ll) / 1
 template <int KIND>
 MF_D double smf_dd2_same(double l, double fl, double Dll, const SmfCoef &C) {
-  if (KIND == POW || KIND == SQRT) l = sel(l > 0, l, 0.0);
-  bool cluster;
-  if (KIND == EXP) cluster = (l - l) <= 1.0;
-  else cluster = (l > 0) & (l - l <= C.tau * l) & (l - l <= C.tau * l);
+  if (KIND == POW || KIND == SQRT) l = l > 0 ? l : 0.0;
   double out;
-  if (KIND == EXP) out = sel(cluster, fl * C.c2[0], Dll - Dll);
-  else out = sel(cluster, ((KIND == LOG ? 1.0 : fl) / (l * l)) * C.c2[0], Dll - Dll);
-  if (KIND == POW || KIND == SQRT) out = sel(l > 0, out, C.z2);
+  if (KIND == EXP) out = fl * C.c2[0];
+  else out = l > 0 ? ((KIND == LOG ? 1.0 : fl) / (l * l)) * C.c2[0] : Dll - Dll;
+  if (KIND == POW || KIND == SQRT) out = l > 0 ? out : C.z2;
   return out;
 }
 
