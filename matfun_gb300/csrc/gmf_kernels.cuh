@@ -37,13 +37,13 @@ namespace mf {
 
 constexpr int GMF_TPB = 128;
 constexpr int GMF_WARPS = GMF_TPB / 32;
+constexpr int GMF_MIN_CTAS = 2;  // CTAs per SM the register allocation of gmf_kernel is bounded for
 constexpr int GMF_REC = 36;  // r1 (9), r2 (9), D2' (6), D3' (10), sc1, sc2
 
 // shared memory layout of one CTA (doubles unless noted)
 struct GmfSmem {
   double x[GMF_TPB * 9];          // input, then F
-  double rec[GMF_TPB * GMF_REC];  // records
-  GmfState state[GMF_TPB];        // the first half's results, by matrix
+  GmfState state[GMF_TPB];        // the first half's results by matrix, then the matrix's record (GMF_REC doubles)
   unsigned key[GMF_TPB];          // sort key of each matrix
   int perm[GMF_TPB];              // processing slot -> matrix
   double work[GMF_WARPS][165 + 405];  // per warp: T6, then Z and Y, then the 405 distinct H values over Z and Y
@@ -269,7 +269,9 @@ MF_D float gmfb_store_h(const TC *wk, TC sc2, const GmfSmem &S, T *o, int lane) 
 // result is recomputed and its J (H) stored again (about 0.5 % (J) and 6 % (H) of random general matrices, under
 // 1 % of the benchmark's).
 constexpr float GMF_F32_AMP = 8.f;
-constexpr int GMF_RECF_BJ = GMF_REC, GMF_RECF_BH = GMF_REC + 1;  // the bounds after the FP32 record
+// the FP32 record in a warp's work area (float offset, past the 570 floats of the FP32 phase B)
+constexpr int GMF_RECF = 1100;
+static_assert(GMF_RECF + GMF_REC <= 2 * (165 + 405), "the FP32 record fits the warp's work area");
 
 // the bounds B_J, B_H of a record rounded to FP32
 MF_D void gmfb_bounds(const float *rc, float &bj, float &bh) {
@@ -307,7 +309,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
     if (e == 9 * p) S.gidx[p] = g;
   }
   static_assert(ORDER < 3 || sizeof(T) == 8, "the tangent form is FP64");
-  static_assert(sizeof(GmfState) >= (GMF_REC + 2) * sizeof(float), "the FP32 record and its bounds fit a state slot");
+  static_assert(sizeof(GmfState) >= GMF_REC * sizeof(double), "a record fits its matrix's state slot");
   constexpr int OD = ORDER == 3 ? 2 : ORDER;  // the order of the derivatives the record holds
   if (ORDER == 2) {  // index tables of phase B
     for (int t = tid; t < 405; t += GMF_TPB) {  // t = 45 (ab) + sym2(cd, ef), cd <= ef
@@ -402,7 +404,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   __syncthreads();
 
   // ---- phase A, finish, in the order of the second key: slot tid takes the matrix of rank tid; F goes straight to
-  // HBM, the record stays in shared memory at the slot
+  // HBM, the record takes the place of the matrix's state (read by gmf_finish and no longer needed)
   const int mine = S.perm[tid];
   if (mine < cnt) {
     GmfRec R;
@@ -419,7 +421,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
       // the scale factors sc1 / sc2 are folded into D2' / D3' when finite and nonzero; otherwise each output entry
       // is multiplied by them (keeping the reference's NaN / Inf); rc[34] / rc[35] hold the factor left to apply.
       // The record stays in FP64 for both storage types (the FP32 path rounds it in phase B).
-      double *rc = S.rec + tid * GMF_REC;
+      double *rc = reinterpret_cast<double *>(&S.state[mine]);
 #pragma unroll
       for (int k = 0; k < 9; k++) { rc[k] = R.r1[k]; rc[9 + k] = R.r2[k]; }
       const bool f1 = isfinite(R.sc1) & (R.sc1 != 0.0);
@@ -434,19 +436,10 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
         for (int k = 0; k < 10; k++) rc[24 + k] = R.D3[k] * s2;
         rc[35] = sel(f2, 1.0, R.sc2);
       }
-      if constexpr (sizeof(T) == 4) {
-        // the FP32 path's record, rounded once, and the bounds of its contractions, in this matrix's state slot
-        // (free once gmf_finish has read it)
-        float *rf = reinterpret_cast<float *>(&S.state[mine]);
+      if (OD < 2) {
 #pragma unroll
-        for (int k = 0; k < (OD >= 2 ? GMF_REC : 24); k++) rf[k] = (float)rc[k];
-        rf[34] = (float)rc[34];
-        rf[35] = OD >= 2 ? (float)rc[35] : 1.f;
-        if (OD < 2) {
-#pragma unroll
-          for (int k = 24; k < 34; k++) rf[k] = 0.f;
-        }
-        gmfb_bounds(rf, rf[GMF_RECF_BJ], rf[GMF_RECF_BH]);
+        for (int k = 24; k < 34; k++) rc[k] = 0.0;
+        rc[35] = 1.0;
       }
     }
   }
@@ -460,7 +453,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   for (int sl = warp * 32; sl < warp * 32 + 32; sl++) {
     const int mi = S.perm[sl];
     if (mi >= cnt) break;  // the padding slots sort last
-    const double *rcd = S.rec + sl * GMF_REC;
+    const double *rcd = reinterpret_cast<const double *>(&S.state[mi]);
     if constexpr (ORDER == 3) {
       gmf_tangent_warp(rcd, S.x + mi * 9, wkd, lane, J ? J + S.gidx[mi] * 9 : nullptr, H + S.gidx[mi] * 81);
       continue;
@@ -475,19 +468,24 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
         gmfb_store_h<double, T>(wkd, rcd[35], S, oh, lane);
       }
     } else {
-      // FP32: contract and store the rounded record; where its bound exceeds GMF_F32_AMP times the largest entry
-      // (uniform in the warp), contract the FP64 record and store the matrix's J (H) again
-      const float *rcf = reinterpret_cast<const float *>(&S.state[mi]);
+      // FP32: the record rounded once (past the FP32 work area) and the bounds of its contractions; contract and store
+      // it; where its bound exceeds GMF_F32_AMP times the largest entry (uniform in the warp), contract the FP64
+      // record and store the matrix's J (H) again
+      float *rcf = wkf + GMF_RECF;
+      for (int k = lane; k < GMF_REC; k += 32) rcf[k] = (float)rcd[k];
+      __syncwarp();
+      float bj, bh;  // (every lane, from the shared copy)
+      gmfb_bounds(rcf, bj, bh);
       gmfb_t4<float>(rcf, wkf, lane);
       const float mj = gmfb_store_j<float, T, true>(wkf, rcf[34], oj, lane);
-      if (rcf[GMF_RECF_BJ] > GMF_F32_AMP * mj) {
+      if (bj > GMF_F32_AMP * mj) {
         gmfb_t4<double>(rcd, wkd, lane);
         gmfb_store_j<double, T>(wkd, rcd[34], oj, lane);
       }
       if (ORDER >= 2) {
         gmfb_u<float>(rcf, wkf, S, lane);
         const float mh = gmfb_store_h<float, T, true>(wkf, rcf[35], S, oh, lane);
-        if (rcf[GMF_RECF_BH] > GMF_F32_AMP * mh) {
+        if (bh > GMF_F32_AMP * mh) {
           gmfb_u<double>(rcd, wkd, S, lane);
           gmfb_store_h<double, T>(wkd, rcd[35], S, oh, lane);
         }
@@ -497,7 +495,7 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
 }
 
 template <int KIND, int ORDER, typename T>
-__global__ void __launch_bounds__(GMF_TPB) gmf_kernel(int64_t n, const T *__restrict__ A, T *__restrict__ F,
+__global__ void __launch_bounds__(GMF_TPB, GMF_MIN_CTAS) gmf_kernel(int64_t n, const T *__restrict__ A, T *__restrict__ F,
                                                       T *__restrict__ J, T *__restrict__ H, const GmfCoef C,
                                                       const int *__restrict__ idx, const double *__restrict__ roots,
                                                       const unsigned char *__restrict__ keys) {
