@@ -28,7 +28,8 @@ struct SmfCoef {
   double bh1, bl1;          // al - 1 split exactly (TwoSum)
   double zp1;               // 0^(al - 1)
   double z2;                // f''(0)/2 for powers: 0 (al == 1) or binom(al, 2) 0^(al - 2)
-  double tau;               // cluster radius of the second divided difference
+  double tau;               // cluster radius of the second divided difference (exp: absolute, else relative)
+  int nterms;               // terms of its cluster series (<= DD2_TERMS)
   double c2[DD2_TERMS];     // Taylor coefficients f^(k+2)/(k+2)! without the m-dependent factor (smf_kernel.hpp:135-146)
 };
 
@@ -50,6 +51,26 @@ inline void smf_coef(int kind, double al, SmfCoef &C) {
   } else {
     double b = al * (al - 1.0) / 2.0;
     for (int k = 0; k < DD2_TERMS; k++) { C.c2[k] = b; b *= (al - k - 2.0) / (k + 3.0); }
+  }
+  // The cluster series is needed only where the difference formula (f[md, hi] - f[lo, md]) / (hi - lo) cancels: its
+  // relative error is about 2 eps f' / ((hi - lo) f''), i.e. 2 eps lambda / (hi - lo) for log, eps / (hi - lo) for exp
+  // and 2 eps lambda / (|al - 1| (hi - lo)) for powers.  So the FP64 path takes the series only within 2^-6 of the
+  // middle point (exp: absolute 2^-4), where about 10 terms reach 1e-17 of the first (the difference formula is then
+  // within 150 eps beyond it), instead of within 0.25 with 30 terms; powers with |al - 1| < 1/4 (f'' small) or al > 12
+  // (growing binomial coefficients) keep 0.25 (3 / al for al > 12) and 30 terms.
+  const bool narrow = kind == EXP || kind == LOG || (std::fabs(al - 1.0) >= 0.25 && al <= 12.0);
+  if (narrow) {
+    C.tau = kind == EXP ? 0.0625 : 0.015625;
+    // the terms of sum_k c2[k] h_k(u, w), |h_k| <= (k + 1) tau^k: stop where the bound of every later term is below
+    // 2^-57 of |c2[0]| (the bound decreases from there on for these coefficients)
+    int n = DD2_TERMS;
+    for (int k = 1; k < DD2_TERMS; k++) {
+      const double bnd = std::fabs(C.c2[k]) * (k + 1) * std::pow(C.tau, k);
+      if (bnd <= 0x1p-57 * std::fabs(C.c2[0]) || C.c2[0] == 0.0) { n = k; break; }
+    }
+    C.nterms = n;
+  } else {
+    C.nterms = DD2_TERMS;
   }
 }
 
@@ -272,7 +293,7 @@ MF_D double smf_dd2(double li, double lj, double lk, double fi, double fj, doubl
   bool cluster;
   double u, w, scale;
   if (KIND == EXP) {
-    cluster = hi - lo <= 1.0;
+    cluster = (md - lo <= C.tau) & (hi - md <= C.tau);
     u = lo - md; w = hi - md; scale = f1;
   } else {
     cluster = (md > 0) & (md - lo <= C.tau * md) & (hi - md <= C.tau * md);
@@ -282,8 +303,8 @@ MF_D double smf_dd2(double li, double lj, double lk, double fi, double fj, doubl
   double out;
   if (cluster) {
     double h = 1.0, wk = 1.0, acc = C.c2[0];
-#pragma unroll
-    for (int k = 1; k < DD2_TERMS; k++) {  // h_k = u h_(k-1) + w^k
+#pragma unroll 4
+    for (int k = 1; k < C.nterms; k++) {  // h_k = u h_(k-1) + w^k
       wk = wk * w;
       h = u * h + wk;
       acc = acc + C.c2[k] * h;
@@ -304,7 +325,7 @@ MF_D double smf_dd2_same(double l, double fl, double Dll, const SmfCoef &C) {
   if (KIND == POW || KIND == SQRT) l = l > 0 ? l : 0.0;
   double out;
   if (KIND == EXP) out = fl * C.c2[0];
-  else out = l > 0 ? ((KIND == LOG ? 1.0 : fl) / (l * l)) * C.c2[0] : Dll - Dll;
+  else out = l > 0 ? ((KIND == LOG ? 1.0 : fl) / (l * l)) * C.c2[0] : Dll - Dll;  // (l > 0: always in the cluster)
   if (KIND == POW || KIND == SQRT) out = l > 0 ? out : C.z2;
   return out;
 }

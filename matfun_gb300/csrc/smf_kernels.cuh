@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(GKEY_TPB) smf_key_kernel(int n, const double *
     for (int t7 = 0; t7 < 7; t7++) {
       const double li = lam[TI[t7]], lj = lam[TJ[t7]], lk = lam[TL[t7]];
       const double lo = fmin(li, fmin(lj, lk)), hi = fmax(li, fmax(lj, lk)), mid = li + lj + lk - lo - hi;
-      const bool cl = KIND == EXP ? (hi - lo <= 1.0)
+      const bool cl = KIND == EXP ? (mid - lo <= (double)tau) & (hi - mid <= (double)tau)
                                   : (mid > 0) & (mid - lo <= (double)tau * mid) & (hi - mid <= (double)tau * mid);
       key |= cl ? 1u << t7 : 0u;
     }

@@ -23,7 +23,7 @@ namespace mf {
 // (31 0.5^30 < 3e-8): outside the cluster the difference formula (D_jk - D_ij) / d subtracts first divided
 // differences that differ by (1 - alpha) d / l_j of their size, so their FP32 rounding is amplified by about
 // 1 / ((1 - alpha) tau); at tau = 0.25 that put H of pow 0.7 at 1.3e-6 .. 1.7e-6 of its maximum on near-double
-// eigenvalues.  The FP64 form keeps the reference's tau = 0.25 and 30 terms.
+// eigenvalues.  (The FP64 form, whose difference formula loses less, takes the series only within 2^-6.)
 constexpr int DD2_TERMS_F = 16, DD2_TERMS_F_POW = 30;
 constexpr double DD2_TAU_F_POW = 0.5;
 
@@ -460,7 +460,9 @@ inline void smf_coef_f(int kind, double al, SmfCoefF &C) {
   C.zp1 = (float)D.zp1;
   C.z2 = (float)D.z2;
   const bool pw = kind == POW || kind == SQRT;
-  C.tau = (float)(pw ? (3.0 / al < DD2_TAU_F_POW ? 3.0 / al : DD2_TAU_F_POW) : D.tau);
+  // (the FP32 form keeps its own cluster radius: 0.25 for exp / log (exp: the spread of the three points <= 1), 0.5
+  // or 3 / al for powers, with its own term count)
+  C.tau = (float)(pw ? (3.0 / al < DD2_TAU_F_POW ? 3.0 / al : DD2_TAU_F_POW) : DD2_TAU);
   for (int k = 0; k < DD2_TERMS; k++) C.c2[k] = (float)D.c2[k];
 }
 

@@ -135,3 +135,47 @@ def test_autotune_roundtrip(tmp_path, monkeypatch):
                                                           {"ctas_per_sm": 2, "longest_first": 1}])
     assert best in ({"ctas_per_sm": 1, "longest_first": 1}, {"ctas_per_sm": 2, "longest_first": 1})
     assert autotune.apply(reqs) == best
+
+
+def test_batched_c3_mix_against_oracle():
+    """a C3-style mix in one persistent launch held directly against the FP64 oracle: every family, kind and order,
+    FP64 and FP32 requests, and gmf log / pow requests of >= 2048 matrices that the launch orders by spectral class
+    first; FP64 within 1e-12 per call with NaN exactly where the oracle has NaN, FP32 per matrix within the bounds of
+    tests/test_mixed_gpu.py (1e-6; smf H 2.5e-6) against the oracle on the FP32 values"""
+    import torch
+
+    from matfun_gb300 import batched
+    from matfun_gb300 import workloads as w
+    from tests import oracle_lib as ol
+    from tests.helpers import maxrel, maxrel_rows_fp32
+    rng = np.random.default_rng(23)
+    reqs, meta = [], []
+    plan = [("gmf", "log", 2, False, 4000), ("gmf", "pow", 2, False, 2500), ("gmf", "log", 2, True, 3000),
+            ("gmf", "sqrt", 1, True, 2200), ("gmf", "exp", 2, False, 900)]
+    for i in range(15):
+        plan.append((["smf_voigt", "smf", "gmf"][i % 3], ["exp", "log", "sqrt", "pow"][i % 4], i % 3, bool(i % 2),
+                     int(rng.integers(1, 1500))))
+    for fam, kind, order, f32, n in plan:
+        x = w.c1_gmf_groups(max(n, 4), seed=n)[:n] if fam == "gmf" else \
+            w.c0_smf_spd(n, seed=n, as_voigt=fam == "smf_voigt")
+        t = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+        t = t.float() if f32 else t
+        alpha = 0.3 if kind == "pow" else None
+        reqs.append(batched.request(fam, kind, t, order=order, alpha=alpha))
+        meta.append((fam, kind, order, f32, alpha))
+    batched.run(reqs)
+    torch.cuda.synchronize()
+    cfam = {"smf_voigt": ("smf_eval", 6), "smf": ("smf_eval_matrix", 9), "gmf": ("gmf_eval", 9)}
+    for r, (fam, kind, order, f32, alpha) in zip(reqs, meta):
+        fn, nf = cfam[fam]
+        X = r.x.double().cpu().numpy().reshape(r.n, -1)
+        ref = ol.call(ol.oracle(), fn, ol.KINDS[kind], alpha or 0.0, X, order, nf)[1:order + 2]
+        for name, got, exp in zip("FJH", (r.F, r.J, r.H), ref):
+            g = got.double().cpu().numpy()
+            assert np.array_equal(np.isnan(g), np.isnan(exp)), (fam, kind, order, f32, name)
+            if f32:
+                bound = 2.5e-6 if (fam != "gmf" and name == "H") else 1e-6
+                e = float(np.max(maxrel_rows_fp32(g, exp), initial=0.0))
+            else:
+                bound, e = 1e-12, maxrel(g, exp)
+            assert e <= bound, (fam, kind, order, f32, name, e)

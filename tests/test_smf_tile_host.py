@@ -192,7 +192,8 @@ def test_tile_random_spectra(lib, kind, alpha, name, f32):
     [1e-3, 1e3], near-double and near-triple clusters at relative gaps 1e-12 .. 1e-3, small strains 1e-6 .. 1e-1.
     Bound 2e-6; exp 1e-5, over matrices whose largest eigenvalue is below 80 (e^lambda within FP32's range; its FP32
     eigenvalues carry |lambda| 6e-8 absolute, 5e-6 relative in e^lambda at 80).  The FP64 tile on the same matrices
-    (unrounded) is held to the parity bound 1e-12 per matrix (measured 8.5e-16 on 60 000 per kind)"""
+    (unrounded) is held to the parity bound 1e-12 per matrix (measured 5.2e-14 on 60 000 per kind: its cluster
+    series covers 2^-6 of the middle point, the difference formula the rest)"""
     from tests.helpers import maxrel_rows
     rng = np.random.default_rng(2026)
 
