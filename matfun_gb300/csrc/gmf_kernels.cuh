@@ -37,7 +37,8 @@ namespace mf {
 
 constexpr int GMF_TPB = 128;
 constexpr int GMF_WARPS = GMF_TPB / 32;
-constexpr int GMF_MIN_CTAS = 2;  // CTAs per SM the register allocation of gmf_kernel is bounded for
+constexpr int GMF_MIN_CTAS = 3;  // CTAs per SM the register allocation of gmf_kernel is bounded for (3: 168 registers,
+                                 // C1 gmf log order 2 12.3 ms against 13.3 ms at 2 CTAs with 255 registers)
 constexpr int GMF_REC = 36;  // r1 (9), r2 (9), D2' (6), D3' (10), sc1, sc2
 
 // shared memory layout of one CTA (doubles unless noted)
