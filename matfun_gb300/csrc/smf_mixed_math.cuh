@@ -321,10 +321,30 @@ MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E) {
     E.xd[i] = {xd.hi * sig, xd.lo * sig};
   }
   E.m = m.hi * sig;
+  // The FP32 cross products leave v a few ulp off its eigenvector, towards the pair's plane; H carries six factors of
+  // it (an error of 2.5 ulp there put H of condition-1e6 matrices at 1.2e-6 of its maximum).  First-order correction
+  // of that coupling: c_i = v^T (A - mu I) r_i in float-float is (the angle of v towards r_i) (th_v - th_i), so
+  // v += sum_i r_i c_i / (th_v - th_i) and r_i -= v c_i / (th_v - th_i), taken where the angle is below 2^-10 (v
+  // and the pair then well apart; near a triple eigenvalue the split does not matter).  The pair's own rotation is
+  // accurate relative to its gap already.
+  {
+    const ffl c1 = bil_ff<LO>(dg, o, v, r1), c2 = bil_ff<LO>(dg, o, v, r2);
+    const float t1 = (c1.hi + c1.lo) / ((th[0].hi - th[1].hi) + (th[0].lo - th[1].lo));
+    const float t2 = (c2.hi + c2.lo) / ((th[0].hi - th[2].hi) + (th[0].lo - th[2].lo));
+    const float a1 = fabsf(t1) <= 0x1p-10f ? t1 : 0.f, a2 = fabsf(t2) <= 0x1p-10f ? t2 : 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const float vi = v[i];
+      v[i] = fmaf(r1[i], a1, fmaf(r2[i], a2, vi));
+      r1[i] = fmaf(-vi, a1, r1[i]);
+      r2[i] = fmaf(-vi, a2, r2[i]);
+    }
+  }
   // Newton-Schulz step with the float-float Gram matrix
+  const ffl nv2 = dot_ff(v, v), n12 = dot_ff(r1, r1), n22 = dot_ff(r2, r2);
   const ffl g01 = dot_ff(v, r1), g02 = dot_ff(v, r2), g12 = dot_ff(r1, r2);
-  float e00 = 0.5f * ((nv.hi - 1.f) + nv.lo), e11 = 0.5f * ((n1.hi - 1.f) + n1.lo);
-  float e22 = 0.5f * ((n2.hi - 1.f) + n2.lo);
+  float e00 = 0.5f * ((nv2.hi - 1.f) + nv2.lo), e11 = 0.5f * ((n12.hi - 1.f) + n12.lo);
+  float e22 = 0.5f * ((n22.hi - 1.f) + n22.lo);
   float e01 = 0.5f * (g01.hi + g01.lo), e02 = 0.5f * (g02.hi + g02.lo), e12 = 0.5f * (g12.hi + g12.lo);
   float nanv = __int_as_float(0x7FC00000);
 #pragma unroll
