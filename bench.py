@@ -51,49 +51,49 @@ def io_bytes(fam, order, elem=8):
 # pipe: FFMA, FADD, FMUL) of each configuration's kernels, from the ncu counters
 # smsp__sass_thread_inst_executed_op_{d,f}{fma,add,mul}_pred_on.sum of `python bench.py --count-pass` divided by the
 # matrices of each launch (profiles/pipe_counts_all_configs.md).  They turn the measured time of a configuration into
-# its FP64 / FP32 pipe fraction.  None: not counted.
+# its FP64 / FP32 pipe fraction.  None: the kernels execute no instruction of that pipe.
 PIPE_FLOPS = {
-    "gmf/log/2/f64": {"fp64": 6739, "fp32": 12399},
-    "gmf/exp/2/f64": {"fp64": 5524, "fp32": 6257},
-    "gmf/sqrt/2/f64": {"fp64": 8719, "fp32": 12237},
-    "gmf/log/2/f32": {"fp64": 2507, "fp32": 40174},
-    "gmf/exp/2/f32": {"fp64": 3143, "fp32": 8193},
-    "gmf/sqrt/2/f32": {"fp64": 4517, "fp32": 39626},
-    "gmf/pow0.3/2/f32": {"fp64": 5178, "fp32": 39843},
-    "gmf/log/tangent/f64": {"fp64": 9034, "fp32": 12450},
-    "smf/log/2/f64/c0": {"fp64": 3009, "fp32": 66},
-    "smf/exp/0/f32": {"fp64": None, "fp32": 1517},
-    "smf/exp/0/f64": {"fp64": 709, "fp32": 14},
-    "smf/exp/1/f32": {"fp64": None, "fp32": 1950},
-    "smf/exp/1/f64": {"fp64": 1109, "fp32": 20},
-    "smf/exp/2/f32": {"fp64": None, "fp32": 3334},
-    "smf/exp/2/f64": {"fp64": 2868, "fp32": 208},
-    "smf/log/0/f32": {"fp64": None, "fp32": 1777},
-    "smf/log/0/f64": {"fp64": 998, "fp32": 22},
-    "smf/log/1/f32": {"fp64": None, "fp32": 2312},
-    "smf/log/1/f64": {"fp64": 1598, "fp32": 41},
-    "smf/log/2/f32": {"fp64": None, "fp32": 3622},
-    "smf/log/2/f64": {"fp64": 3210, "fp32": 242},
-    "smf/sqrt/0/f32": {"fp64": None, "fp32": 1505},
-    "smf/sqrt/0/f64": {"fp64": 661, "fp32": 14},
-    "smf/sqrt/1/f32": {"fp64": None, "fp32": 1854},
-    "smf/sqrt/1/f64": {"fp64": 1004, "fp32": 14},
-    "smf/sqrt/2/f32": {"fp64": None, "fp32": 3413},
-    "smf/sqrt/2/f64": {"fp64": 2640, "fp32": 226},
-    "smf/pow/0/f32": {"fp64": None, "fp32": 1664},
-    "smf/pow/0/f64": {"fp64": 986, "fp32": 14},
-    "smf/pow/1/f32": {"fp64": None, "fp32": 2433},
-    "smf/pow/1/f64": {"fp64": 2004, "fp32": 31},
-    "smf/pow/2/f32": {"fp64": None, "fp32": 3928},
-    "smf/pow/2/f64": {"fp64": 3641, "fp32": 242},
-    "smf/log/vjp/f64": {"fp64": 1518, "fp32": 49},
-    "smf/log/hvp/f64": {"fp64": 2306, "fp32": 66},
-    "smf/log/vjp/f32": {"fp64": None, "fp32": 2262},
-    "smf/log/hvp/f32": {"fp64": None, "fp32": 2790},
-    "gmf/pow0.3/vjp/f64": {"fp64": 5233, "fp32": 10693},
-    "gmf/pow0.3/hvp/f64": {"fp64": 10403, "fp32": 24383},
-    "gmf/pow0.3/vjp/f32": {"fp64": 3927, "fp32": 29029},
-    "gmf/pow0.3/hvp/f32": {"fp64": 5826, "fp32": 70819},
+    "gmf/log/2/f64": {"fp64": 5586, "fp32": 12353},
+    "gmf/exp/2/f64": {"fp64": 4911, "fp32": 6229},
+    "gmf/sqrt/2/f64": {"fp64": 7872, "fp32": 12200},
+    "gmf/log/2/f32": {"fp64": 1558, "fp32": 41877},
+    "gmf/exp/2/f32": {"fp64": 2640, "fp32": 9914},
+    "gmf/sqrt/2/f32": {"fp64": 3820, "fp32": 41338},
+    "gmf/pow0.3/2/f32": {"fp64": 4537, "fp32": 41555},
+    "gmf/log/tangent/f64": {"fp64": 7809, "fp32": 12401},
+    "smf/log/2/f64/c0": {"fp64": 3000, "fp32": 90},
+    "smf/exp/0/f32": {"fp64": None, "fp32": 1969},
+    "smf/exp/0/f64": {"fp64": 701, "fp32": 14},
+    "smf/exp/1/f32": {"fp64": None, "fp32": 2402},
+    "smf/exp/1/f64": {"fp64": 1104, "fp32": 20},
+    "smf/exp/2/f32": {"fp64": None, "fp32": 3786},
+    "smf/exp/2/f64": {"fp64": 2345, "fp32": 214},
+    "smf/log/0/f32": {"fp64": None, "fp32": 2229},
+    "smf/log/0/f64": {"fp64": 989, "fp32": 22},
+    "smf/log/1/f32": {"fp64": None, "fp32": 2764},
+    "smf/log/1/f64": {"fp64": 1589, "fp32": 41},
+    "smf/log/2/f32": {"fp64": None, "fp32": 4074},
+    "smf/log/2/f64": {"fp64": 3208, "fp32": 263},
+    "smf/sqrt/0/f32": {"fp64": None, "fp32": 1957},
+    "smf/sqrt/0/f64": {"fp64": 653, "fp32": 14},
+    "smf/sqrt/1/f32": {"fp64": None, "fp32": 2306},
+    "smf/sqrt/1/f64": {"fp64": 999, "fp32": 14},
+    "smf/sqrt/2/f32": {"fp64": None, "fp32": 3865},
+    "smf/sqrt/2/f64": {"fp64": 2720, "fp32": 256},
+    "smf/pow/0/f32": {"fp64": None, "fp32": 2116},
+    "smf/pow/0/f64": {"fp64": 981, "fp32": 14},
+    "smf/pow/1/f32": {"fp64": None, "fp32": 2885},
+    "smf/pow/1/f64": {"fp64": 1998, "fp32": 31},
+    "smf/pow/2/f32": {"fp64": None, "fp32": 4380},
+    "smf/pow/2/f64": {"fp64": 3720, "fp32": 273},
+    "smf/log/vjp/f64": {"fp64": 1509, "fp32": 49},
+    "smf/log/hvp/f64": {"fp64": 2299, "fp32": 90},
+    "smf/log/vjp/f32": {"fp64": None, "fp32": 2726},
+    "smf/log/hvp/f32": {"fp64": None, "fp32": 3254},
+    "gmf/pow0.3/vjp/f64": {"fp64": 4287, "fp32": 10652},
+    "gmf/pow0.3/hvp/f64": {"fp64": 9066, "fp32": 24339},
+    "gmf/pow0.3/vjp/f32": {"fp64": 3241, "fp32": 29333},
+    "gmf/pow0.3/hvp/f32": {"fp64": 5012, "fp32": 72434},
 }
 
 
@@ -699,13 +699,17 @@ def batched_c3(lib, args, dev, pk):
            (0, 1): lib.smf_cuda_eval_f32, (1, 1): lib.smf_cuda_eval_matrix_f32, (2, 1): lib.gmf_cuda_eval_f32}
     p = lambda t: None if t is None else t.data_ptr()
 
-    def singles():
+    def singles(fams=(0, 1, 2)):
         for r in reqs:
             c = r.c
-            fns[(c.family, c.dtype)](c.kind, c.alpha, c.n, r.x.data_ptr(), p(r.F), p(r.J), p(r.H), None)
+            if c.family in fams:
+                fns[(c.family, c.dtype)](c.kind, c.alpha, c.n, r.x.data_ptr(), p(r.F), p(r.J), p(r.H), None)
 
     t_graph = timed_ms(g.replay, args.c3_steps, 1)
     t_single = timed_ms(singles, args.c3_steps, 1)
+    # where the single launches spend their time: the general family's requests alone, the symmetric ones alone
+    t_single_gmf = timed_ms(lambda: singles((2,)), args.c3_steps, 1)
+    t_single_smf = timed_ms(lambda: singles((0, 1)), args.c3_steps, 1)
     # the CPU path: each request's FP64 entry point on a sample of its inputs, its time scaled to the request's size
     cpu_s, sampled = 0.0, 0
     cfam = {"smf_voigt": "smf_eval", "smf": "smf_eval_matrix", "gmf": "gmf_eval"}
@@ -725,6 +729,9 @@ def batched_c3(lib, args, dev, pk):
             "batched_graph_matrices_per_s": total / (t_graph * 1e-3), "batched_ms": t_graph,
             "single_launches_matrices_per_s": total / (t_single * 1e-3), "single_ms": t_single,
             "speedup": t_single / t_graph, "autotuned": choice,
+            "tile_matrices": {"gmf": 128, "smf": int(choice.get("smf_tile", 128))},
+            "single_ms_by_family": {"gmf": t_single_gmf, "smf": t_single_smf},
+            "gmf_matrices": int(sum(r.n for r, m in zip(reqs, meta) if m[0] == "gmf")),
             "autotune_ms": {k: round(v, 3) for k, v in tune_ms.items()},
             "roofline": roofline(total, t_graph, nbytes / total, "batched/c3", pk),
             "cpu_baseline": {"value": total / cpu_s, "unit": "matrices/s", "cores": cores, "kind": cpu_lib()[1],
@@ -858,11 +865,11 @@ def run_ours(args, rank, world, local):
 
 
 # DRAM bytes per matrix of the ordered gmf_kernel<LOG, 2> launch from one ncu capture at n = 262144 on the same
-# workload (101.4 MB read + 1752.0 MB written for 259 584 matrices; the algorithmic bytes are 6624 per matrix, the
-# extra reads are the partial sectors at the ends of the rows the ordered launch scatters)
-NCU_DRAM_BYTES_PER_MATRIX = (101.44e6 + 1752.03e6) / 259584
+# workload (132.8 MB read + 1915.7 MB written for 259 584 matrices; the algorithmic bytes are 6624 per matrix, the
+# extra bytes are the partial sectors at the ends of the rows the ordered launch scatters)
+NCU_DRAM_BYTES_PER_MATRIX = (132.77e6 + 1915.68e6) / 259584
 NCU_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the ordered gmf_kernel<LOG,2> launch at "
-                      "n=262144 (1853.5 MB), scaled by n (profiles/gmf_kernel_log_o2_c1.md)")
+                      "n=262144 (2048.4 MB), scaled by n (profiles/gmf_kernel_log_o2_c1.md)")
 
 
 def launches_per_call(kind, n):

@@ -132,6 +132,11 @@ int matfun_cuda_batched_noalloc(const mf_request *requests, int count, void *str
  * requests are laid out longest first (1) or as given (0).  Returns 0 or -1. */
 int matfun_cuda_batched_tune(int ctas_per_sm, int longest_first);
 
+/* Matrices per tile of the symmetric-family requests of later batched tables: 128 (default) or 64; the general family
+ * always takes 128.  A 64-matrix tile needs half the shared memory of a 128-matrix one, its per-matrix phase runs on
+ * half of the CTA's 128 threads.  Returns 0 or -1. */
+int matfun_cuda_batched_tune_tiles(int smf_tile);
+
 /* Host-buffer forms: the reference's CPU entry points smf_eval, smf_eval_matrix and gmf_eval
  * (c/include/matfun/matfun.h:28-41; implementation c/src/matfun.cc:87-97) evaluated on the current GPU: HOST arrays
  * in and out, synchronous, same return codes as the CPU library (0, -1 invalid arguments, -3 when a matrix given to

@@ -1,6 +1,8 @@
-"""Autotuner of the batched persistent launch: CTAs per SM (1..4) and the request layout (as given / longest work
-first), chosen by timing matfun_cuda_batched_run on a request mix, and kept in a JSON cache keyed by the GPU name and
-the mix.  `apply()` sets the cached choice (matfun_cuda_batched_tune); `tune(reqs)` measures and stores it.
+"""Autotuner of the batched persistent launch: CTAs per SM (1..4), the request layout (as given / longest work
+first) and the tile geometry of the symmetric family (64 or 128 matrices per tile of 128 threads; the general family's
+tile is 128), chosen by timing matfun_cuda_batched_run on a request mix, and kept in a JSON cache keyed by the GPU
+name and the mix.  `apply()` sets the cached choice (matfun_cuda_batched_tune, matfun_cuda_batched_tune_tiles);
+`tune(reqs)` measures and stores it.
 
 The cache lives in $MATFUN_AUTOTUNE_CACHE or ~/.cache/matfun_gb300/autotune.json.
 """
@@ -12,7 +14,12 @@ import torch
 from . import batched
 from ._lib import load
 
-DEFAULT = {"ctas_per_sm": 2, "longest_first": 1}
+DEFAULT = {"ctas_per_sm": 2, "longest_first": 1, "smf_tile": 128}
+
+
+def _set(lib, choice):
+    lib.matfun_cuda_batched_tune(int(choice["ctas_per_sm"]), int(choice["longest_first"]))
+    lib.matfun_cuda_batched_tune_tiles(int(choice.get("smf_tile", 128)))
 
 
 def cache_path():
@@ -40,18 +47,19 @@ def apply(reqs=None):
     if choice is None:
         name = torch.cuda.get_device_name()
         choice = next((v for k, v in c.items() if k.startswith(name + "|")), DEFAULT)
-    load().matfun_cuda_batched_tune(int(choice["ctas_per_sm"]), int(choice["longest_first"]))
+    _set(load(), choice)
     return choice
 
 
 def tune(reqs, reps=3, candidates=None, save=True):
     """time every candidate on the mix, keep the fastest (and store it); returns (choice, timings in ms)"""
     lib = load()
-    cands = candidates or [{"ctas_per_sm": c, "longest_first": lf} for c in (1, 2, 3, 4) for lf in (1, 0)]
+    cands = candidates or [{"ctas_per_sm": c, "longest_first": lf, "smf_tile": t}
+                           for c in (1, 2, 3, 4) for lf in (1, 0) for t in (128, 64)]
     times = {}
     for cand in cands:
-        lib.matfun_cuda_batched_tune(cand["ctas_per_sm"], cand["longest_first"])
-        plan = batched.Plan(reqs)  # the layout is fixed when the table is built
+        _set(lib, cand)
+        plan = batched.Plan(reqs)  # the layout and the tiles are fixed when the table is built
         plan.run()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -63,7 +71,7 @@ def tune(reqs, reps=3, candidates=None, save=True):
         times[json.dumps(cand, sort_keys=True)] = e0.elapsed_time(e1) / reps
         del plan
     best = json.loads(min(times, key=times.get))
-    lib.matfun_cuda_batched_tune(best["ctas_per_sm"], best["longest_first"])
+    _set(lib, best)
     if save:
         c = _load()
         c[_key(reqs)] = best

@@ -1,11 +1,12 @@
 // batched.cu -- many requests of uneven size and mixed family / kind / order / precision in one launch.
 //
-// The host cuts every request into tiles of 128 matrices and writes a table (requests, their coefficient blocks,
-// the prefix sum of their tile counts) into device memory.  One persistent kernel (grid = SMs x CTAs per SM) then
-// pulls tiles from a global atomic cursor until all are taken; each tile runs the same tile routine as the
-// standalone kernel of its request (smf FP64 / mixed FP32 in either layout, gmf FP64 / mixed FP32).  There is no
-// waiting between CTAs: a CTA only increments the cursor and stops when it passes the tile count, so no wait can
-// hang.
+// The host cuts every request into tiles (gmf: 128 matrices; smf: 64 or 128, matfun_cuda_batched_tune_tiles) and
+// writes a table (requests, their coefficient blocks, the prefix sum of their tile counts) into device memory.  One
+// persistent kernel (grid = SMs x CTAs per SM) then pulls tiles from a global atomic cursor until all are taken; each
+// tile runs the same tile routine as the standalone kernel of its request (smf FP64 / mixed FP32 in either layout,
+// gmf FP64 / mixed FP32), by the CTA's 128 threads.  The launch's dynamic shared memory is that of its largest tile.
+// There is no waiting between CTAs: a CTA only increments the cursor and stops when it passes the tile count, so no
+// wait can hang.
 //
 // Two ways to run it:
 //   matfun_cuda_batched(requests, count, stream)          table in a per-device cached buffer, uploaded on `stream`
@@ -15,8 +16,9 @@
 // into an order region after the table (in the cached buffer, or in the plan's allocation).
 //   matfun_cuda_batched_plan / _run / _free                 table uploaded once; _run only clears the cursor and
 //                                                           launches, so it can be captured in a CUDA graph
-// The CTAs per SM and the order in which requests are laid out (as given, or longest tile work first) come from
-// matfun_cuda_batched_tune (set by the autotuner of matfun_gb300/autotune.py).
+// The CTAs per SM, the order in which requests are laid out (as given, or longest tile work first) and the smf tile
+// size come from matfun_cuda_batched_tune / _tune_tiles (set by the autotuner of matfun_gb300/autotune.py); a plan
+// keeps the layout and tile size in force when it was made.
 #include <algorithm>
 #include <climits>
 #include <cstddef>
@@ -60,10 +62,18 @@ namespace {
 __device__ void run_tile(const DevReq &R, long long base, int cnt, const unsigned char *coef, unsigned char *smem) {
   if (R.family == 2) {
     if (R.dtype == 0) { MF_GMF_KIND(bt_gmf) } else { MF_GMF_KIND(bt_gmf32) }
-  } else if (R.family == 1) {
-    if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, m) } else { MF_SMF_KIND(bt_smf32, m) }
+  } else if (R.tile == BT_TPB) {
+    if (R.family == 1) {
+      if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, m) } else { MF_SMF_KIND(bt_smf32, m) }
+    } else {
+      if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, v) } else { MF_SMF_KIND(bt_smf32, v) }
+    }
   } else {
-    if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, v) } else { MF_SMF_KIND(bt_smf32, v) }
+    if (R.family == 1) {
+      if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, m64) } else { MF_SMF_KIND(bt_smf32, m64) }
+    } else {
+      if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, v64) } else { MF_SMF_KIND(bt_smf32, v64) }
+    }
   }
 }
 
@@ -87,14 +97,35 @@ __global__ void __launch_bounds__(BT_TPB) batched_kernel(const DevReq *__restric
       else hi = mid;
     }
     const DevReq R = reqs[lo];
-    const long long base = (t - tile_start[lo]) * BT_TPB;
-    const int cnt = (int)min((long long)BT_TPB, R.n - base);
+    const long long base = (t - tile_start[lo]) * R.tile;
+    const int cnt = (int)min((long long)R.tile, R.n - base);
     run_tile(R, base, cnt, coefs + R.coef_off, smem);
     __syncthreads();  // the tile's shared memory is reused by the next tile
   }
 }
 
-constexpr size_t smem_bytes() {
+// the dynamic shared memory of one request's tiles
+size_t tile_smem(int family, int order, int dtype, int tile) {
+  const bool mat = family == 1;
+  if (family == 2) return sizeof(GmfSmem);
+  if (tile == BT_TPB) {
+    if (dtype == 0) return order == 2 ? (mat ? sizeof(SmfS<2, true>) : sizeof(SmfS<2, false>))
+                                      : order == 1 ? (mat ? sizeof(SmfS<1, true>) : sizeof(SmfS<1, false>))
+                                                   : (mat ? sizeof(SmfS<0, true>) : sizeof(SmfS<0, false>));
+    return order == 2 ? (mat ? sizeof(SmfxS<2, true>) : sizeof(SmfxS<2, false>))
+                      : order == 1 ? (mat ? sizeof(SmfxS<1, true>) : sizeof(SmfxS<1, false>))
+                                   : (mat ? sizeof(SmfxS<0, true>) : sizeof(SmfxS<0, false>));
+  }
+  if (dtype == 0) return order == 2 ? (mat ? sizeof(SmfS<2, true, 64>) : sizeof(SmfS<2, false, 64>))
+                                    : order == 1 ? (mat ? sizeof(SmfS<1, true, 64>) : sizeof(SmfS<1, false, 64>))
+                                                 : (mat ? sizeof(SmfS<0, true, 64>) : sizeof(SmfS<0, false, 64>));
+  return order == 2 ? (mat ? sizeof(SmfxS<2, true, 64>) : sizeof(SmfxS<2, false, 64>))
+                    : order == 1 ? (mat ? sizeof(SmfxS<1, true, 64>) : sizeof(SmfxS<1, false, 64>))
+                                 : (mat ? sizeof(SmfxS<0, true, 64>) : sizeof(SmfxS<0, false, 64>));
+}
+
+// the largest dynamic shared memory of any tile (the kernel's attribute is raised to it once per device)
+constexpr size_t smem_max() {
   size_t m = sizeof(GmfSmem);
   m = std::max(m, sizeof(SmfS<2, true>));
   m = std::max(m, sizeof(SmfS<2, false>));
@@ -106,6 +137,7 @@ constexpr size_t smem_bytes() {
 struct Tuning {
   int ctas_per_sm = 2;
   int longest_first = 1;
+  int smf_tile = BT_TPB;  // matrices per smf tile: 64 or 128
 };
 Tuning g_tune;
 
@@ -126,6 +158,7 @@ struct Table {                  // a validated request list laid out for the dev
   int count = 0;
   std::vector<Ord> ords;
   size_t ord_bytes = 0;
+  size_t smem = 0;  // dynamic shared memory of the launch: the largest of its requests' tiles
 };
 
 size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -161,7 +194,7 @@ int build_table(const mf_request *req, int count, Table &T) {
     if (kind != SMF_POW) al = kind == SMF_SQRT ? 0.5 : 0.0;
     Item it;
     it.d = DevReq{r.family, kind, r.order, r.dtype, al, (long long)r.n, r.x, r.F, r.order >= 1 ? r.J : nullptr,
-                  r.order >= 2 ? r.H : nullptr, 0, nullptr};
+                  r.order >= 2 ? r.H : nullptr, 0, nullptr, r.family == 2 ? BT_TPB : g_tune.smf_tile};
     if (r.family == 2) {
       GmfCoef C;
       gmf_coef(kind, al, r.order, C);
@@ -178,7 +211,8 @@ int build_table(const mf_request *req, int count, Table &T) {
       it.coef.resize(sizeof C);
       std::memcpy(it.coef.data(), &C, sizeof C);
     }
-    it.tiles = (r.n + BT_TPB - 1) / BT_TPB;
+    it.tiles = (r.n + it.d.tile - 1) / it.d.tile;
+    T.smem = std::max(T.smem, tile_smem(r.family, r.order, r.dtype, it.d.tile));
     // relative work per matrix (measured orders of magnitude): gmf order 2 >> smf order 2 >> first orders
     const double per = (r.family == 2 ? 4.0 : 1.0) * (r.order == 2 ? 4.0 : (r.order == 1 ? 1.5 : 1.0)) *
                        (r.dtype == 1 ? (r.family == 2 ? 0.8 : 0.3) : 1.0);
@@ -254,7 +288,7 @@ cudaError_t launch_orders(const Table &T, unsigned char *ord_base, cudaStream_t 
 
 cudaError_t prepare_kernel() {
   static std::atomic<unsigned long long> done{0};  // one bit per device
-  return smem_limit_per_device(batched_kernel, (int)smem_bytes(), done);
+  return smem_limit_per_device(batched_kernel, (int)smem_max(), done);
 }
 
 cudaError_t launch_table(const unsigned char *dev_table, const Table &T, unsigned long long *cursor,
@@ -268,9 +302,9 @@ cudaError_t launch_table(const unsigned char *dev_table, const Table &T, unsigne
   e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   const unsigned grid = (unsigned)(sms * std::max(1, g_tune.ctas_per_sm));
-  batched_kernel<<<grid, BT_TPB, smem_bytes(), st>>>((const DevReq *)dev_table, T.count,
-                                                     (const long long *)(dev_table + T.off_tiles), cursor,
-                                                     dev_table + T.off_coef);
+  batched_kernel<<<grid, BT_TPB, T.smem, st>>>((const DevReq *)dev_table, T.count,
+                                               (const long long *)(dev_table + T.off_tiles), cursor,
+                                               dev_table + T.off_coef);
   return cudaGetLastError();
 }
 
@@ -379,6 +413,12 @@ extern "C" int matfun_cuda_batched_tune(int ctas_per_sm, int longest_first) {
   if (ctas_per_sm < 1 || ctas_per_sm > 8 || (longest_first != 0 && longest_first != 1)) return -1;
   g_tune.ctas_per_sm = ctas_per_sm;
   g_tune.longest_first = longest_first;
+  return 0;
+}
+
+extern "C" int matfun_cuda_batched_tune_tiles(int smf_tile) {
+  if (smf_tile != 64 && smf_tile != BT_TPB) return -1;
+  g_tune.smf_tile = smf_tile;
   return 0;
 }
 

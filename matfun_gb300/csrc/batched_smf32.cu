@@ -2,12 +2,14 @@
 #include "batched_tiles.cuh"
 
 namespace mf {
-#define MF_DEF(K, O, M, SUF)                                                                                       \
-  __device__ __noinline__ void bt_smf32_##K##_##O##_##SUF MF_BT_SIG {                                              \
-    smf_mixed_tile<K, O, M, BT_TPB>(base, cnt, (const float *)R.x, (float *)R.F, (float *)R.J, (float *)R.H,       \
-                                    *(const SmfCoefF *)coef, *(SmfxS<O, M> *)smem);                               \
+// (SUF v / m: 128 matrices per tile; v64 / m64: 64 matrices per tile; both by the 128 threads of the CTA)
+#define MF_DEF(K, O, M, SUF, TM)                                                                                 \
+  __device__ __noinline__ void bt_smf32_##K##_##O##_##SUF MF_BT_SIG {                                           \
+    smf_mixed_tile<K, O, M, TM, BT_TPB>(base, cnt, (const float *)R.x, (float *)R.F, (float *)R.J, (float *)R.H,          \
+                                  *(const SmfCoefF *)coef, *(SmfxS<O, M, TM> *)smem);                       \
   }
-#define MF_DEF_K(K) MF_DEF(K, 0, false, v) MF_DEF(K, 1, false, v) MF_DEF(K, 2, false, v) \
-                    MF_DEF(K, 0, true, m) MF_DEF(K, 1, true, m) MF_DEF(K, 2, true, m)
+#define MF_DEF_S(K, O) MF_DEF(K, O, false, v, BT_TPB) MF_DEF(K, O, true, m, BT_TPB) \
+                       MF_DEF(K, O, false, v64, 64) MF_DEF(K, O, true, m64, 64)
+#define MF_DEF_K(K) MF_DEF_S(K, 0) MF_DEF_S(K, 1) MF_DEF_S(K, 2)
 MF_DEF_K(0) MF_DEF_K(1) MF_DEF_K(2) MF_DEF_K(3)
 }  // namespace mf

@@ -19,14 +19,16 @@ struct SmfxTileSmem {
   float sG[ORDER >= 2 ? TPB * 56 : 1];
 };
 
-template <int KIND, int ORDER, bool MAT, int SMFX_TPB>
+// (cnt <= SMFX_TPB matrices by a CTA of NT >= SMFX_TPB threads: phase A by the first cnt threads, the cooperative
+// loads and stores by all NT)
+template <int KIND, int ORDER, bool MAT, int SMFX_TPB, int NT = SMFX_TPB>
 MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, float *__restrict__ F,
                          float *__restrict__ J, float *__restrict__ H, const SmfCoefF &C,
                          SmfxTileSmem<ORDER, MAT, SMFX_TPB> &TS) {
   constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6, NJ = NF * NF, NH = NJ * NF;
   float *sX = TS.sX, *sF = TS.sF, *sK = TS.sK, *sG = TS.sG;
   const int tid = threadIdx.x;
-  for (int e = tid; e < cnt * NIN; e += SMFX_TPB) sX[e] = x[base * NIN + e];
+  for (int e = tid; e < cnt * NIN; e += NT) sX[e] = x[base * NIN + e];
   __syncthreads();
   if (tid < cnt) {
     const float *xi = sX + tid * NIN;
@@ -142,14 +144,14 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
     }
   }
   __syncthreads();
-  for (int e = tid; e < cnt * NF; e += SMFX_TPB) F[base * NF + e] = sF[e];
+  for (int e = tid; e < cnt * NF; e += NT) F[base * NF + e] = sF[e];
   if (ORDER >= 1) {
-    constexpr int KJ = (NJ + SMFX_TPB - 1) / SMFX_TPB;
+    constexpr int KJ = (NJ + NT - 1) / NT;
     int jidx[KJ];
     float jw[KJ];  // layout weight 2^ex (an FP32 multiplication by a power of two is exact)
 #pragma unroll
     for (int k = 0; k < KJ; k++) {
-      const int w = min(tid + SMFX_TPB * k, NJ - 1);
+      const int w = min(tid + NT * k, NJ - 1);
       int I, p, ex;
       if (MAT) {
         I = midx(w / 9); p = midx(w % 9);
@@ -166,16 +168,16 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
       const float *s = sK + mi * 21;
 #pragma unroll
       for (int k = 0; k < KJ; k++)
-        if (tid + SMFX_TPB * k < NJ) o[tid + SMFX_TPB * k] = s[jidx[k]] * jw[k];
+        if (tid + NT * k < NJ) o[tid + NT * k] = s[jidx[k]] * jw[k];
     }
   }
   if (ORDER >= 2) {
-    constexpr int KH = (NH + SMFX_TPB - 1) / SMFX_TPB;
+    constexpr int KH = (NH + NT - 1) / NT;
     int hidx[KH];
     float hw[KH];
 #pragma unroll
     for (int k = 0; k < KH; k++) {
-      const int w = min(tid + SMFX_TPB * k, NH - 1);
+      const int w = min(tid + NT * k, NH - 1);
       int I, p, q, ex;
       if (MAT) {
         const int m = w / 81, c = (w / 9) % 9, e = w % 9;
@@ -194,7 +196,7 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
       const float *s = sG + mi * 56;
 #pragma unroll
       for (int k = 0; k < KH; k++)
-        if (tid + SMFX_TPB * k < NH) o[tid + SMFX_TPB * k] = s[hidx[k]] * hw[k];
+        if (tid + NT * k < NH) o[tid + NT * k] = s[hidx[k]] * hw[k];
     }
   }
 }

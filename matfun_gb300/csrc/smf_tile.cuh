@@ -43,10 +43,27 @@ struct SmfTileSmem {
   long long gidx[TPB];  // tile position -> matrix index in the arrays
 };
 
-// one tile: matrices base .. base + cnt - 1 by a CTA of TPB threads (the standalone kernel and the batched
-// persistent kernel run the same code); idx (optional): tile position p holds matrix idx[base + p] of the arrays
-// instead of base + p (the ordered launch)
-template <int KIND, int ORDER, bool MAT, int SMF_TPB>
+// order 2: whether a matrix's eigenvalues hold a pair inside the cluster radius of the second divided differences
+// (exp: |a - b| <= tau; log, powers: |a - b| <= tau max(a, b), max > 0): without one, every f[x, y, z] of the matrix
+// takes the difference formula (smf_dd2)
+template <int KIND>
+MF_D bool smf_any_cluster(const double lam[3], const SmfCoef &C) {
+  auto close = [&](double a, double b) -> bool {
+    const double d = fabs(a - b);
+    if (KIND == EXP) return d <= C.tau;
+    const double m = fmax(a, b);
+    return (m > 0) & (d <= C.tau * m);
+  };
+  return close(lam[0], lam[1]) | close(lam[0], lam[2]) | close(lam[1], lam[2]);
+}
+
+// one tile: matrices base .. base + cnt - 1 (cnt <= SMF_TPB) by a CTA of NT >= SMF_TPB threads (the standalone kernel
+// and the batched persistent kernel run the same code): phase A by the first cnt threads, the cooperative loads and
+// stores by all NT; idx (optional): tile position p holds matrix idx[base + p] of the arrays instead of base + p (the
+// ordered launch).  At order 2 the matrices are dealt out to the threads anew after the eigensystem: those with a
+// cluster (smf_any_cluster) go to the last threads, so that the warps before them run the difference formula on
+// every lane instead of both branches of the second divided differences; results do not depend on the assignment.
+template <int KIND, int ORDER, bool MAT, int SMF_TPB, int NT = SMF_TPB>
 MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *__restrict__ F,
                    double *__restrict__ J, double *__restrict__ H, const SmfCoef &C, int *__restrict__ asym,
                    SmfTileSmem<ORDER, MAT, SMF_TPB> &TS, const int *__restrict__ idx = nullptr) {
@@ -54,14 +71,19 @@ MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *
   double *sX = TS.sX, *sF = TS.sF, *sK = TS.sK, *sG = TS.sG;
   const int tid = threadIdx.x;
 
-  for (int e = tid; e < cnt * NIN; e += SMF_TPB) {  // coalesced input (row-wise under idx)
+  for (int e = tid; e < cnt * NIN; e += NT) {  // coalesced input (row-wise under idx)
     const int p = e / NIN;
     const long long g = idx ? (long long)idx[base + p] : base + p;
     sX[e] = x[g * NIN + (e - NIN * p)];
     if (e == NIN * p) TS.gidx[p] = g;
   }
+  // order 2, until the eigensystems are dealt out: sK holds perm[SMF_TPB] (thread -> tile position of the matrix whose
+  // J and H it computes) and part[2] (positions taken from the front, matrices without a cluster, and from the back)
+  int *perm = reinterpret_cast<int *>(sK), *part = perm + (ORDER >= 2 ? SMF_TPB : 0);
+  if (ORDER >= 2 && tid == 0) part[0] = part[1] = 0;
   __syncthreads();
 
+  double lam[3], fl[3], V[3][3];
   if (tid < cnt) {
     double v[6];
     const double *xi = sX + tid * NIN;
@@ -80,7 +102,6 @@ MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *
 #pragma unroll
       for (int k = 0; k < 6; k++) v[k] = xi[k];
     }
-    double lam[3], fl[3], V[3][3];
     smf_eigen<KIND>(v, C.al, lam, fl, V);
     // F = V diag(f) V^T
     double Fv[6];
@@ -96,6 +117,35 @@ MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *
 #pragma unroll
       for (int s = 0; s < 6; s++) sF[tid * 6 + s] = Fv[s];
     }
+  }
+  int mi = tid;  // the tile position whose J and H this thread computes
+  if (ORDER >= 2) {
+    double *stt = sG;  // the eigensystems, [15][SMF_TPB], until sG receives the results
+    if (tid < cnt) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        stt[k * SMF_TPB + tid] = lam[k];
+        stt[(3 + k) * SMF_TPB + tid] = fl[k];
+#pragma unroll
+        for (int b = 0; b < 3; b++) stt[(6 + 3 * k + b) * SMF_TPB + tid] = V[k][b];
+      }
+      const int pos = smf_any_cluster<KIND>(lam, C) ? cnt - 1 - atomicAdd(&part[1], 1) : atomicAdd(&part[0], 1);
+      perm[pos] = tid;
+    }
+    __syncthreads();
+    if (tid < cnt) {
+      mi = perm[tid];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        lam[k] = stt[k * SMF_TPB + mi];
+        fl[k] = stt[(3 + k) * SMF_TPB + mi];
+#pragma unroll
+        for (int b = 0; b < 3; b++) V[k][b] = stt[(6 + 3 * k + b) * SMF_TPB + mi];
+      }
+    }
+    __syncthreads();  // every eigensystem and perm are read before sG and sK receive results
+  }
+  if (tid < cnt) {
     if (ORDER >= 1) {
       // divided differences D (smf_kernel.hpp:299-302)
       double D01 = smf_dd1<KIND>(lam[0], lam[1], fl[0], fl[1], C);
@@ -123,7 +173,7 @@ MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *
 #pragma unroll
           for (int b2 = 0; b2 <= g; b2++) Bv[sym2(b2, g)] = P[b2][0] * dy[0] + P[b2][1] * dy[1] + P[b2][2] * dy[2];
         }
-        double *k_out = sK + tid * 21;
+        double *k_out = sK + mi * 21;
 #pragma unroll
         for (int I = 0; I < 6; I++)
 #pragma unroll
@@ -184,7 +234,7 @@ MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *
         }
         // G'(I, y, z) / 2 = sum over the outer-product terms (s1, t1), (s2, t2), (s3, t3) of E_I, E_y, E_z of
         // T(P[s1 s2], P[t2 s3], P[t1 t3]); the factor 2 goes into the output weight
-        double *g_out = sG + tid * 56;
+        double *g_out = sG + mi * 56;
 #pragma unroll
         for (int z = 0; z < 6; z++)
 #pragma unroll
@@ -217,13 +267,13 @@ MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *
   __syncthreads();
 
   // ---- phase B: coalesced expansion into the output layout
-  for (int e = tid; e < cnt * NF; e += SMF_TPB) F[TS.gidx[e / NF] * NF + e % NF] = sF[e];
+  for (int e = tid; e < cnt * NF; e += NT) F[TS.gidx[e / NF] * NF + e % NF] = sF[e];
   if (ORDER >= 1) {
-    constexpr int KJ = (NJ + SMF_TPB - 1) / SMF_TPB;
+    constexpr int KJ = (NJ + NT - 1) / NT;
     int jidx[KJ], jexp[KJ];
 #pragma unroll
     for (int k = 0; k < KJ; k++) {
-      const int w = min(tid + SMF_TPB * k, NJ - 1);
+      const int w = min(tid + NT * k, NJ - 1);
       int I, p, ex;
       if (MAT) {
         I = midx(w / 9); p = midx(w % 9);
@@ -240,15 +290,15 @@ MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *
       const double *s = sK + mi * 21;
 #pragma unroll
       for (int k = 0; k < KJ; k++)
-        if (tid + SMF_TPB * k < NJ) o[tid + SMF_TPB * k] = mulpow2(s[jidx[k]], jexp[k]);
+        if (tid + NT * k < NJ) o[tid + NT * k] = mulpow2(s[jidx[k]], jexp[k]);
     }
   }
   if (ORDER >= 2) {
-    constexpr int KH = (NH + SMF_TPB - 1) / SMF_TPB;
+    constexpr int KH = (NH + NT - 1) / NT;
     int hidx[KH], hexp[KH];
 #pragma unroll
     for (int k = 0; k < KH; k++) {
-      const int w = min(tid + SMF_TPB * k, NH - 1);
+      const int w = min(tid + NT * k, NH - 1);
       int I, p, q, ex;
       if (MAT) {
         const int m = w / 81, c = (w / 9) % 9, e = w % 9;
@@ -267,7 +317,7 @@ MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *
       const double *s = sG + mi * 56;
 #pragma unroll
       for (int k = 0; k < KH; k++)
-        if (tid + SMF_TPB * k < NH) o[tid + SMF_TPB * k] = mulpow2(s[hidx[k]], hexp[k]);
+        if (tid + NT * k < NH) o[tid + NT * k] = mulpow2(s[hidx[k]], hexp[k]);
     }
   }
 }

@@ -62,7 +62,18 @@ def single(r):
     return outs
 
 
-def test_batched_equals_single_entry_points():
+@pytest.fixture
+def smf_tile(request):
+    """the smf tile geometry of the batched tables built during one test (128 restored afterwards)"""
+    import matfun_gb300
+    lib = matfun_gb300.load()
+    assert lib.matfun_cuda_batched_tune_tiles(request.param) == 0
+    yield request.param
+    lib.matfun_cuda_batched_tune_tiles(128)
+
+
+@pytest.mark.parametrize("smf_tile", [128, 64], indirect=True)
+def test_batched_equals_single_entry_points(smf_tile):
     import torch
 
     from matfun_gb300 import batched
@@ -125,19 +136,23 @@ def test_invalid_requests_rejected():
     assert lib.matfun_cuda_batched(ctypes.cast(batched._array([f32bad]), ctypes.c_void_p), 1, None) == -1
     assert lib.matfun_cuda_batched(None, 0, None) == 0
     assert lib.matfun_cuda_batched_tune(0, 1) == -1 and lib.matfun_cuda_batched_tune(2, 1) == 0
+    assert lib.matfun_cuda_batched_tune_tiles(32) == -1 and lib.matfun_cuda_batched_tune_tiles(128) == 0
 
 
 def test_autotune_roundtrip(tmp_path, monkeypatch):
     from matfun_gb300 import autotune
     monkeypatch.setenv("MATFUN_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
     reqs = mixed_requests(4, count=12, nmax=2000)
-    best, times = autotune.tune(reqs, reps=1, candidates=[{"ctas_per_sm": 1, "longest_first": 1},
-                                                          {"ctas_per_sm": 2, "longest_first": 1}])
-    assert best in ({"ctas_per_sm": 1, "longest_first": 1}, {"ctas_per_sm": 2, "longest_first": 1})
+    cands = [{"ctas_per_sm": 1, "longest_first": 1, "smf_tile": 128},
+             {"ctas_per_sm": 2, "longest_first": 1, "smf_tile": 64}]
+    best, times = autotune.tune(reqs, reps=1, candidates=cands)
+    assert best in cands and len(times) == 2
     assert autotune.apply(reqs) == best
+    autotune._set(autotune.load(), autotune.DEFAULT)  # later tests run with the default tuning
 
 
-def test_batched_c3_mix_against_oracle():
+@pytest.mark.parametrize("smf_tile", [128, 64], indirect=True)
+def test_batched_c3_mix_against_oracle(smf_tile):
     """a C3-style mix in one persistent launch held directly against the FP64 oracle: every family, kind and order,
     FP64 and FP32 requests, and gmf log / pow requests of >= 2048 matrices that the launch orders by spectral class
     first; FP64 within 1e-12 per call with NaN exactly where the oracle has NaN, FP32 per matrix within the bounds of
