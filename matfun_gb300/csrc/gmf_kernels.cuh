@@ -361,6 +361,8 @@ MF_D void gmf_tile(int64_t base, int cnt, const T *__restrict__ A, T *__restrict
   }
   S.key[tid] = key;
   __syncthreads();
+  // the scratch of an ordered launch (idx, roots, keys: rows of the last matrices' H) has been read by this CTA
+  griddep_launch_dependents();
   {
     int rank = 0;
     for (int j = 0; j < GMF_TPB; j++) {
@@ -542,15 +544,31 @@ __global__ void __launch_bounds__(GKEY_TPB) gmf_key_kernel(int n, const T *__res
   for (int k = threadIdx.x; k < GKEY_BINS; k += GKEY_TPB) counts[k * nblk + blockIdx.x] = hist[k];
 }
 
+// (early: launched with programmatic stream serialisation, so that it may start once every CTA of the preceding
+// gmf_kernel launch has read its scratch -- griddep_launch_dependents in gmf_tile -- instead of after its last CTA)
 template <int KIND, int ORDER, typename T>
 cudaError_t gmf_launch_one(cudaStream_t st, unsigned blocks, int64_t n, const T *A, T *F, T *J, T *H,
                            const GmfCoef &C, const int *idx = nullptr, const double *roots = nullptr,
-                           const unsigned char *keys = nullptr) {
+                           const unsigned char *keys = nullptr, bool early = false) {
   static std::atomic<unsigned long long> attr{0};  // per instantiation, one bit per device
-  const cudaError_t e = smem_limit_per_device(gmf_kernel<KIND, ORDER, T>, (int)sizeof(GmfSmem), attr);
+  cudaError_t e = smem_limit_per_device(gmf_kernel<KIND, ORDER, T>, (int)sizeof(GmfSmem), attr);
   if (e != cudaSuccess) return e;
-  gmf_kernel<KIND, ORDER, T><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C, idx, roots, keys);
-  return cudaGetLastError();
+  if (!early) {
+    gmf_kernel<KIND, ORDER, T><<<blocks, GMF_TPB, sizeof(GmfSmem), st>>>(n, A, F, J, H, C, idx, roots, keys);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(GMF_TPB);
+  cfg.dynamicSmemBytes = sizeof(GmfSmem);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, gmf_kernel<KIND, ORDER, T>, n, A, F, J, H, C, idx, roots, keys);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 // orders 1 and 2 of a large batch: key, sort, reordered evaluation of the first nm matrices, plain evaluation of the
@@ -588,8 +606,9 @@ cudaError_t gmf_launch_sorted(cudaStream_t st, int64_t n, const T *A, T *F, T *J
   T *Ft = F ? F + nm * 9 : nullptr;
   T *Jt = ORDER == 3 ? (J ? J + nm * 9 : nullptr) : J + nm * 81;
   T *Ht = ORDER == 3 ? H + nm * 81 : (ORDER == 2 ? H + nm * 729 : nullptr);
+  // the tail overwrites the scratch only: it may start as soon as every CTA of the ordered launch has read it
   return gmf_launch_one<KIND, ORDER, T>(st, (unsigned)((tail + GMF_TPB - 1) / GMF_TPB), tail, A + nm * 9, Ft, Jt, Ht,
-                                        C);
+                                        C, nullptr, nullptr, nullptr, true);
 }
 
 constexpr int64_t GMF_SORT_MIN = 1 << 15;  // below this the reordering does not pay for its launches

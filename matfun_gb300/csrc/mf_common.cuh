@@ -49,6 +49,15 @@ MF_D void split_exponent(double al, double k, double &bh, double &bl) {
 
 MF_D double copysgn(double x, double y) { return y < 0 ? -fabs(x) : fabs(x); }
 
+// Programmatic dependent launch: this CTA no longer needs what a dependent grid launched with programmatic stream
+// serialisation will overwrite, so that grid may start once every CTA of this one has said so or exited.  Without
+// such a dependent (a plain launch) it has no effect.  (Host builds of the tile code: nothing to signal.)
+MF_D void griddep_launch_dependents() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
 // ------------------------------------------------------------------------------------------- complex (re, im)
 struct cx {
   double re, im;

@@ -231,7 +231,10 @@ MF_D void smf_eigen(const double *v, double al, double lam[3], double fl[3], dou
 // ---- first divided differences f[a, b] (f[a, a] = f'(a)) in forms stable for close arguments
 // exp: e^max(a, b) (1 - e^-d) / d, d = |a - b| (no overflow, no cancellation)
 // log: with s = (a + b) / 2, z = (a - b) / (a + b): log a - log b = 2 atanh z, so f[a, b] = atanh(z) / (z s); its
-//      series (1 + z^2/3 + z^4/5 + z^6/7) / s for |z| < 1e-3, and the plain quotient for |z| >= 0.5
+//      series (1 + z^2/3 + z^4/5 + z^6/7) / s for |z| < 1e-3, and the plain quotient (fa - fb) / (a - b) of the
+//      logarithms already at hand for |z| >= 0.5 (a / b >= 3: their difference is >= log 3, so it is as accurate as
+//      log a - log b evaluated anew, and a warp whose lanes split between this and the atanh form pays two
+//      subtractions and a division for it instead of two more logarithms)
 // sqrt: 1 / (sqrt a + sqrt b) (arguments clamped at 0: PSD round-off)
 // powers: with s the mean and z = (a - b) / (2 s): a^al - b^al = s^al ((1 + z)^al - (1 - z)^al), so
 //      f[a, b] = s^(al - 1) (expm1(al log1p z) - expm1(al log1p(-z))) / (2 z) for 0 < |z| < 0.5, al s^(al - 1) at
@@ -245,7 +248,7 @@ MF_D double smf_dd1(double a, double b, double fa, double fb, const SmfCoef &C) 
   }
   if (KIND == LOG) {
     const double s = 0.5 * (a + b), z = (a - b) / (a + b), az = fabs(z);
-    if (az >= 0.5) return (log(a) - log(b)) / (a - b);
+    if (az >= 0.5) return (fa - fb) / (a - b);
     if (az < 1e-3) {
       const double z2 = z * z;
       return (1.0 + z2 / 3.0 + z2 * z2 / 5.0 + z2 * z2 * z2 / 7.0) / s;

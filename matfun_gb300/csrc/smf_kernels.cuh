@@ -115,9 +115,20 @@ cudaError_t smf_launch_sorted(cudaStream_t st, int64_t n, const double *x, doubl
   gmf_scatter_kernel<<<nblk, GKEY_TPB, 0, st>>>((int)nm, keys, counts, totals, nblk, order);
   smf_kernel<KIND, 2, MAT><<<(unsigned)((nm + SMF_TPB - 1) / SMF_TPB), SMF_TPB, 0, st>>>(nm, x, F, J, H, C, asym,
                                                                                          order);
-  smf_kernel<KIND, 2, MAT><<<(unsigned)((tail + SMF_TPB - 1) / SMF_TPB), SMF_TPB, 0, st>>>(
-      tail, x + nm * NIN, F + nm * NF, J + nm * NJ, H + nm * NH, C, asym, nullptr);
-  return cudaGetLastError();
+  // the tail overwrites the scratch only: launched with programmatic stream serialisation, it may start as soon as
+  // every CTA of the ordered launch has read its part of the order (griddep_launch_dependents in smf_tile)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)((tail + SMF_TPB - 1) / SMF_TPB));
+  cfg.blockDim = dim3(SMF_TPB);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, smf_kernel<KIND, 2, MAT>, (int64_t)tail, x + nm * NIN, F + nm * NF,
+                                           J + nm * NJ, H + nm * NH, C, asym, (const int *)nullptr);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int KIND, bool MAT>

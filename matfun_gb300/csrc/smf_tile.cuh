@@ -82,6 +82,7 @@ MF_D void smf_tile(int64_t base, int cnt, const double *__restrict__ x, double *
   int *perm = reinterpret_cast<int *>(sK), *part = perm + (ORDER >= 2 ? SMF_TPB : 0);
   if (ORDER >= 2 && tid == 0) part[0] = part[1] = 0;
   __syncthreads();
+  griddep_launch_dependents();  // the scratch of an ordered launch (idx: rows of the last matrices' H) has been read
 
   double lam[3], fl[3], V[3][3];
   if (tid < cnt) {
