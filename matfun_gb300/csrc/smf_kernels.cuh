@@ -14,6 +14,9 @@
 
 namespace mf {
 
+// (order 2: 228 registers and 46 KB of shared memory, 4 CTAs per SM.  A form with the inputs staged inside sG (43 KB,
+// 166 registers, 5 CTAs per SM) ran 8 % slower on C0 -- n = 65536 then fills 1.35 waves of CTAs instead of 1.68 --
+// and within +-4 % at n = 2^24.)
 template <int KIND, int ORDER, bool MAT>
 __global__ void __launch_bounds__(SMF_TPB) smf_kernel(int64_t n, const double *__restrict__ x,
                                                       double *__restrict__ F, double *__restrict__ J,

@@ -10,10 +10,12 @@ namespace mf {
 
 constexpr int SMFX_TPB = 64;  // matrices per CTA of the standalone kernel
 
+// (order 2: the inputs are staged in the last TPB * NIN floats of sG, read before sG receives results -- 21 KB per
+// 64 Voigt matrices, 10 CTAs per SM)
 template <int ORDER, bool MAT, int TPB>
 struct SmfxTileSmem {
   static constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6;
-  float sX[TPB * NIN];
+  float sX[ORDER >= 2 ? 1 : TPB * NIN];
   float sF[TPB * NF];
   float sK[ORDER >= 1 ? TPB * 21 : 1];
   float sG[ORDER >= 2 ? TPB * 56 : 1];
@@ -26,15 +28,19 @@ MF_D void smf_mixed_tile(int64_t base, int cnt, const float *__restrict__ x, flo
                          float *__restrict__ J, float *__restrict__ H, const SmfCoefF &C,
                          SmfxTileSmem<ORDER, MAT, SMFX_TPB> &TS) {
   constexpr int NIN = MAT ? 9 : 6, NF = MAT ? 9 : 6, NJ = NF * NF, NH = NJ * NF;
-  float *sX = TS.sX, *sF = TS.sF, *sK = TS.sK, *sG = TS.sG;
+  float *sF = TS.sF, *sK = TS.sK, *sG = TS.sG;
+  float *sX = ORDER >= 2 ? sG + SMFX_TPB * (56 - NIN) : TS.sX;
   const int tid = threadIdx.x;
   for (int e = tid; e < cnt * NIN; e += NT) sX[e] = x[base * NIN + e];
   __syncthreads();
+  SmfInF in;
   if (tid < cnt) {
     const float *xi = sX + tid * NIN;
-    SmfInF in;
     if (MAT) sym_in_f(xi, in);
     else voigt_in_f(xi, in);
+  }
+  if (ORDER >= 2) __syncthreads();  // every staged input is read before sG receives results
+  if (tid < cnt) {
     SmfSpecF Sp;
     smf_spectrum_f<KIND, MAT>(in, C, Sp);
     const float(&V)[3][3] = Sp.V;
