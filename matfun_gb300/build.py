@@ -56,11 +56,17 @@ def _rdc(src):
     return os.path.basename(src).startswith("batched")
 
 
+def _extra(src):
+    """the general family's batched tile routines: 168 registers (65536 / (128 threads x 3 CTAs per SM)), so that
+    batched_gmf_kernel runs 3 CTAs per SM like the standalone gmf kernel, whose launch bounds give the same"""
+    return ["-maxrregcount=168"] if os.path.basename(src) in ("batched_gmf.cu", "batched_gmf32.cu") else []
+
+
 def _compile(src, hdr_time, verbose):
     obj = os.path.join(OBJ, os.path.basename(src)[:-3] + ".o")
     if _fresh(obj, max(os.path.getmtime(src), hdr_time)):
         return obj, ""
-    cmd = [_nvcc()] + NVFLAGS + (["-rdc=true"] if _rdc(src) else []) + ["-c", src, "-o", obj]
+    cmd = [_nvcc()] + NVFLAGS + (["-rdc=true"] if _rdc(src) else []) + _extra(src) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -70,7 +76,7 @@ def _compile(src, hdr_time, verbose):
 def build_cuda(verbose=False, jobs=None):
     os.makedirs(OBJ, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
-    hdr = _newest_header()
+    hdr = max(_newest_header(), os.path.getmtime(__file__))  # (the compiler flags live in this file)
     jobs = jobs or max(1, min(len(srcs), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(jobs) as ex:
         res = list(ex.map(lambda s: _compile(s, hdr, verbose), srcs))

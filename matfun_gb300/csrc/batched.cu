@@ -1,12 +1,14 @@
 // batched.cu -- many requests of uneven size and mixed family / kind / order / precision in one launch.
 //
 // The host cuts every request into tiles (gmf: 128 matrices; smf: 64 or 128, matfun_cuda_batched_tune_tiles) and
-// writes a table (requests, their coefficient blocks, the prefix sum of their tile counts) into device memory.  One
-// persistent kernel (grid = SMs x CTAs per SM) then pulls tiles from a global atomic cursor until all are taken; each
-// tile runs the same tile routine as the standalone kernel of its request (smf FP64 / mixed FP32 in either layout,
-// gmf FP64 / mixed FP32), by the CTA's 128 threads.  The launch's dynamic shared memory is that of its largest tile.
-// There is no waiting between CTAs: a CTA only increments the cursor and stops when it passes the tile count, so no
-// wait can hang.
+// writes a table (requests, their coefficient blocks, the prefix sum of their tile counts; the general family's
+// requests first) into device memory.  Two persistent kernels (grid = SMs x CTAs per SM) then pull tiles from their
+// global atomic cursors until all are taken: batched_gmf_kernel the general family's, at the 3 CTAs per SM of the
+// standalone gmf kernel, and batched_kernel the others, launched as a programmatic dependent of the first so that it
+// fills the SMs the first one leaves as it drains.  Each tile runs the same tile routine as the standalone kernel of
+// its request (smf FP64 / mixed FP32 in either layout, gmf FP64 / mixed FP32), by the CTA's 128 threads; a launch's
+// dynamic shared memory is that of its largest tile.  There is no waiting between CTAs: a CTA only increments its
+// cursor and stops when it passes the tile count, so no wait can hang.
 //
 // Two ways to run it:
 //   matfun_cuda_batched(requests, count, stream)          table in a per-device cached buffer, uploaded on `stream`
@@ -59,10 +61,13 @@ namespace {
     default: MF_GMF_CALL(pfx, 2) break; \
   }
 
+__device__ void run_gmf_tile(const DevReq &R, long long base, int cnt, const unsigned char *coef,
+                             unsigned char *smem) {
+  if (R.dtype == 0) { MF_GMF_KIND(bt_gmf) } else { MF_GMF_KIND(bt_gmf32) }
+}
+
 __device__ void run_tile(const DevReq &R, long long base, int cnt, const unsigned char *coef, unsigned char *smem) {
-  if (R.family == 2) {
-    if (R.dtype == 0) { MF_GMF_KIND(bt_gmf) } else { MF_GMF_KIND(bt_gmf32) }
-  } else if (R.tile == BT_TPB) {
+  if (R.tile == BT_TPB) {
     if (R.family == 1) {
       if (R.dtype == 0) { MF_SMF_KIND(bt_smf64, m) } else { MF_SMF_KIND(bt_smf32, m) }
     } else {
@@ -77,15 +82,16 @@ __device__ void run_tile(const DevReq &R, long long base, int cnt, const unsigne
   }
 }
 
-__global__ void __launch_bounds__(BT_TPB) batched_kernel(const DevReq *__restrict__ reqs, int nreq,
-                                                         const long long *__restrict__ tile_start,
-                                                         unsigned long long *__restrict__ cursor,
-                                                         const unsigned char *__restrict__ coefs) {
-  extern __shared__ __align__(16) unsigned char smem[];
+// the persistent loop over the tiles tile_start[0] .. tile_start[nreq] - 1 of requests reqs[0 .. nreq - 1]
+template <bool GMF_ONLY>
+__device__ __forceinline__ void batched_loop(const DevReq *__restrict__ reqs, int nreq,
+                                             const long long *__restrict__ tile_start,
+                                             unsigned long long *__restrict__ cursor,
+                                             const unsigned char *__restrict__ coefs, unsigned char *smem) {
   __shared__ long long s_tile;
-  const long long total = tile_start[nreq];
+  const long long first = tile_start[0], total = tile_start[nreq];
   for (;;) {
-    if (threadIdx.x == 0) s_tile = (long long)atomicAdd(cursor, 1ull);
+    if (threadIdx.x == 0) s_tile = first + (long long)atomicAdd(cursor, 1ull);
     __syncthreads();
     const long long t = s_tile;
     __syncthreads();
@@ -99,9 +105,31 @@ __global__ void __launch_bounds__(BT_TPB) batched_kernel(const DevReq *__restric
     const DevReq R = reqs[lo];
     const long long base = (t - tile_start[lo]) * R.tile;
     const int cnt = (int)min((long long)R.tile, R.n - base);
-    run_tile(R, base, cnt, coefs + R.coef_off, smem);
+    if (GMF_ONLY) run_gmf_tile(R, base, cnt, coefs + R.coef_off, smem);
+    else run_tile(R, base, cnt, coefs + R.coef_off, smem);
     __syncthreads();  // the tile's shared memory is reused by the next tile
   }
+}
+
+// every family (the symmetric tile routines take up to 255 registers: 2 CTAs per SM)
+__global__ void __launch_bounds__(BT_TPB) batched_kernel(const DevReq *__restrict__ reqs, int nreq,
+                                                         const long long *__restrict__ tile_start,
+                                                         unsigned long long *__restrict__ cursor,
+                                                         const unsigned char *__restrict__ coefs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  batched_loop<false>(reqs, nreq, tile_start, cursor, coefs, smem);
+}
+
+// the general family's requests, at the 3 CTAs per SM of the standalone gmf kernel (its tile routines are compiled
+// for 168 registers); the launch that follows it on the stream may start once every CTA has started (the requests
+// of one table are independent)
+__global__ void __launch_bounds__(BT_TPB, GMF_MIN_CTAS) batched_gmf_kernel(const DevReq *__restrict__ reqs, int nreq,
+                                                                          const long long *__restrict__ tile_start,
+                                                                          unsigned long long *__restrict__ cursor,
+                                                                          const unsigned char *__restrict__ coefs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  griddep_launch_dependents();
+  batched_loop<true>(reqs, nreq, tile_start, cursor, coefs, smem);
 }
 
 // the dynamic shared memory of one request's tiles
@@ -158,7 +186,8 @@ struct Table {                  // a validated request list laid out for the dev
   int count = 0;
   std::vector<Ord> ords;
   size_t ord_bytes = 0;
-  size_t smem = 0;  // dynamic shared memory of the launch: the largest of its requests' tiles
+  int gmf_count = 0;  // requests 0 .. gmf_count - 1 are the general family's (batched_gmf_kernel), the rest the others
+  size_t smem = 0;    // dynamic shared memory of the launch of the other families: the largest of their tiles
 };
 
 size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -212,7 +241,7 @@ int build_table(const mf_request *req, int count, Table &T) {
       std::memcpy(it.coef.data(), &C, sizeof C);
     }
     it.tiles = (r.n + it.d.tile - 1) / it.d.tile;
-    T.smem = std::max(T.smem, tile_smem(r.family, r.order, r.dtype, it.d.tile));
+    if (r.family != 2) T.smem = std::max(T.smem, tile_smem(r.family, r.order, r.dtype, it.d.tile));
     // relative work per matrix (measured orders of magnitude): gmf order 2 >> smf order 2 >> first orders
     const double per = (r.family == 2 ? 4.0 : 1.0) * (r.order == 2 ? 4.0 : (r.order == 1 ? 1.5 : 1.0)) *
                        (r.dtype == 1 ? (r.family == 2 ? 0.8 : 0.3) : 1.0);
@@ -221,6 +250,9 @@ int build_table(const mf_request *req, int count, Table &T) {
   }
   if (g_tune.longest_first)
     std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) { return a.work > b.work; });
+  // the general family's requests first: their own persistent launch precedes that of the others
+  std::stable_partition(items.begin(), items.end(), [](const Item &a) { return a.d.family == 2; });
+  T.gmf_count = (int)std::count_if(items.begin(), items.end(), [](const Item &a) { return a.d.family == 2; });
   T.count = (int)items.size();
   T.off_tiles = align16(sizeof(DevReq) * T.count);
   T.off_coef = align16(T.off_tiles + sizeof(long long) * (T.count + 1));
@@ -287,10 +319,12 @@ cudaError_t launch_orders(const Table &T, unsigned char *ord_base, cudaStream_t 
 }
 
 cudaError_t prepare_kernel() {
-  static std::atomic<unsigned long long> done{0};  // one bit per device
-  return smem_limit_per_device(batched_kernel, (int)smem_max(), done);
+  static std::atomic<unsigned long long> done{0}, done_g{0};  // one bit per device
+  const cudaError_t e = smem_limit_per_device(batched_kernel, (int)smem_max(), done);
+  return e != cudaSuccess ? e : smem_limit_per_device(batched_gmf_kernel, (int)sizeof(GmfSmem), done_g);
 }
 
+// cursors: two 8-byte counters (general family, the others) at `cursor`
 cudaError_t launch_table(const unsigned char *dev_table, const Table &T, unsigned long long *cursor,
                          cudaStream_t st) {
   if (T.count == 0) return cudaSuccess;
@@ -299,12 +333,30 @@ cudaError_t launch_table(const unsigned char *dev_table, const Table &T, unsigne
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), st);
+  e = cudaMemsetAsync(cursor, 0, 2 * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  const unsigned grid = (unsigned)(sms * std::max(1, g_tune.ctas_per_sm));
-  batched_kernel<<<grid, BT_TPB, T.smem, st>>>((const DevReq *)dev_table, T.count,
-                                               (const long long *)(dev_table + T.off_tiles), cursor,
-                                               dev_table + T.off_coef);
+  const DevReq *reqs = (const DevReq *)dev_table;
+  const long long *tiles = (const long long *)(dev_table + T.off_tiles);
+  const unsigned char *coefs = dev_table + T.off_coef;
+  if (T.gmf_count > 0)
+    batched_gmf_kernel<<<(unsigned)(sms * GMF_MIN_CTAS), BT_TPB, sizeof(GmfSmem), st>>>(reqs, T.gmf_count, tiles,
+                                                                                       cursor, coefs);
+  if (T.count > T.gmf_count) {
+    // the other families' launch may start while the general family's drains (programmatic dependent launch)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(sms * std::max(1, g_tune.ctas_per_sm)));
+    cfg.blockDim = dim3(BT_TPB);
+    cfg.dynamicSmemBytes = T.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = T.gmf_count > 0 ? 1 : 0;
+    e = cudaLaunchKernelEx(&cfg, batched_kernel, reqs + T.gmf_count, T.count - T.gmf_count, tiles + T.gmf_count,
+                           cursor + 1, coefs);
+    if (e != cudaSuccess) return e;
+  }
   return cudaGetLastError();
 }
 

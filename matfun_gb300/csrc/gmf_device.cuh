@@ -158,7 +158,7 @@ MF_D void group_tail(int K, int j1, int j2, const GmfCoef &C, const bool *inG, c
     ur[i] = ff_of(u[i].re * us);
     ui[i] = REAL ? zero : ff_of(u[i].im * us);
   }
-  ffl Er[ND], Ei[ND], Fr[ND], Fi[ND], Sr[ND], Si[ND];
+  ffl Er[ND], Ei[ND], Sr[ND], Si[ND];  // (the state updated in place, as in group_series)
 #pragma unroll
   for (int c = 0; c < ND; c++) {
     const double es = pow2i(-sh * (j1 - 1 - gdeg(c, inG)));
@@ -171,31 +171,31 @@ MF_D void group_tail(int K, int j1, int j2, const GmfCoef &C, const bool *inG, c
   for (int j = j1; j < jb; j++) {
     const ffl bj = {C.bth[j], C.btl[j]};
 #pragma unroll
-    for (int c = 0; c < ND; c++) {
+    for (int c = ND - 1; c >= 0; c--) {
       const int par = gpar(c), i = gnode(c);
-      ffl eppr = par < 0 ? zero : Er[par < 0 ? 0 : par];
-      ffl epcr = par < 0 ? zero : Fr[par < 0 ? 0 : par];
+      const ffl eppr = par < 0 ? zero : Er[par < 0 ? 0 : par];
       if (REAL) {
-        Fr[c] = ff_sel(inG[i], ff_add_s(eppr, ff_prod(ur[i], Er[c])), epcr);
-        acc_ff_add(Sr[c], ff_prod(Fr[c], bj));
+        Er[c] = ff_sel(inG[i], ff_add_s(eppr, ff_prod(ur[i], Er[c])), Er[c]);
       } else {
-        ffl eppi = par < 0 ? zero : Ei[par < 0 ? 0 : par];
-        ffl epci = par < 0 ? zero : Fi[par < 0 ? 0 : par];
-        ffl tr = ff_add3(eppr, ff_prod(ur[i], Er[c]), ff_neg(ff_prod(ui[i], Ei[c])));
-        ffl ti = ff_add3(eppi, ff_prod(ur[i], Ei[c]), ff_prod(ui[i], Er[c]));
-        Fr[c] = ff_sel(inG[i], tr, epcr);
-        Fi[c] = ff_sel(inG[i], ti, epci);
-        acc_ff_add(Sr[c], ff_prod(Fr[c], bj));
-        acc_ff_add(Si[c], ff_prod(Fi[c], bj));
+        const ffl eppi = par < 0 ? zero : Ei[par < 0 ? 0 : par];
+        const ffl tr = ff_add3(eppr, ff_prod(ur[i], Er[c]), ff_neg(ff_prod(ui[i], Ei[c])));
+        const ffl ti = ff_add3(eppi, ff_prod(ur[i], Ei[c]), ff_prod(ui[i], Er[c]));
+        Er[c] = ff_sel(inG[i], tr, Er[c]);
+        Ei[c] = ff_sel(inG[i], ti, Ei[c]);
       }
     }
 #pragma unroll
     for (int c = 0; c < ND; c++) {
-      Er[c] = Fr[c];
-      if (!REAL) Ei[c] = Fi[c];
+      const int par = gpar(c), i = gnode(c);
+      Er[c] = ff_sel(inG[i], Er[c], par < 0 ? zero : Er[par < 0 ? 0 : par]);
+      acc_ff_add(Sr[c], ff_prod(Er[c], bj));
+      if (!REAL) {
+        Ei[c] = ff_sel(inG[i], Ei[c], par < 0 ? zero : Ei[par < 0 ? 0 : par]);
+        acc_ff_add(Si[c], ff_prod(Ei[c], bj));
+      }
     }
   }
-  float er[ND], ei[ND], fr[ND], fi[ND], sr[ND], si[ND], vr[3], vi[3];
+  float er[ND], ei[ND], sr[ND], si[ND], vr[3], vi[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     vr[i] = ur[i].hi;
@@ -211,25 +211,27 @@ MF_D void group_tail(int K, int j1, int j2, const GmfCoef &C, const bool *inG, c
   for (int j = jb > j1 ? jb : j1; j < K; j++) {
     const float bj = C.bth[j];
 #pragma unroll
-    for (int c = 0; c < ND; c++) {
+    for (int c = ND - 1; c >= 0; c--) {
       const int par = gpar(c), i = gnode(c);
-      float eppr = par < 0 ? 0.f : er[par < 0 ? 0 : par], epcr = par < 0 ? 0.f : fr[par < 0 ? 0 : par];
+      const float eppr = par < 0 ? 0.f : er[par < 0 ? 0 : par];
       if (REAL) {
-        fr[c] = inG[i] ? fmaf(vr[i], er[c], eppr) : epcr;
-        sr[c] = fmaf(fr[c], bj, sr[c]);
+        er[c] = inG[i] ? fmaf(vr[i], er[c], eppr) : er[c];
       } else {
-        float eppi = par < 0 ? 0.f : ei[par < 0 ? 0 : par], epci = par < 0 ? 0.f : fi[par < 0 ? 0 : par];
-        float tr = fmaf(-vi[i], ei[c], fmaf(vr[i], er[c], eppr)), ti = fmaf(vi[i], er[c], fmaf(vr[i], ei[c], eppi));
-        fr[c] = inG[i] ? tr : epcr;
-        fi[c] = inG[i] ? ti : epci;
-        sr[c] = fmaf(fr[c], bj, sr[c]);
-        si[c] = fmaf(fi[c], bj, si[c]);
+        const float eppi = par < 0 ? 0.f : ei[par < 0 ? 0 : par];
+        const float tr = fmaf(-vi[i], ei[c], fmaf(vr[i], er[c], eppr)), ti = fmaf(vi[i], er[c], fmaf(vr[i], ei[c], eppi));
+        er[c] = inG[i] ? tr : er[c];
+        ei[c] = inG[i] ? ti : ei[c];
       }
     }
 #pragma unroll
     for (int c = 0; c < ND; c++) {
-      er[c] = fr[c];
-      if (!REAL) ei[c] = fi[c];
+      const int par = gpar(c), i = gnode(c);
+      er[c] = inG[i] ? er[c] : (par < 0 ? 0.f : er[par < 0 ? 0 : par]);
+      sr[c] = fmaf(er[c], bj, sr[c]);
+      if (!REAL) {
+        ei[c] = inG[i] ? ei[c] : (par < 0 ? 0.f : ei[par < 0 ? 0 : par]);
+        si[c] = fmaf(ei[c], bj, si[c]);
+      }
     }
   }
 #pragma unroll
@@ -243,10 +245,16 @@ MF_D void group_tail(int K, int j1, int j2, const GmfCoef &C, const bool *inG, c
 // the streamed group series (gmf_kernel.hpp:493-519) of the ND divided differences; REAL: every in-group offset
 // and hence every term is real (half the FP64 instructions of the complex recursion).  FP64 terms up to j1, the tail
 // by group_tail (j1 >= K: all in FP64)
+//
+// The recursion state is updated in place: a term of entry c is its parent's previous term plus u_i times its own
+// previous term (entries with an in-group node i), or its parent's new term (the others).  So the in-group entries
+// are updated from the last to the first (a parent has the lower index and still holds its previous term), then the
+// others from the first to the last (their parent already holds its new term): one state array instead of two, the
+// same arithmetic.
 template <int ND, bool REAL>
 MF_D void group_series(int K, double b0, const GmfCoef &C, const bool *inG, const bool *pk, const cx *u, double iap,
                        cx *D, int j1 = G_KMAX, int j2 = G_KMAX) {
-  cx Ep[ND], Ec[ND];
+  cx Ep[ND];
 #pragma unroll
   for (int c = 0; c < ND; c++)
     Ep[c] = csel(inG[gnode(c)], cmk(0.0, 0.0), gpar(c) < 0 ? cmk(1.0, 0.0) : Ep[gpar(c) < 0 ? 0 : gpar(c)]);
@@ -258,22 +266,25 @@ MF_D void group_series(int K, double b0, const GmfCoef &C, const bool *inG, cons
     q1 = g1; q2 = g2; q3 = g3;
     double qv[4] = {bj, g1, g2, g3};
 #pragma unroll
-    for (int c = 0; c < ND; c++) {
+    for (int c = ND - 1; c >= 0; c--) {
       const int par = gpar(c), i = gnode(c);
-      cx epp = par < 0 ? cmk(sel(j == 0, 1.0, 0.0), 0.0) : Ep[par < 0 ? 0 : par];
-      cx epc = par < 0 ? cmk(0.0, 0.0) : Ec[par < 0 ? 0 : par];
-      double g = sel(pk[0], qv[gms(c, 0)], sel(pk[1], qv[gms(c, 1)], sel(pk[2], qv[gms(c, 2)], qv[0])));
-      if (REAL) {
-        Ec[c].re = sel(inG[i], epp.re + u[i].re * Ep[c].re, epc.re);
-        Ec[c].im = 0.0;
-        D[c].re = D[c].re + Ec[c].re * g;
-      } else {
-        Ec[c] = csel(inG[i], cadd(epp, cmul(u[i], Ep[c])), epc);
-        D[c] = cadd(D[c], cscl(Ec[c], g));
-      }
+      const cx epp = par < 0 ? cmk(sel(j == 0, 1.0, 0.0), 0.0) : Ep[par < 0 ? 0 : par];
+      if (REAL) Ep[c].re = sel(inG[i], epp.re + u[i].re * Ep[c].re, Ep[c].re);
+      else Ep[c] = csel(inG[i], cadd(epp, cmul(u[i], Ep[c])), Ep[c]);
     }
 #pragma unroll
-    for (int c = 0; c < ND; c++) Ep[c] = Ec[c];
+    for (int c = 0; c < ND; c++) {
+      const int par = gpar(c), i = gnode(c);
+      const cx epc = par < 0 ? cmk(0.0, 0.0) : Ep[par < 0 ? 0 : par];
+      const double g = sel(pk[0], qv[gms(c, 0)], sel(pk[1], qv[gms(c, 1)], sel(pk[2], qv[gms(c, 2)], qv[0])));
+      if (REAL) {
+        Ep[c].re = sel(inG[i], Ep[c].re, epc.re);
+        D[c].re = D[c].re + Ep[c].re * g;
+      } else {
+        Ep[c] = csel(inG[i], Ep[c], epc);
+        D[c] = cadd(D[c], cscl(Ep[c], g));
+      }
+    }
   }
   if (K > ja) group_tail<ND, REAL>(K, ja, j2, C, inG, u, Ep, D);
 }
@@ -297,7 +308,7 @@ MF_D void group_series_ff(int K, double b0, const GmfCoef &C, const bool *inG, c
     ui[i] = REAL ? ffl{0.f, 0.f} : ff_of(u[i].im * up);
   }
   const ffl qh = ff_of(iap / up), zero = {0.f, 0.f}, one = {1.f, 0.f}, b0f = ff_of(b0);
-  ffl Epr[ND], Epi[ND], Ecr[ND], Eci[ND], Dr[ND], Di[ND];
+  ffl Epr[ND], Epi[ND], Dr[ND], Di[ND];  // (the state updated in place, as in group_series)
 #pragma unroll
   for (int c = 0; c < ND; c++) {
     Epr[c] = ff_sel(inG[gnode(c)], zero, gpar(c) < 0 ? one : Epr[gpar(c) < 0 ? 0 : gpar(c)]);
@@ -316,29 +327,29 @@ MF_D void group_series_ff(int K, double b0, const GmfCoef &C, const bool *inG, c
     q1 = g1; q2 = g2; q3 = g3;
     ffl qv[4] = {bj, g1, g2, g3};
 #pragma unroll
-    for (int c = 0; c < ND; c++) {
+    for (int c = ND - 1; c >= 0; c--) {
       const int par = gpar(c), i = gnode(c);
-      ffl eppr = par < 0 ? ff_sel(j == 0, one, zero) : Epr[par < 0 ? 0 : par];
-      ffl epcr = par < 0 ? zero : Ecr[par < 0 ? 0 : par];
-      ffl g = ff_sel(pk[0], qv[gms(c, 0)], ff_sel(pk[1], qv[gms(c, 1)], ff_sel(pk[2], qv[gms(c, 2)], qv[0])));
+      const ffl eppr = par < 0 ? ff_sel(j == 0, one, zero) : Epr[par < 0 ? 0 : par];
       if (REAL) {
-        Ecr[c] = ff_sel(inG[i], ff_add_s(eppr, ff_prod(ur[i], Epr[c])), epcr);
-        acc_ff_add(Dr[c], ff_prod(Ecr[c], g));
+        Epr[c] = ff_sel(inG[i], ff_add_s(eppr, ff_prod(ur[i], Epr[c])), Epr[c]);
       } else {
-        ffl eppi = par < 0 ? zero : Epi[par < 0 ? 0 : par];
-        ffl epci = par < 0 ? zero : Eci[par < 0 ? 0 : par];
-        ffl tr = ff_add3(eppr, ff_prod(ur[i], Epr[c]), ff_neg(ff_prod(ui[i], Epi[c])));
-        ffl ti = ff_add3(eppi, ff_prod(ur[i], Epi[c]), ff_prod(ui[i], Epr[c]));
-        Ecr[c] = ff_sel(inG[i], tr, epcr);
-        Eci[c] = ff_sel(inG[i], ti, epci);
-        acc_ff_add(Dr[c], ff_prod(Ecr[c], g));
-        acc_ff_add(Di[c], ff_prod(Eci[c], g));
+        const ffl eppi = par < 0 ? zero : Epi[par < 0 ? 0 : par];
+        const ffl tr = ff_add3(eppr, ff_prod(ur[i], Epr[c]), ff_neg(ff_prod(ui[i], Epi[c])));
+        const ffl ti = ff_add3(eppi, ff_prod(ur[i], Epi[c]), ff_prod(ui[i], Epr[c]));
+        Epr[c] = ff_sel(inG[i], tr, Epr[c]);
+        Epi[c] = ff_sel(inG[i], ti, Epi[c]);
       }
     }
 #pragma unroll
     for (int c = 0; c < ND; c++) {
-      Epr[c] = Ecr[c];
-      if (!REAL) Epi[c] = Eci[c];
+      const int par = gpar(c), i = gnode(c);
+      const ffl g = ff_sel(pk[0], qv[gms(c, 0)], ff_sel(pk[1], qv[gms(c, 1)], ff_sel(pk[2], qv[gms(c, 2)], qv[0])));
+      Epr[c] = ff_sel(inG[i], Epr[c], par < 0 ? zero : Epr[par < 0 ? 0 : par]);
+      acc_ff_add(Dr[c], ff_prod(Epr[c], g));
+      if (!REAL) {
+        Epi[c] = ff_sel(inG[i], Epi[c], par < 0 ? zero : Epi[par < 0 ? 0 : par]);
+        acc_ff_add(Di[c], ff_prod(Epi[c], g));
+      }
     }
   }
 #pragma unroll
