@@ -218,23 +218,30 @@ MF_D void smf_eigen(const double *v, double al, double lam[3], double fl[3], dou
     lam[i] = E.lam[i];
 #pragma unroll
     for (int j = 0; j < 3; j++) V[i][j] = E.V[i][j];
-    fl[i] = smf_fun<KIND>(lam[i], al);
+    if (KIND != LOG) fl[i] = smf_fun<KIND>(lam[i], al);
   }
-  if (KIND == LOG) {  // near m: log(m sig) + log1p(x / m), x from the deviator
-    double lms = log(E.m * E.sig);
+  if (KIND == LOG) {
+    // near m (|x| <= m / 2, x = lam - m from the deviator): log(m sig) + log1p(x / m); else log(lam).  One logarithm
+    // per eigenvalue serves both: u = 1 + x / m near m (then log1p(x / m) = log(u) (x / m) / (u - 1), exact u - 1 by
+    // Sterbenz, x / m where u rounds to 1 -- Goldberg's form of log1p, a few ulps), u = lam otherwise.
+    const double lms = log(E.m * E.sig);
 #pragma unroll
-    for (int i = 0; i < 3; i++)
-      fl[i] = sel(fabs(E.xd[i]) <= 0.5 * E.m, lms + log1p(E.xd[i] / E.m), fl[i]);
+    for (int i = 0; i < 3; i++) {
+      const bool near = fabs(E.xd[i]) <= 0.5 * E.m;
+      const double y = E.xd[i] / E.m, u = near ? 1.0 + y : lam[i], L = log(u), um1 = u - 1.0;
+      fl[i] = near ? lms + (um1 == 0.0 ? y : L * (y / um1)) : L;
+    }
   }
 }
 
 // ---- first divided differences f[a, b] (f[a, a] = f'(a)) in forms stable for close arguments
 // exp: e^max(a, b) (1 - e^-d) / d, d = |a - b| (no overflow, no cancellation)
-// log: with s = (a + b) / 2, z = (a - b) / (a + b): log a - log b = 2 atanh z, so f[a, b] = atanh(z) / (z s); its
-//      series (1 + z^2/3 + z^4/5 + z^6/7) / s for |z| < 1e-3, and the plain quotient (fa - fb) / (a - b) of the
-//      logarithms already at hand for |z| >= 0.5 (a / b >= 3: their difference is >= log 3, so it is as accurate as
-//      log a - log b evaluated anew, and a warp whose lanes split between this and the atanh form pays two
-//      subtractions and a division for it instead of two more logarithms)
+// log: with s = (a + b) / 2, z = (a - b) / (a + b): log a - log b = 2 atanh z, so f[a, b] = atanh(z) / (z s) for
+//      |z| < 0.5 (1 / s at z = 0; near 0 the ratio atanh(z) / z = 1 + z^2 / 3 + ... hardly depends on z, so the
+//      rounding of z does not reach it and no separate series is needed), and the plain quotient (fa - fb) / (a - b)
+//      of the logarithms already at hand for |z| >= 0.5 (a / b >= 3: their difference is >= log 3, so it is as
+//      accurate as log a - log b evaluated anew).  Two forms instead of three: the lanes of a warp split between them,
+//      and the warp pays for every form one of its lanes takes.
 // sqrt: 1 / (sqrt a + sqrt b) (arguments clamped at 0: PSD round-off)
 // powers: with s the mean and z = (a - b) / (2 s): a^al - b^al = s^al ((1 + z)^al - (1 - z)^al), so
 //      f[a, b] = s^(al - 1) (expm1(al log1p z) - expm1(al log1p(-z))) / (2 z) for 0 < |z| < 0.5, al s^(al - 1) at
@@ -249,11 +256,8 @@ MF_D double smf_dd1(double a, double b, double fa, double fb, const SmfCoef &C) 
   if (KIND == LOG) {
     const double s = 0.5 * (a + b), z = (a - b) / (a + b), az = fabs(z);
     if (az >= 0.5) return (fa - fb) / (a - b);
-    if (az < 1e-3) {
-      const double z2 = z * z;
-      return (1.0 + z2 / 3.0 + z2 * z2 / 5.0 + z2 * z2 * z2 / 7.0) / s;
-    }
-    return atanh(z) / z / s;
+    const double zs = z != 0.0 ? z : 0.5;
+    return (z != 0.0 ? atanh(zs) / zs : 1.0) / s;
   }
   a = a > 0 ? a : 0.0;
   b = b > 0 ? b : 0.0;
