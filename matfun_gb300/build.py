@@ -151,14 +151,20 @@ def reference_root():
 
 def build_reference_oracle(ref):
     """the reference's own CPU library (oracle/_ref/libmatfun_ref.so) and its CUDA kernels as an sm_103a cubin
-    (oracle/_ref/matfun_cuda_ref.cubin), built from the reference tree `ref` where it lies; None when `ref` is not
-    a reference tree"""
-    if not _is_reference_tree(ref):
+    (oracle/_ref/matfun_cuda_ref.cubin), built from the reference tree `ref` where it lies; the library's sources are
+    also staged into oracle/_ref/src (never committed) so that a host without the tree builds the same library from
+    them.  On such a host (`ref` is not a reference tree) the library is built from the staged sources, the cubin
+    having travelled with the working tree.  None when neither is present."""
+    staged = os.path.join(REF_OUT, "src")
+    mk = ["make", "-s", "-f", os.path.join("oracle", "Makefile.ref")]
+    if _is_reference_tree(ref):
+        subprocess.run(mk + [f"REF={ref}", "all", "stage"], cwd=ROOT, check=True)
+        with open(REF_ROOT_FILE, "w") as f:
+            f.write(os.path.abspath(ref) + "\n")
+    elif _is_reference_tree(staged):
+        subprocess.run(mk + [f"REF={staged}", "lib"], cwd=ROOT, check=True)
+    else:
         return None
-    subprocess.run(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={ref}", "all"], cwd=ROOT,
-                   check=True)
-    with open(REF_ROOT_FILE, "w") as f:
-        f.write(os.path.abspath(ref) + "\n")
     return os.path.join(REF_OUT, "libmatfun_ref.so")
 
 
