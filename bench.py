@@ -457,10 +457,14 @@ def mixed_sweep(lib, args, dev, pk):
     per batch and per matrix"""
     import torch
 
+    from matfun_gb300 import autotune
     from matfun_gb300 import workloads as w
     n = args.mixed_n
     xh = w.c2_smf_spd(n, seed=2)
     x32 = torch.from_numpy(xh)
+    xd = x32.to(dev)
+    path, path_ms = autotune.tune_smf_f32(xd, save=False)  # the store path of orders 1 and 2, timed on log
+    del xd
     rng = np.random.default_rng(2)
     rows = []
     for name, kind in (("exp", 0), ("log", 1), ("sqrt", 3), ("pow", 2)):
@@ -481,7 +485,10 @@ def mixed_sweep(lib, args, dev, pk):
     return {"workload": f"C2: smf Voigt, n={n} SPD, condition log-uniform [1,1e6], smallest gap log-uniform "
                         "[1e-12,1], FP32 storage; every kind and order; errors of the FP32 results against the FP64 "
                         "path on the same values (per batch, and per matrix where its outputs fit FP32's range)",
-            "err_sample": ns, "rows": rows}
+            "err_sample": ns, "rows": rows,
+            "store_path": {"chosen": {str(o): autotune.SMF_F32_PATHS[p] for o, p in path.items()},
+                           "log_ms": {str(o): {autotune.SMF_F32_PATHS[p]: round(t, 4) for p, t in d.items()}
+                                      for o, d in path_ms.items()}}}
 
 
 def mixed_gmf(lib, args, dev, pk, cpu_log):

@@ -45,6 +45,7 @@ SIGNATURES = {
     "matfun_cuda_batched_free": (ctypes.c_int, [ctypes.c_void_p]),
     "matfun_cuda_batched_tune": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "matfun_cuda_batched_tune_tiles": (ctypes.c_int, [ctypes.c_int]),
+    "matfun_cuda_smf_f32_tune": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "matfun_cuda_version": (ctypes.c_char_p, []),
 }
 

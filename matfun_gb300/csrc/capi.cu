@@ -1,6 +1,7 @@
 // capi.cu -- the C ABI of include/matfun_cuda.h: argument checks, normalisation of kind / alpha, grid limits and
 // return codes as the reference's launchers (cuda/src/matfun_cuda.cu:119-141 launch, :169-190 glaunch), then the
 // launch of the per-kind kernels (smf_<kind>.cu, gmf_<kind>.cu).
+#include <atomic>
 #include <climits>
 #include <cstdint>
 
@@ -116,6 +117,16 @@ int smf_call_f32(int kind, double alpha, int64_t n, const float *x, bool mat, fl
 extern "C" int smf_cuda_eval_f32(int kind, double alpha, int64_t n, const float *v, float *F, float *J, float *H,
                                  void *stream) {
   return smf_call_f32(kind, alpha, n, v, false, F, J, H, stream);
+}
+
+namespace mf {
+std::atomic<int> smf_voigt_variant[2] = {{2}, {2}};  // the store path of the FP32 Voigt kernels at orders 1, 2
+}
+
+extern "C" int matfun_cuda_smf_f32_tune(int order, int variant) {
+  if (order < 1 || order > 2 || variant < 0 || variant > 2) return -1;
+  mf::smf_voigt_variant[order - 1] = variant;
+  return 0;
 }
 
 extern "C" int smf_cuda_eval_matrix_f32(int kind, double alpha, int64_t n, const float *A, float *F, float *J,

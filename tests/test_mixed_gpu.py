@@ -202,6 +202,48 @@ def test_gmf_adjoint_f32_random_general_per_matrix(kind, alpha, name):
     assert max(pm) <= GMF_TOL
 
 
+@pytest.mark.parametrize("kind,alpha", [(1, 0.0), (2, 0.7)])
+@pytest.mark.parametrize("order", [1, 2])
+def test_smf_mixed_voigt_store_paths(kind, alpha, order):
+    """Voigt orders 1 and 2 write J and H rows by per-entry stores (path 0) or through the TMA unit in boxes of 128-
+    or 64-byte rows (paths 1, 2; J and H 16-byte aligned, else path 0 runs).  On batch tails around the 32 matrices
+    of a warp and the 64 of a CTA every path gives the rows of path 0 to rounding, with the same NaN positions, and
+    none writes past row n; path 2 on J and H one float past an aligned address falls back to path 0."""
+    import torch
+
+    import matfun_gb300
+    from matfun_gb300 import workloads as w
+    lib = matfun_gb300.load()
+    cols = [6, 36, 216][:order + 1]
+
+    def run(X, path, shift):
+        n = len(X)
+        assert lib.matfun_cuda_smf_f32_tune(order, path) == 0
+        dX = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+        bufs = [torch.full(((n + 3) * c + 4,), 7.0, dtype=torch.float32, device="cuda") for c in cols]
+        views = [b[shift: shift + (n + 3) * c].view(n + 3, c) for b, c in zip(bufs, cols)]
+        p = [v.data_ptr() for v in views] + [None] * (2 - order)
+        assert (p[1] % 16 == 0) == (shift == 0)
+        assert lib.smf_cuda_eval_f32(kind, alpha, n, dX.data_ptr(), *p, None) == 0
+        torch.cuda.synchronize()
+        for v in views:
+            assert bool((v[n:] == 7.0).all()), f"n={n}, path {path}: rows past n written"
+        return [v[:n].double().cpu().numpy() for v in views]
+
+    try:
+        for n in (1, 7, 31, 32, 33, 63, 64, 65, 97, 129, 1000):
+            X = w.c2_smf_spd(n, seed=40 + n)
+            if n > 5:
+                X[5, 3] = np.nan  # a NaN input row
+            ref = run(X, 0, 0)
+            for path, shift in ((1, 0), (2, 0), (2, 1)):
+                for a, b in zip(run(X, path, shift), ref):
+                    assert np.array_equal(np.isnan(a), np.isnan(b)), f"n={n}, path {path}"
+                    assert maxrel(a, b) <= 1e-6, f"n={n}, path {path}"
+    finally:
+        lib.matfun_cuda_smf_f32_tune(order, 2)
+
+
 @pytest.mark.parametrize("scale,order", [(1e-30, 0), (1e30, 0), (2.0 ** -20, 2), (2.0 ** 40, 2)])
 def test_smf_mixed_extreme_scales(scale, order):
     """the float-float eigensystem scales by a power of two first: matrices of 1e-30 and 1e30 (FP32 range) keep the
