@@ -20,12 +20,19 @@
 namespace mf {
 
 constexpr double G_RHO = 0.7, G_R_EXP = 4.0, G_RHO_POLE = 0.6;  // gmf_kernel.hpp:30
+// log forms its series groups only within 0.5 of the centre instead of the reference's 0.7: nodes spread wider are
+// taken as a closer pair group and a single node, or as single nodes (dd_three_single, the residues), so that the
+// longest series (40-100 terms at radii 0.5-0.7) are not run: C1 log order 2 12.03 -> 11.37 ms on GB300.  Measured
+// against the oracle on the host build of this header: C1 within 5e-14 per matrix, the stress sets within 8e-15 per
+// call, every golden case of the reference within 0.17 of its tolerance (the same as at 0.7).  Powers keep 0.7:
+// there the single-node forms lost up to 7e-11 per matrix at 0.5.
+constexpr double G_RHO_LOG = 0.5;
 constexpr int G_KMAX = 200;                                      // gmf_kernel.hpp:31
 
 // launch constants of the gmf kernels (host-computed once per call)
 struct GmfCoef {
   double al;              // exponent (pow; sqrt arrives as pow 0.5), 0 otherwise
-  double rho_f;           // group radius ratio: 0.7, or min(0.7, 3 / al) for pow
+  double rho_f;           // group radius ratio: 0.5 for log, 0.7 or min(0.7, 3 / al) for pow
   double bh[3], bl[3];    // al - k split exactly (k = 0, 1, 2)
   double bt[G_KMAX];      // series coefficients b_j of f(c (1 + u)) (gmf_kernel.hpp:48-53)
   float lterm[G_KMAX];    // log2(|b_(n+k)| C(k + n, n)), n = 3 (order + 1) - 1: the term bound of gmf_kernel.hpp:73-97
@@ -39,7 +46,7 @@ struct GmfCoef {
 // recurrence of gmf_kernel.hpp:84, as log2 values)
 inline void gmf_coef(int kind, double al, int order, GmfCoef &C) {
   C.al = al;
-  C.rho_f = (kind == POW && 3.0 / al < G_RHO) ? 3.0 / al : G_RHO;
+  C.rho_f = kind == LOG ? G_RHO_LOG : ((kind == POW && 3.0 / al < G_RHO) ? 3.0 / al : G_RHO);
   for (int k = 0; k < 3; k++) {
     const double bh = al - k, bb = bh - al;
     C.bh[k] = bh;

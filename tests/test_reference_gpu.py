@@ -74,8 +74,8 @@ def _time(fn, reps):
 def test_faster_than_reference_kernels():
     """the measured speed against the reference's kernels on the same GB300 and buffers (CUDA events, printed per
     kind and order): gmf at n = 2^20 on the C1 groups, smf log (Voigt) at n = 65536 on the C0 matrices.  Measured:
-    gmf log order 2 3.56x, smf log order 2 1.51x; asserted with a margin for the run-to-run spread of a shared GPU:
-    gmf log order 2 >= 3x, smf log order 2 >= 1.4x, every other case faster than the reference"""
+    gmf log order 2 3.8x, smf log order 2 1.70x; asserted with a margin for the run-to-run spread of a shared GPU:
+    gmf log order 2 >= 3x, smf log order 2 >= 1.5x, every other case faster than the reference"""
     import torch
 
     import matfun_gb300
@@ -102,5 +102,5 @@ def test_faster_than_reference_kernels():
         tr = _time(lambda: ref.refgpu_smf(1, 0.0, order, m, V.data_ptr(), *p, None), 20)
         speed[("smf", "log", order)] = tr / to
         print(f"smf log Voigt order {order} n=65536: ours {to:7.3f} ms, reference kernel {tr:7.3f} ms, {tr / to:.2f}x")
-    assert speed[("gmf", "log", 2)] >= 3.0 and speed[("smf", "log", 2)] >= 1.4, speed
+    assert speed[("gmf", "log", 2)] >= 3.0 and speed[("smf", "log", 2)] >= 1.5, speed
     assert min(speed.values()) > 1.0, speed
