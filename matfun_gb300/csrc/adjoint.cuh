@@ -94,7 +94,7 @@ cudaError_t gmf_adjoint_t(double al, int64_t n, const T *A, const T *W, const T 
                           cudaStream_t st) {
   const int order = HWV ? 2 : 1;
   GmfCoef C;
-  gmf_coef(KIND, al, order, C);
+  gmf_coef(KIND, al, order, C, sizeof(T) == 4);
   const unsigned blocks = (unsigned)((n + GADJ_TPB - 1) / GADJ_TPB);
   int *ord = nullptr;
   if ((KIND != EXP) & (n >= GMF_SORT_MIN) & (n <= INT_MAX)) {

@@ -226,7 +226,7 @@ int build_table(const mf_request *req, int count, Table &T) {
                   r.order >= 2 ? r.H : nullptr, 0, nullptr, r.family == 2 ? BT_TPB : g_tune.smf_tile};
     if (r.family == 2) {
       GmfCoef C;
-      gmf_coef(kind, al, r.order, C);
+      gmf_coef(kind, al, r.order, C, r.dtype != 0);
       it.coef.resize(sizeof C);
       std::memcpy(it.coef.data(), &C, sizeof C);
     } else if (r.dtype == 0) {

@@ -27,6 +27,13 @@ constexpr double G_RHO = 0.7, G_R_EXP = 4.0, G_RHO_POLE = 0.6;  // gmf_kernel.hp
 // call, every golden case of the reference within 0.17 of its tolerance (the same as at 0.7).  Powers keep 0.7:
 // there the single-node forms lost up to 7e-11 per matrix at 0.5.
 constexpr double G_RHO_LOG = 0.5;
+// The FP32-storage kernels (results to about 1e-7) take their series groups only within 0.35 of the centre and end
+// their series 2^-44 below the largest term instead of 1e-17: on GB300 C1 order 2 log 7.40 -> 6.92 ms, sqrt 10.59 ->
+// 9.77, pow 0.3 11.84 -> 10.90 (exp unchanged, so it keeps its radius of 4), with the per-matrix errors of 6000
+// random general matrices unchanged (3.5e-7 at most).  At 0.25 with a stop at 2^-34 the single-node forms of
+// near-defective matrices lost up to 3e-4.
+constexpr double G_RHO_F32 = 0.35, G_R_EXP_F32 = 4.0;
+constexpr float G_LSTOP = -56.5237f - 0.05f, G_LSTOP_F32 = -44.f;  // log2(1e-17) less a margin; 2^-44
 constexpr int G_KMAX = 200;                                      // gmf_kernel.hpp:31
 
 // launch constants of the gmf kernels (host-computed once per call)
@@ -40,13 +47,22 @@ struct GmfCoef {
   int ffser;              // 1: the group series may run on the FP32 pipe (every |bth[j]| <= 2^100)
   int tsh;                // bth, btl hold b_j 2^(tsh j) and group_tail takes the offsets times 2^-tsh (exp: 2, so
                           // that 4^j / j! stays in FP32's range; log, pow: 0)
+  double rexp;            // exp: the group radius (offsets from the group's centre)
+  float lstop;            // log2 of the last series term's size relative to the largest
 };
 
 // host: launch constants (series coefficients gmf_kernel.hpp:48-53; the binomial factors of the term bound by the
-// recurrence of gmf_kernel.hpp:84, as log2 values)
-inline void gmf_coef(int kind, double al, int order, GmfCoef &C) {
+// recurrence of gmf_kernel.hpp:84, as log2 values); fp32: those of the FP32-storage kernels
+inline void gmf_coef(int kind, double al, int order, GmfCoef &C, bool fp32 = false) {
   C.al = al;
   C.rho_f = kind == LOG ? G_RHO_LOG : ((kind == POW && 3.0 / al < G_RHO) ? 3.0 / al : G_RHO);
+  C.rexp = G_R_EXP;
+  C.lstop = G_LSTOP;
+  if (fp32) {
+    C.rho_f = C.rho_f < G_RHO_F32 ? C.rho_f : G_RHO_F32;
+    C.rexp = G_R_EXP_F32;
+    C.lstop = G_LSTOP_F32;
+  }
   for (int k = 0; k < 3; k++) {
     const double bh = al - k, bb = bh - al;
     C.bh[k] = bh;
@@ -97,7 +113,8 @@ MF_D constexpr int gpos3(int j, int k, int l) {
 }
 
 // number of series terms (gmf_kernel.hpp:73-97): the group series needs terms until |b_(n+k)| C(k+n, n) r^k drops
-// below 1e-17 of the largest, the pole series until C(k+2, 2) q^k <= 1e-17.  Evaluated on log2 values in FP32 (the
+// below 1e-17 of the largest, the pole series until C(k+2, 2) q^k <= 1e-17 (2^-44 for the FP32-storage kernels,
+// C.lstop).  Evaluated on log2 values in FP32 (the
 // FP64 pipe is the bottleneck of this kernel) with a threshold 2^-0.05 below 1e-17, so that the count is never
 // smaller than the FP64 bound's; one term more changes a result by less than 1e-17 relative.
 //
@@ -106,7 +123,7 @@ MF_D constexpr int gpos3(int j, int k, int l) {
 // rounding errors (2^-48 and 2^-24 of the term) then stay below 2^-54 of the largest term, under the FP64 rounding of
 // the leading terms (2^-53 of the largest).
 MF_D int nterms(const GmfCoef &C, int n, double r, double q, int &j1, int &j2) {
-  constexpr float L17 = -56.5237f - 0.05f;  // log2(1e-17) less a margin
+  const float L17 = C.lstop;  // log2(1e-17) less a margin (FP64 results), 2^-34 (FP32 results)
   int M = 1, k1 = G_KMAX, k2 = G_KMAX;
   if (r > 0) {
     const float lr = log2f((float)r);
@@ -701,7 +718,7 @@ MF_D void gmf_classify_from(const double *a, const cx *xr, const GmfCoef &C, Gmf
   // real or conjugate) within reach whose radius is <= 0.6 of its distance to the third node (the series' pole), else
   // none
   auto reach = [&](double c, double R) -> bool {
-    if (KIND == EXP) return R <= G_R_EXP;
+    if (KIND == EXP) return R <= C.rexp;
     return (m + c > 0) & (R <= C.rho_f * (m + c));
   };
   const bool cplx = nd[1].x.im != 0 || nd[0].x.im != 0;
@@ -804,7 +821,7 @@ MF_D void gmf_classify_from(const double *a, const cx *xr, const GmfCoef &C, Gmf
   for (int i = 0; i < 3; i++) rr = tmax(rr, u[i].im == 0 ? fabs(u[i].re) : cabs_s(u[i]));
   const bool anypk = pk[0] | pk[1] | pk[2];
   const double rq = (anypk & (rr * fabs(iap) <= 1.0)) ? rr * fabs(iap) : 0.0;
-  rr = (hasg & (rr <= G_R_EXP + 0.5)) ? rr : 0.0;
+  rr = (hasg & (rr <= C.rexp + 0.5)) ? rr : 0.0;
   int j1 = G_KMAX, j2 = G_KMAX;
   St.K = hasg ? nterms(C, 3 * (ORDER + 1) - 1, rr, rq, j1, j2) : 0;
   // the float-float / FP32 tail of the series: groups without a pole node, coefficients within FP32's range

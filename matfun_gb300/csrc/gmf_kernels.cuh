@@ -641,7 +641,7 @@ template <int KIND, typename T = double>
 cudaError_t gmf_launch_t(double al, int64_t n, const T *A, T *F, T *J, T *H, cudaStream_t st, bool reorder = true) {
   const int order = H ? 2 : (J ? 1 : 0);
   GmfCoef C;
-  gmf_coef(KIND, al, order, C);
+  gmf_coef(KIND, al, order, C, sizeof(T) == 4);
   const unsigned blocks = (unsigned)((n + GMF_TPB - 1) / GMF_TPB);
   return gmf_launch_kind<KIND, T>(order, st, blocks, n, A, F, J, H, C, reorder);
 }

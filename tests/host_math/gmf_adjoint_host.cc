@@ -15,7 +15,7 @@ namespace {
 template <int KIND, int ORDER, typename T>
 void run(double al, int64_t n, const T *A, const T *W, const T *V, T *F, T *Abar, T *JV, T *HWV) {
   GmfCoef C;
-  gmf_coef(KIND, al, ORDER, C);
+  gmf_coef(KIND, al, ORDER, C, sizeof(T) == 4);  // (the launch constants the device launch of this storage type takes)
   static GadjSmemT<1> S;
   for (int64_t i = 0; i < n; i++) gmf_adjoint_tile<KIND, ORDER, T, 1>(i, 1, A, W, V, F, Abar, JV, HWV, C, nullptr, S);
 }

@@ -5,7 +5,8 @@
 //   J_abcd = sc1 T4[ac, db],  H_abcdef = sc2 (T6[ac, de, fb] + T6[ae, fc, db]),  r_0 = I,
 //   T4[x, y] = sum_mn r_m[x] D2'_mn r_n[y],  T6[x, y, z] = sum_mnp r_m[x] r_n[y] r_p[z] D3'_mnp.
 // The warp votes of the series take a warp of one lane (host_intrinsics.h).  ff = 1 runs the float-float group series
-// of the FP32-storage kernels (gmf_finish<..., true>), ff = 0 the FP64 / split series of the FP64 kernels.
+// of the FP32-storage kernels (gmf_finish<..., true>), ff = 2 the same with those kernels' launch constants (their
+// group radii and series stop, gmf_coef fp32), ff = 0 the FP64 / split series of the FP64 kernels.
 #include "host_intrinsics.h"
 #include "../../matfun_gb300/csrc/gmf_device.cuh"
 
@@ -14,9 +15,10 @@ using namespace mf;
 namespace {
 
 template <int KIND, int ORDER, bool FF>
-void all(double al, int64_t n, const double *A, double *F, double *R12, double *D2, double *D3, double *sc) {
+void all(double al, int64_t n, const double *A, double *F, double *R12, double *D2, double *D3, double *sc,
+         bool f32coef) {
   GmfCoef C;
-  gmf_coef(KIND, al, ORDER, C);
+  gmf_coef(KIND, al, ORDER, C, f32coef);
   for (int64_t i = 0; i < n; i++) {
     GmfState St;
     gmf_classify<KIND, ORDER>(A + 9 * i, C, St);
@@ -36,17 +38,17 @@ void all(double al, int64_t n, const double *A, double *F, double *R12, double *
 
 template <int KIND, bool FF>
 void by_order(int order, double al, int64_t n, const double *A, double *F, double *R12, double *D2, double *D3,
-              double *sc) {
-  if (order == 2) all<KIND, 2, FF>(al, n, A, F, R12, D2, D3, sc);
-  else if (order == 1) all<KIND, 1, FF>(al, n, A, F, R12, D2, D3, sc);
-  else all<KIND, 0, FF>(al, n, A, F, R12, D2, D3, sc);
+              double *sc, bool f32coef) {
+  if (order == 2) all<KIND, 2, FF>(al, n, A, F, R12, D2, D3, sc, f32coef);
+  else if (order == 1) all<KIND, 1, FF>(al, n, A, F, R12, D2, D3, sc, f32coef);
+  else all<KIND, 0, FF>(al, n, A, F, R12, D2, D3, sc, f32coef);
 }
 
 template <int KIND>
 void by_ff(int ff, int order, double al, int64_t n, const double *A, double *F, double *R12, double *D2, double *D3,
            double *sc) {
-  if (ff) by_order<KIND, true>(order, al, n, A, F, R12, D2, D3, sc);
-  else by_order<KIND, false>(order, al, n, A, F, R12, D2, D3, sc);
+  if (ff) by_order<KIND, true>(order, al, n, A, F, R12, D2, D3, sc, ff == 2);
+  else by_order<KIND, false>(order, al, n, A, F, R12, D2, D3, sc, false);
 }
 
 }  // namespace

@@ -185,6 +185,31 @@ def test_ff_series_stress(lib, kind, alpha, name):
         assert max(errs) <= 1e-10, (sname, errs)
 
 
+@pytest.mark.parametrize("kind,alpha,name", KINDS + [(2, 2.5, "pow 2.5")])
+def test_ff_series_fp32_constants(lib, kind, alpha, name):
+    """the record with the FP32-storage kernels' launch constants (series groups within 0.35 of the centre, series
+    ended 2^-44 below the largest term; gmf_coef fp32) on C1, the stress sets and the FP32 golden inputs, all rounded
+    to FP32: within 1e-8 of the oracle per call (the FP32 rounding of the record that follows is 6e-8), NaN exactly
+    where the oracle has NaN"""
+    from matfun_gb300 import workloads as w
+    sets = {"C1": w.c1_gmf_groups(2000, seed=9).reshape(-1, 9)}
+    sets.update({k: v.reshape(-1, 9) for k, v in stress_sets(200).items()})
+    g = np.load(os.path.join(HERE, "golden", "cases_gmf_f32.npz"))
+    sel = (g["kind"] == kind) & ((kind != 2) | (g["alpha"] == alpha))
+    if sel.any():
+        sets["golden f32"] = g["x"][sel]
+    for sname, A in sets.items():
+        X = np.asarray(A, dtype=np.float32).astype(np.float64)
+        ref = ol.call(ol.oracle(), "gmf_eval", kind, alpha, X, 2, 9)[1:]
+        got = contract(2, *record(lib, kind, alpha, 2, 2, X))
+        for gg, r, out in zip(got, ref, "FJH"):
+            assert np.array_equal(np.isnan(gg), np.isnan(r)), (sname, out)
+        if kind == 0 and sname == "scale 2^60":  # exp overflows there in any precision
+            continue
+        errs = [maxrel(gg, r) for gg, r in zip(got, ref)]
+        assert max(errs) <= 1e-8, (sname, errs)
+
+
 @pytest.fixture(scope="module")
 def adj(tmp_path_factory):
     out = build_host_math("gmf_adjoint_host.cc", tmp_path_factory.mktemp("host_math"), "-O1")
