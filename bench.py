@@ -53,47 +53,47 @@ def io_bytes(fam, order, elem=8):
 # matrices of each launch (profiles/pipe_counts_all_configs.md).  They turn the measured time of a configuration into
 # its FP64 / FP32 pipe fraction.  None: the kernels execute no instruction of that pipe.
 PIPE_FLOPS = {
-    "gmf/log/2/f64": {"fp64": 5586, "fp32": 12353},
-    "gmf/exp/2/f64": {"fp64": 4911, "fp32": 6229},
-    "gmf/sqrt/2/f64": {"fp64": 7872, "fp32": 12200},
-    "gmf/log/2/f32": {"fp64": 1558, "fp32": 41877},
-    "gmf/exp/2/f32": {"fp64": 2640, "fp32": 9914},
-    "gmf/sqrt/2/f32": {"fp64": 3820, "fp32": 41338},
-    "gmf/pow0.3/2/f32": {"fp64": 4537, "fp32": 41555},
-    "gmf/log/tangent/f64": {"fp64": 7809, "fp32": 12401},
-    "smf/log/2/f64/c0": {"fp64": 3000, "fp32": 90},
+    "gmf/log/2/f64": {"fp64": 5438, "fp32": 7486},
+    "gmf/exp/2/f64": {"fp64": 4912, "fp32": 6229},
+    "gmf/sqrt/2/f64": {"fp64": 7873, "fp32": 12200},
+    "gmf/log/2/f32": {"fp64": 1687, "fp32": 20409},
+    "gmf/exp/2/f32": {"fp64": 2641, "fp32": 9646},
+    "gmf/sqrt/2/f32": {"fp64": 3804, "fp32": 20265},
+    "gmf/pow0.3/2/f32": {"fp64": 4468, "fp32": 20323},
+    "gmf/log/tangent/f64": {"fp64": 7661, "fp32": 7534},
+    "smf/log/2/f64/c0": {"fp64": 2877, "fp32": 90},
     "smf/exp/0/f32": {"fp64": None, "fp32": 1969},
     "smf/exp/0/f64": {"fp64": 701, "fp32": 14},
-    "smf/exp/1/f32": {"fp64": None, "fp32": 2402},
+    "smf/exp/1/f32": {"fp64": None, "fp32": 2378},
     "smf/exp/1/f64": {"fp64": 1104, "fp32": 20},
-    "smf/exp/2/f32": {"fp64": None, "fp32": 3786},
-    "smf/exp/2/f64": {"fp64": 2345, "fp32": 214},
+    "smf/exp/2/f32": {"fp64": None, "fp32": 3680},
+    "smf/exp/2/f64": {"fp64": 2348, "fp32": 214},
     "smf/log/0/f32": {"fp64": None, "fp32": 2229},
-    "smf/log/0/f64": {"fp64": 989, "fp32": 22},
-    "smf/log/1/f32": {"fp64": None, "fp32": 2764},
-    "smf/log/1/f64": {"fp64": 1589, "fp32": 41},
-    "smf/log/2/f32": {"fp64": None, "fp32": 4074},
-    "smf/log/2/f64": {"fp64": 3208, "fp32": 263},
+    "smf/log/0/f64": {"fp64": 882, "fp32": 22},
+    "smf/log/1/f32": {"fp64": None, "fp32": 2738},
+    "smf/log/1/f64": {"fp64": 1331, "fp32": 41},
+    "smf/log/2/f32": {"fp64": None, "fp32": 3968},
+    "smf/log/2/f64": {"fp64": 2956, "fp32": 263},
     "smf/sqrt/0/f32": {"fp64": None, "fp32": 1957},
     "smf/sqrt/0/f64": {"fp64": 653, "fp32": 14},
-    "smf/sqrt/1/f32": {"fp64": None, "fp32": 2306},
+    "smf/sqrt/1/f32": {"fp64": None, "fp32": 2282},
     "smf/sqrt/1/f64": {"fp64": 999, "fp32": 14},
-    "smf/sqrt/2/f32": {"fp64": None, "fp32": 3865},
-    "smf/sqrt/2/f64": {"fp64": 2720, "fp32": 256},
+    "smf/sqrt/2/f32": {"fp64": None, "fp32": 3759},
+    "smf/sqrt/2/f64": {"fp64": 2726, "fp32": 256},
     "smf/pow/0/f32": {"fp64": None, "fp32": 2116},
     "smf/pow/0/f64": {"fp64": 981, "fp32": 14},
-    "smf/pow/1/f32": {"fp64": None, "fp32": 2885},
+    "smf/pow/1/f32": {"fp64": None, "fp32": 2861},
     "smf/pow/1/f64": {"fp64": 1998, "fp32": 31},
-    "smf/pow/2/f32": {"fp64": None, "fp32": 4380},
-    "smf/pow/2/f64": {"fp64": 3720, "fp32": 273},
-    "smf/log/vjp/f64": {"fp64": 1509, "fp32": 49},
-    "smf/log/hvp/f64": {"fp64": 2299, "fp32": 90},
+    "smf/pow/2/f32": {"fp64": None, "fp32": 4274},
+    "smf/pow/2/f64": {"fp64": 3726, "fp32": 273},
+    "smf/log/vjp/f64": {"fp64": 1381, "fp32": 49},
+    "smf/log/hvp/f64": {"fp64": 2170, "fp32": 90},
     "smf/log/vjp/f32": {"fp64": None, "fp32": 2726},
     "smf/log/hvp/f32": {"fp64": None, "fp32": 3254},
-    "gmf/pow0.3/vjp/f64": {"fp64": 4287, "fp32": 10652},
-    "gmf/pow0.3/hvp/f64": {"fp64": 9066, "fp32": 24339},
-    "gmf/pow0.3/vjp/f32": {"fp64": 3241, "fp32": 29333},
-    "gmf/pow0.3/hvp/f32": {"fp64": 5012, "fp32": 72434},
+    "gmf/pow0.3/vjp/f64": {"fp64": 4288, "fp32": 10652},
+    "gmf/pow0.3/hvp/f64": {"fp64": 9067, "fp32": 24339},
+    "gmf/pow0.3/vjp/f32": {"fp64": 3263, "fp32": 11624},
+    "gmf/pow0.3/hvp/f32": {"fp64": 4874, "fp32": 29369},
 }
 
 
