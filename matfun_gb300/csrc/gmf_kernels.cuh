@@ -532,7 +532,12 @@ __global__ void __launch_bounds__(GKEY_TPB) gmf_key_kernel(int n, const T *__res
 #pragma unroll
     for (int k = 0; k < 9; k++) a[k] = (double)A[(int64_t)i * 9 + k];
     cx x[3];
-    const unsigned key = gmf_roots<KIND>(a, x) & (GKEY_BINS - 1);
+    const unsigned key0 = gmf_roots<KIND>(a, x) & (GKEY_BINS - 1);
+    // log, powers: the classes in descending key order, so that the launch starts with the complex pairs, the pairs
+    // refined from A and the branch-cut pairs and ends with the real spectra of the smallest spread (equal
+    // eigenvalues: the shortest work), and fewer SMs idle behind its last CTAs (C1 order 2: log 11.36 -> 10.84 ms,
+    // sqrt 15.54 -> 14.82 ms); exp keeps the ascending order (7.74 ms against 7.78 ms descending)
+    const unsigned key = KIND == EXP ? key0 : (GKEY_BINS - 1) - key0;
     keys[i] = (unsigned char)key;
     if (roots) {
 #pragma unroll
