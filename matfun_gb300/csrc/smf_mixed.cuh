@@ -107,9 +107,11 @@ __global__ void __launch_bounds__(SMFV_TPB, MINB)
   bufs[1] = bufs[0] + B::BYTES;
 
   // lanes past the end evaluate the identity (rows the TMA unit clips), so that the warp stays converged
-  const float eye[6] = {1.f, 1.f, 1.f, 0.f, 0.f, 0.f};
+  float xin[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) xin[k] = live ? sX[tid * 6 + k] : (k < 3 ? 1.f : 0.f);
   SmfInF in;
-  voigt_in_f(live ? sX + tid * 6 : eye, in);
+  voigt_in_f(xin, in);
   SmfSpecF Sp;
   smf_spectrum_f<KIND, false>(in, C, Sp);
   const float(&V)[3][3] = Sp.V;
