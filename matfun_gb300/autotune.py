@@ -84,7 +84,8 @@ def tune(reqs, reps=3, candidates=None, save=True):
 
 
 # ---- store path of the FP32 symmetric kernels (Voigt layout, orders 1 and 2)
-SMF_F32_PATHS = {0: "per-entry stores", 1: "TMA boxes of 32 rows x 128 B", 2: "TMA boxes of 32 rows x 64 B"}
+SMF_F32_PATHS = {0: "per-entry stores", 1: "TMA boxes of 32 rows x 128 B", 2: "TMA boxes of 32 rows x 64 B",
+                 3: "TMA boxes of 32 rows x 64 B, 14 CTAs per SM at order 2"}
 
 
 def tune_smf_f32(x, kind=1, alpha=0.0, reps=3, save=True):

@@ -120,11 +120,11 @@ extern "C" int smf_cuda_eval_f32(int kind, double alpha, int64_t n, const float 
 }
 
 namespace mf {
-std::atomic<int> smf_voigt_variant[2] = {{2}, {2}};  // the store path of the FP32 Voigt kernels at orders 1, 2
+std::atomic<int> smf_voigt_variant[2] = {{2}, {3}};  // the store path of the FP32 Voigt kernels at orders 1, 2
 }
 
 extern "C" int matfun_cuda_smf_f32_tune(int order, int variant) {
-  if (order < 1 || order > 2 || variant < 0 || variant > 2) return -1;
+  if (order < 1 || order > 2 || variant < 0 || variant > 3) return -1;
   mf::smf_voigt_variant[order - 1] = variant;
   return 0;
 }

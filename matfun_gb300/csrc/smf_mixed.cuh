@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(SMFV_TPB, MINB)
 
 // the store path of the Voigt FP32 kernels at orders 1-2: 0 = per-entry stores (smf_mixed_kernel), 1 = TMA boxes of
 // 128-byte rows (registers bounded for 8 CTAs per SM at order 2, 12 at order 1), 2 = TMA boxes of 64-byte rows
-// (12 CTAs per SM at order 2, 16 at order 1)
+// (12 CTAs per SM at order 2, 16 at order 1), 3 = TMA boxes of 64-byte rows at 14 CTAs per SM (order 2; 12 at order 1)
 extern std::atomic<int> smf_voigt_variant[2];  // (by order - 1)
 
 template <int KIND, int ORDER>
@@ -172,6 +172,7 @@ cudaError_t smfv_launch(int variant, int64_t n, const float *x, float *F, float 
   if (ORDER == 1) mH = mJ;
   const unsigned vb = (unsigned)((n + SMFV_TPB - 1) / SMFV_TPB);
   if (variant == 1) smf_mixed_voigt_kernel<KIND, ORDER, ORDER == 2 ? 8 : 12, 32><<<vb, SMFV_TPB, 0, st>>>(n, x, F, mJ, mH, C);
+  else if (variant == 3) smf_mixed_voigt_kernel<KIND, ORDER, ORDER == 2 ? 14 : 12, 16><<<vb, SMFV_TPB, 0, st>>>(n, x, F, mJ, mH, C);
   else smf_mixed_voigt_kernel<KIND, ORDER, ORDER == 2 ? 12 : 16, 16><<<vb, SMFV_TPB, 0, st>>>(n, x, F, mJ, mH, C);
   return cudaGetLastError();
 }

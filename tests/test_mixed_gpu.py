@@ -206,7 +206,7 @@ def test_gmf_adjoint_f32_random_general_per_matrix(kind, alpha, name):
 @pytest.mark.parametrize("order", [1, 2])
 def test_smf_mixed_voigt_store_paths(kind, alpha, order):
     """Voigt orders 1 and 2 write J and H rows by per-entry stores (path 0) or through the TMA unit in boxes of 128-
-    or 64-byte rows (paths 1, 2; J and H 16-byte aligned, else path 0 runs).  On batch tails around the 32 matrices
+    or 64-byte rows (paths 1-3; J and H 16-byte aligned, else path 0 runs).  On batch tails around the 32 matrices
     of a warp and the 64 of a CTA every path gives the rows of path 0 to rounding, with the same NaN positions, and
     none writes past row n; path 2 on J and H one float past an aligned address falls back to path 0."""
     import torch
@@ -236,12 +236,12 @@ def test_smf_mixed_voigt_store_paths(kind, alpha, order):
             if n > 5:
                 X[5, 3] = np.nan  # a NaN input row
             ref = run(X, 0, 0)
-            for path, shift in ((1, 0), (2, 0), (2, 1)):
+            for path, shift in ((1, 0), (2, 0), (3, 0), (2, 1)):
                 for a, b in zip(run(X, path, shift), ref):
                     assert np.array_equal(np.isnan(a), np.isnan(b)), f"n={n}, path {path}"
                     assert maxrel(a, b) <= 1e-6, f"n={n}, path {path}"
     finally:
-        lib.matfun_cuda_smf_f32_tune(order, 2)
+        lib.matfun_cuda_smf_f32_tune(order, 2 if order == 1 else 3)  # the library's defaults
 
 
 @pytest.mark.parametrize("scale,order", [(1e-30, 0), (1e30, 0), (2.0 ** -20, 2), (2.0 ** 40, 2)])
