@@ -1,5 +1,6 @@
-// smf_mixed.cuh -- mixed-precision symmetric family: the standalone kernel over the tile of smf_mixed_tile.cuh and
-// its launch.
+// smf_mixed.cuh -- mixed-precision symmetric family: the standalone kernels and their launch.  The matrix layout,
+// order 0 and store path 0 run the tile of smf_mixed_tile.cuh (per-entry stores of the expanded rows); the Voigt
+// layout at orders 1 and 2 runs smf_mixed_voigt_kernel below, whose J and H rows the TMA unit writes.
 #pragma once
 #include "smf_kernels.cuh"
 #include "smf_mixed_tile.cuh"

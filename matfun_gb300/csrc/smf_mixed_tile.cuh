@@ -1,6 +1,7 @@
 // smf_mixed_tile.cuh -- one tile of the mixed-precision symmetric family: coalesced FP32 input, the eigensystem and
-// divided differences of smf_mixed_math.cuh per thread, the J / H forms of smf_tile.cuh in FP32, coalesced FP32
-// output; the code a CTA of the standalone kernel and of the batched persistent kernel runs.
+// divided differences of smf_mixed_math.cuh per thread, the J / H forms of smf_tile.cuh in FP32 (smfx_jform,
+// smfx_hform, which the TMA-store kernel of smf_mixed.cuh shares), coalesced FP32 output; the code a CTA of the
+// standalone kernel and of the batched persistent kernel runs.
 #pragma once
 
 #include "smf_mixed_math.cuh"
