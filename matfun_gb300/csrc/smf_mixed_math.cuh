@@ -55,10 +55,11 @@ MF_D float dd1s_f(float a, float b, float dab, float fa, float fb, const SmfCoef
   if (KIND == LOG) {
     float s = 0.5f * (a + b), z = dab / (a + b), az = fabsf(z), z2 = z * z;
     if (az < 1e-3f) return (1.f + z2 / 3.f + z2 * z2 / 5.f + z2 * z2 * z2 / 7.f) / s;
-    // far pair: log(b / a) as log1p(dab / a), free of log |A| (whose ulp a difference of two logs would carry);
-    // a <= 0 keeps the difference of logs, with its infinities and NaNs
-    if (az >= 0.5f) return (a > 0.f ? log1pf(dab / a) : logf(b) - logf(a)) / dab;
-    return atanhf(z) / z / s;
+    // log(b / a) as log1p(dab / a), free of log |A| (whose ulp a difference of two logs would carry) and within a few
+    // ulp for every ratio, so one form serves the near and the far pairs (the FP64 form's atanh branch for
+    // 1e-3 <= |z| < 0.5 would be a third divergent path); a <= 0 keeps the difference of logs, with its infinities
+    // and NaNs
+    return (a > 0.f ? log1pf(dab / a) : logf(b) - logf(a)) / dab;
   }
   if (KIND == SQRT) return 1.f / (sqrtf(a) + sqrtf(b));
   float s = 0.5f * (a + b), ss = self(s > 0.f, s, 1.f);
