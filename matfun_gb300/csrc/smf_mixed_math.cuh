@@ -61,7 +61,7 @@ MF_D float dd1s_f(float a, float b, float dab, float fa, float fb, const SmfCoef
     // and NaNs
     return (a > 0.f ? log1pf(dab / a) : logf(b) - logf(a)) / dab;
   }
-  if (KIND == SQRT) return 1.f / (sqrtf(a) + sqrtf(b));
+  if (KIND == SQRT) return 1.f / (fa + fb);  // (fa, fb: the square roots of a, b >= 0)
   float s = 0.5f * (a + b), ss = self(s > 0.f, s, 1.f);
   float z = dab / (2.f * ss), az = fabsf(z);
   bool zero = az == 0.f, near = !zero & (az < 0.5f);
@@ -75,7 +75,7 @@ MF_D float deriv_f(float x, float fx, const SmfCoefF &C) {
   if (KIND == EXP) return fx;
   if (KIND == LOG) return 1.f / x;
   float xf = self(x > 0.f, x, 0.f);
-  if (KIND == SQRT) return 1.f / (2.f * sqrtf(xf));
+  if (KIND == SQRT) return 1.f / (2.f * fx);  // (fx = sqrt(x), x >= 0)
   return xf > 0.f ? C.al * powf(xf, C.alm1) : C.al * C.zp1;
 }
 
@@ -457,6 +457,22 @@ MF_D void smf_dm_f(const SmfSpecF &Sp, const SmfCoefF &C, float Dm[3][3]) {
 // second divided differences D2_ijl = f[l_i, l_j, l_l] (symmetric) in FP32
 template <int KIND>
 MF_D void smf_d2_f(const SmfSpecF &Sp, const float Dm[3][3], const SmfCoefF &C, float D2[3][3][3]) {
+  if (KIND == SQRT) {
+    // sqrt: f[a, b, c] = -1 / ((sa + sb)(sa + sc)(sb + sc)) with s = sqrt, exactly (f''(a) / 2 = -1 / (8 a^(3/2))
+    // where points coincide): sums of non-negative terms, free of cancellation at every spacing, so neither the
+    // cluster series nor the difference formula is needed (a zero eigenvalue pair gives -inf, as f''(0) / 2)
+    const float *sq = Sp.fl;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = i; j < 3; j++)
+#pragma unroll
+        for (int l = j; l < 3; l++) {
+          const float d = -1.f / ((sq[i] + sq[j]) * (sq[i] + sq[l]) * (sq[j] + sq[l]));
+          D2[i][j][l] = D2[i][l][j] = D2[j][i][l] = D2[j][l][i] = D2[l][i][j] = D2[l][j][i] = d;
+        }
+    return;
+  }
   const float dd[3][3] = {{0.f, Sp.d10, Sp.d20}, {0.f, 0.f, Sp.d21}, {0.f, 0.f, 0.f}};
 #pragma unroll
   for (int i = 0; i < 3; i++)
