@@ -27,11 +27,18 @@ namespace mf {
 constexpr int DD2_TERMS_F = 16, DD2_TERMS_F_POW = 30;
 constexpr double DD2_TAU_F_POW = 0.5;
 
+constexpr int G1_TERMS_F = 16;  // terms of the series of g(z) below
+
 struct SmfCoefF {
   float al, alm1;   // exponent and exponent - 1
   float zp1, z2;    // 0^(al - 1), f''(0)/2 for powers
   float tau;        // cluster radius of the second divided difference
   float c2[DD2_TERMS];
+  // powers, f[a, b] = s^(al - 1) g(z) for s = (a + b) / 2, z = (b - a) / (2 s), |z| < 1/2:
+  // g(z) = ((1 + z)^al - (1 - z)^al) / (2 z) = sum_m binom(al, 2m + 1) z^(2m); g1ser = 1 where that series, with
+  // G1_TERMS_F terms, is summed without cancellation and truncated below 1e-9 (small exponents)
+  int g1ser;
+  float g1[G1_TERMS_F];
 };
 
 MF_D float self(bool m, float a, float b) { return m ? a : b; }
@@ -66,7 +73,15 @@ MF_D float dd1s_f(float a, float b, float dab, float fa, float fb, const SmfCoef
   float z = dab / (2.f * ss), az = fabsf(z);
   bool zero = az == 0.f, near = !zero & (az < 0.5f);
   if (!zero & !near) return (fb - fa) / dab;
-  float g = zero ? C.al : (expm1f(C.al * log1pf(z)) - expm1f(C.al * log1pf(-z))) / (2.f * z);
+  float g;
+  if (C.g1ser) {  // (uniform: a launch constant) the series of g in z^2, Horner
+    const float zz = z * z;
+    g = C.g1[G1_TERMS_F - 1];
+#pragma unroll
+    for (int k = G1_TERMS_F - 2; k >= 0; k--) g = fmaf(g, zz, C.g1[k]);
+  } else {
+    g = zero ? C.al : (expm1f(C.al * log1pf(z)) - expm1f(C.al * log1pf(-z))) / (2.f * z);
+  }
   return (s > 0.f ? powf(ss, C.alm1) : C.zp1) * g;
 }
 
@@ -76,7 +91,7 @@ MF_D float deriv_f(float x, float fx, const SmfCoefF &C) {
   if (KIND == LOG) return 1.f / x;
   float xf = self(x > 0.f, x, 0.f);
   if (KIND == SQRT) return 1.f / (2.f * fx);  // (fx = sqrt(x), x >= 0)
-  return xf > 0.f ? C.al * powf(xf, C.alm1) : C.al * C.zp1;
+  return xf > 0.f ? C.al * (fx / xf) : C.al * C.zp1;  // al x^(al - 1) from fx = x^al at hand
 }
 
 // f[li, lj, lk] for li <= lj <= lk; dji = lj - li, dkj = lk - lj, dki = lk - li -- smf_kernel.hpp:148-192 (the widest
@@ -501,6 +516,17 @@ inline void smf_coef_f(int kind, double al, SmfCoefF &C) {
   // or 3 / al for powers, with its own term count)
   C.tau = (float)(pw ? (3.0 / al < DD2_TAU_F_POW ? 3.0 / al : DD2_TAU_F_POW) : DD2_TAU);
   for (int k = 0; k < DD2_TERMS; k++) C.c2[k] = (float)D.c2[k];
+  // g1: binom(al, 2m + 1); the series is used where the magnitudes of its terms at |z| = 1/2 add up to at most 4 al
+  // (its sum, g, is al at z = 0) and its last term is below 1e-9 al: exponents up to about 7, not al = 60.5
+  double b = al, tot = 0.0;  // binom(al, 1)
+  bool ok = kind == POW && al > 0.0;
+  for (int m = 0; m < G1_TERMS_F; m++) {
+    C.g1[m] = (float)b;
+    tot += std::fabs(b) * std::pow(0.25, m);
+    if (m == G1_TERMS_F - 1) ok &= std::fabs(b) * std::pow(0.25, m) <= 1e-9 * al;
+    b = b * (al - (2 * m + 1)) * (al - (2 * m + 2)) / ((2.0 * m + 2) * (2.0 * m + 3));  // binom(al, 2m + 3)
+  }
+  C.g1ser = ok && tot <= 4.0 * al ? 1 : 0;
 }
 
 }  // namespace mf
