@@ -55,24 +55,27 @@ MF_D float fun_f(float x, float al) {
 // rounded once (dab = b - a >= 0 and friends), so the near-coalescent branches see the same relative precision as
 // the FP64 kernel; with the order known, the choice of difference formula and of the cluster midpoint of the FP64
 // kernel becomes static.
-// f[a, b], a <= b, dab = b - a -- smf_kernel.hpp:84-115
+// f[a, b], a <= b, dab = b - a, rdab = 1 / dab (1 where dab = 0), ra = 1 / a (log and powers) -- smf_kernel.hpp:84-115.
+// Quotients by dab and a are products with the matrix's shared reciprocals (smf_rec_f): a correctly rounded
+// division costs about as much as the reciprocal it is built on, and the three eigenvalues and three differences
+// serve every first and second divided difference of the matrix.
 template <int KIND>
-MF_D float dd1s_f(float a, float b, float dab, float fa, float fb, const SmfCoefF &C) {
-  if (KIND == EXP) return fb * self(dab > 0.f, -expm1f(-dab) / dab, 1.f);
+MF_D float dd1s_f(float a, float b, float dab, float rdab, float ra, float fa, float fb, const SmfCoefF &C) {
+  if (KIND == EXP) return fb * self(dab > 0.f, -expm1f(-dab) * rdab, 1.f);
   if (KIND == LOG) {
-    float s = 0.5f * (a + b), z = dab / (a + b), az = fabsf(z), z2 = z * z;
-    if (az < 1e-3f) return (1.f + z2 / 3.f + z2 * z2 / 5.f + z2 * z2 * z2 / 7.f) / s;
+    const float rs = 1.f / (a + b), z = dab * rs, az = fabsf(z), z2 = z * z;
+    if (az < 1e-3f) return (1.f + z2 / 3.f + z2 * z2 / 5.f + z2 * z2 * z2 / 7.f) * (2.f * rs);
     // log(b / a) as log1p(dab / a), free of log |A| (whose ulp a difference of two logs would carry) and within a few
     // ulp for every ratio, so one form serves the near and the far pairs (the FP64 form's atanh branch for
     // 1e-3 <= |z| < 0.5 would be a third divergent path); a <= 0 keeps the difference of logs, with its infinities
     // and NaNs
-    return (a > 0.f ? log1pf(dab / a) : logf(b) - logf(a)) / dab;
+    return (a > 0.f ? log1pf(dab * ra) : logf(b) - logf(a)) * rdab;
   }
   if (KIND == SQRT) return 1.f / (fa + fb);  // (fa, fb: the square roots of a, b >= 0)
   float s = 0.5f * (a + b), ss = self(s > 0.f, s, 1.f);
-  float z = dab / (2.f * ss), az = fabsf(z);
+  float z = dab * (s > 0.f ? 1.f / (a + b) : 0.5f), az = fabsf(z);
   bool zero = az == 0.f, near = !zero & (az < 0.5f);
-  if (!zero & !near) return (fb - fa) / dab;
+  if (!zero & !near) return (fb - fa) * rdab;
   float g;
   if (C.g1ser) {  // (uniform: a launch constant) the series of g in z^2, Horner
     const float zz = z * z;
@@ -85,19 +88,23 @@ MF_D float dd1s_f(float a, float b, float dab, float fa, float fb, const SmfCoef
   return (s > 0.f ? powf(ss, C.alm1) : C.zp1) * g;
 }
 
+// f'(x) from fx = f(x) and rx = 1 / x (log and powers)
 template <int KIND>
-MF_D float deriv_f(float x, float fx, const SmfCoefF &C) {
+MF_D float deriv_f(float x, float fx, float rx, const SmfCoefF &C) {
   if (KIND == EXP) return fx;
-  if (KIND == LOG) return 1.f / x;
+  if (KIND == LOG) return rx;
   float xf = self(x > 0.f, x, 0.f);
   if (KIND == SQRT) return 1.f / (2.f * fx);  // (fx = sqrt(x), x >= 0)
   return xf > 0.f ? C.al * (fx / xf) : C.al * C.zp1;  // al x^(al - 1) from fx = x^al at hand
 }
 
-// f[li, lj, lk] for li <= lj <= lk; dji = lj - li, dkj = lk - lj, dki = lk - li -- smf_kernel.hpp:148-192 (the widest
-// difference is the denominator, the middle eigenvalue the cluster centre)
-template <int KIND>
-MF_D float dd2s_f(float lj, float lk, float fj, float Dij, float Djk, float dji, float dkj, float dki,
+// f[li, lj, lk] for li <= lj <= lk; dji = lj - li, dkj = lk - lj, dki = lk - li, rlj = 1 / lj (log and powers),
+// rdki = 1 / dki (1 where dki = 0) -- smf_kernel.hpp:148-192 (the widest difference is the denominator, the middle
+// eigenvalue the cluster centre).  SHAPE is what the caller knows statically: 0 three distinct indices, 1 li = lj
+// (dji = 0), 2 lj = lk (dkj = 0).  With one offset zero, the complete homogeneous polynomials h_k(u, w) of the
+// cluster series are powers of the other, and the series is one Horner sum (one FMA a term instead of three).
+template <int KIND, int SHAPE>
+MF_D float dd2s_f(float lj, float lk, float fj, float rlj, float Dij, float Djk, float dji, float dkj, float rdki,
                   const SmfCoefF &C) {
   bool cluster;
   if (KIND == EXP) cluster = (dkj + dji) <= 1.f;
@@ -108,30 +115,39 @@ MF_D float dd2s_f(float lj, float lk, float fj, float Dij, float Djk, float dji,
     if (KIND == EXP) {
       u = -dji; w = dkj; scale = fj;
     } else {
-      u = -dji / lj; w = dkj / lj;
-      scale = (KIND == LOG ? 1.f : fj) / (lj * lj);
+      u = -dji * rlj; w = dkj * rlj;
+      scale = (KIND == LOG ? rlj : fj * rlj) * rlj;
     }
     constexpr int NT = (KIND == POW || KIND == SQRT) ? DD2_TERMS_F_POW : DD2_TERMS_F;
-    float h = 1.f, wk = 1.f, sm = C.c2[0];
+    float sm;
+    if (SHAPE == 0) {
+      float h = 1.f, wk = 1.f;
+      sm = C.c2[0];
 #pragma unroll
-    for (int k = 1; k < NT; k++) {
-      wk = wk * w;
-      h = fmaf(u, h, wk);
-      sm = fmaf(C.c2[k], h, sm);
+      for (int k = 1; k < NT; k++) {
+        wk = wk * w;
+        h = fmaf(u, h, wk);
+        sm = fmaf(C.c2[k], h, sm);
+      }
+    } else {
+      const float x = SHAPE == 1 ? w : u;
+      sm = C.c2[NT - 1];
+#pragma unroll
+      for (int k = NT - 2; k >= 0; k--) sm = fmaf(sm, x, C.c2[k]);
     }
     out = scale * sm;
   } else {
-    out = (Djk - Dij) / self(dki != 0.f, dki, 1.f);
+    out = (Djk - Dij) * rdki;
   }
   if (KIND == POW || KIND == SQRT) out = self(lk > 0.f, out, C.z2);
   return out;
 }
 
 template <int KIND>
-MF_D float dd2_same_f(float lf, float fl, float Dll, const SmfCoefF &C) {
+MF_D float dd2_same_f(float lf, float fl, float rl, float Dll, const SmfCoefF &C) {
   bool cluster = KIND == EXP ? true : (lf > 0.f);
   float out = KIND == EXP ? self(cluster, fl * C.c2[0], Dll - Dll)
-                          : self(cluster, ((KIND == LOG ? 1.f : fl) / (lf * lf)) * C.c2[0], Dll - Dll);
+                          : self(cluster, ((KIND == LOG ? rl : fl * rl) * rl) * C.c2[0], Dll - Dll);
   if (KIND == POW || KIND == SQRT) out = self(lf > 0.f, out, C.z2);
   return out;
 }
@@ -458,14 +474,32 @@ MF_D void smf_spectrum_f(const SmfInF &in, const SmfCoefF &C, SmfSpecF &Sp) {
   }
 }
 
+// the reciprocals a matrix's divided differences share: of the eigenvalue differences (1 where one is 0) and, for
+// log and powers, of the eigenvalues
+struct SmfRecF {
+  float rd10, rd20, rd21, rl[3];
+};
+
+template <int KIND>
+MF_D SmfRecF smf_rec_f(const SmfSpecF &Sp) {
+  SmfRecF R;
+  R.rd10 = 1.f / self(Sp.d10 != 0.f, Sp.d10, 1.f);
+  R.rd20 = 1.f / self(Sp.d20 != 0.f, Sp.d20, 1.f);
+  R.rd21 = 1.f / self(Sp.d21 != 0.f, Sp.d21, 1.f);
+#pragma unroll
+  for (int i = 0; i < 3; i++) R.rl[i] = (KIND == LOG || KIND == POW) ? 1.f / Sp.lf[i] : 0.f;
+  return R;
+}
+
 // first divided differences D_ij = f[l_i, l_j] (D_ii = f'(l_i)) in FP32
 template <int KIND>
 MF_D void smf_dm_f(const SmfSpecF &Sp, const SmfCoefF &C, float Dm[3][3]) {
-  const float D01 = dd1s_f<KIND>(Sp.lf[0], Sp.lf[1], Sp.d10, Sp.fl[0], Sp.fl[1], C);
-  const float D02 = dd1s_f<KIND>(Sp.lf[0], Sp.lf[2], Sp.d20, Sp.fl[0], Sp.fl[2], C);
-  const float D12 = dd1s_f<KIND>(Sp.lf[1], Sp.lf[2], Sp.d21, Sp.fl[1], Sp.fl[2], C);
-  Dm[0][0] = deriv_f<KIND>(Sp.lf[0], Sp.fl[0], C); Dm[1][1] = deriv_f<KIND>(Sp.lf[1], Sp.fl[1], C);
-  Dm[2][2] = deriv_f<KIND>(Sp.lf[2], Sp.fl[2], C);
+  const SmfRecF R = smf_rec_f<KIND>(Sp);
+  const float D01 = dd1s_f<KIND>(Sp.lf[0], Sp.lf[1], Sp.d10, R.rd10, R.rl[0], Sp.fl[0], Sp.fl[1], C);
+  const float D02 = dd1s_f<KIND>(Sp.lf[0], Sp.lf[2], Sp.d20, R.rd20, R.rl[0], Sp.fl[0], Sp.fl[2], C);
+  const float D12 = dd1s_f<KIND>(Sp.lf[1], Sp.lf[2], Sp.d21, R.rd21, R.rl[1], Sp.fl[1], Sp.fl[2], C);
+#pragma unroll
+  for (int i = 0; i < 3; i++) Dm[i][i] = deriv_f<KIND>(Sp.lf[i], Sp.fl[i], R.rl[i], C);
   Dm[0][1] = Dm[1][0] = D01; Dm[0][2] = Dm[2][0] = D02; Dm[1][2] = Dm[2][1] = D12;
 }
 
@@ -488,17 +522,26 @@ MF_D void smf_d2_f(const SmfSpecF &Sp, const float Dm[3][3], const SmfCoefF &C, 
         }
     return;
   }
+  const SmfRecF R = smf_rec_f<KIND>(Sp);
   const float dd[3][3] = {{0.f, Sp.d10, Sp.d20}, {0.f, 0.f, Sp.d21}, {0.f, 0.f, 0.f}};
+  const float rd[3][3] = {{1.f, R.rd10, R.rd20}, {1.f, 1.f, R.rd21}, {1.f, 1.f, 1.f}};
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = i; j < 3; j++)
 #pragma unroll
       for (int l = j; l < 3; l++) {
-        const float d = (i == j && j == l)
-                            ? dd2_same_f<KIND>(Sp.lf[i], Sp.fl[i], Dm[i][i], C)
-                            : dd2s_f<KIND>(Sp.lf[j], Sp.lf[l], Sp.fl[j], Dm[i][j], Dm[j][l], dd[i][j], dd[j][l],
-                                           dd[i][l], C);
+        float d;
+        if (i == j && j == l) {
+          d = dd2_same_f<KIND>(Sp.lf[i], Sp.fl[i], R.rl[i], Dm[i][i], C);
+        } else {
+          d = i == j ? dd2s_f<KIND, 1>(Sp.lf[j], Sp.lf[l], Sp.fl[j], R.rl[j], Dm[i][j], Dm[j][l], 0.f, dd[j][l],
+                                       rd[i][l], C)
+              : j == l ? dd2s_f<KIND, 2>(Sp.lf[j], Sp.lf[l], Sp.fl[j], R.rl[j], Dm[i][j], Dm[j][l], dd[i][j], 0.f,
+                                         rd[i][l], C)
+                       : dd2s_f<KIND, 0>(Sp.lf[j], Sp.lf[l], Sp.fl[j], R.rl[j], Dm[i][j], Dm[j][l], dd[i][j],
+                                         dd[j][l], rd[i][l], C);
+        }
         D2[i][j][l] = D2[i][l][j] = D2[j][i][l] = D2[j][l][i] = D2[l][i][j] = D2[l][j][i] = d;
       }
 }
