@@ -126,6 +126,9 @@ __global__ void __launch_bounds__(SMFV_TPB, MINB)
   }
   float Dm[3][3];
   smf_dm_f<KIND>(Sp, C, Dm);
+  // the second divided differences before the J boxes: their 10 values stay live across them instead of the spectrum
+  float D2[3][3][3];
+  if (ORDER >= 2) smf_d2_f<KIND>(Sp, Dm, C, D2);
   float P[6][3];
   smfx_pvec(V, P);
   int nb = 0;  // boxes issued by this warp; box k uses buffer k & 1
@@ -142,8 +145,6 @@ __global__ void __launch_bounds__(SMFV_TPB, MINB)
     }
   }
   if (ORDER >= 2) {
-    float D2[3][3][3];
-    smf_d2_f<KIND>(Sp, Dm, C, D2);
     float G[56];
     smfx_hform(P, D2, G);
 #pragma unroll

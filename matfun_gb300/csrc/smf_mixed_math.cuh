@@ -64,12 +64,12 @@ MF_D float dd1s_f(float a, float b, float dab, float rdab, float ra, float fa, f
   if (KIND == EXP) return fb * self(dab > 0.f, -expm1f(-dab) * rdab, 1.f);
   if (KIND == LOG) {
     const float rs = 1.f / (a + b), z = dab * rs, az = fabsf(z), z2 = z * z;
-    if (az < 1e-3f) return (1.f + z2 / 3.f + z2 * z2 / 5.f + z2 * z2 * z2 / 7.f) * (2.f * rs);
+    if (az < 1e-3f) return (1.f + z2 * (1.f / 3.f) + z2 * z2 * 0.2f + z2 * z2 * z2 * (1.f / 7.f)) * (2.f * rs);
     // log(b / a) as log1p(dab / a), free of log |A| (whose ulp a difference of two logs would carry) and within a few
     // ulp for every ratio, so one form serves the near and the far pairs (the FP64 form's atanh branch for
     // 1e-3 <= |z| < 0.5 would be a third divergent path); a <= 0 keeps the difference of logs, with its infinities
-    // and NaNs
-    return (a > 0.f ? log1pf(dab * ra) : logf(b) - logf(a)) * rdab;
+    // and NaNs (fa, fb: log a, log b)
+    return (a > 0.f ? log1pf(dab * ra) : fb - fa) * rdab;
   }
   if (KIND == SQRT) return 1.f / (fa + fb);  // (fa, fb: the square roots of a, b >= 0)
   float s = 0.5f * (a + b), ss = self(s > 0.f, s, 1.f);
@@ -262,8 +262,9 @@ MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E) {
   // mean of the diagonal and deviator, float-float
   ffl s01 = two_sum(a[0], a[1]), s = two_sum(s01.hi, a[2]);
   s = fast_two_sum(s.hi, s.lo + s01.lo);
-  float q1 = s.hi / 3.f;
-  float q2 = (fmaf(-q1, 3.f, s.hi) + s.lo) / 3.f;
+  // (q1 within an ulp of s.hi / 3; the residue s.hi - 3 q1 is exact, so q1 + q2 is the mean to float-float accuracy)
+  float q1 = s.hi * (1.f / 3.f);
+  float q2 = (fmaf(-q1, 3.f, s.hi) + s.lo) * (1.f / 3.f);
   const ffl m = fast_two_sum(q1, q2);
   // deviator in FP32 (the input of the trigonometric root only), from the float-float mean: a - m.hi is exact near
   // the mean, and subtracting m.lo too leaves it traceless to FP32 rounding, as the root formula assumes (the
@@ -287,7 +288,7 @@ MF_D void smf_eigsys_ff(const SmfInF &in, SmfEigF &E) {
   float pg = self(iso, 1.f, p), qg = self(iso, 0.f, q);
   float r = 3.f * SQRT6 * qg / (pg * sqrtf(pg));
   r = self(r > 1.f, 1.f, self(r < -1.f, -1.f, r));
-  float t = sqrtf(2.f * pg / 3.f), ph = acosf(r) / 3.f;
+  float t = sqrtf(pg * (2.f / 3.f)), ph = acosf(r) * (1.f / 3.f);
   float sh = t * cosf(self(r >= 0.f, ph, ph + TWO_PI_3));
   float m00 = g0 - sh, m11 = g1 - sh, m22 = g2 - sh;
   float cxv = g3 * g5 - g4 * m11, cyv = g4 * g3 - m00 * g5, czv = m00 * m11 - g3 * g3;
