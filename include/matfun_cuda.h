@@ -62,8 +62,8 @@ int gmf_cuda_eval_f32(int kind, double alpha, int64_t n, const float *A, float *
  * matfun_gb300/autotune.py): 0 = per-entry stores of the expanded rows; 1 = J / H rows staged in shared-memory boxes
  * of 32 rows x 128 bytes and written by the TMA unit; 2 = the same with boxes of 32 rows x 64 bytes (less shared
  * memory and fewer registers per thread, more resident warps); 3 = 64-byte boxes with fewer registers per thread and
- * more resident warps than 2 at order 2.  J and H must be 16-byte aligned for 1-3, else the call takes path 0.  Results agree
- * to FP32 rounding.  Returns 0 or -1 (unknown order or path). */
+ * more resident warps than 2 at order 2.  Defaults: 2 at order 1, 1 at order 2.  J and H must be 16-byte aligned for
+ * 1-3, else the call takes path 0.  Results agree to FP32 rounding.  Returns 0 or -1 (unknown order or path). */
 int matfun_cuda_smf_f32_tune(int order, int variant);
 
 /* Adjoints (no counterpart in the reference): contractions of J and H with directions, without

@@ -120,7 +120,7 @@ extern "C" int smf_cuda_eval_f32(int kind, double alpha, int64_t n, const float 
 }
 
 namespace mf {
-std::atomic<int> smf_voigt_variant[2] = {{2}, {3}};  // the store path of the FP32 Voigt kernels at orders 1, 2
+std::atomic<int> smf_voigt_variant[2] = {{2}, {1}};  // the store path of the FP32 Voigt kernels at orders 1, 2
 }
 
 extern "C" int matfun_cuda_smf_f32_tune(int order, int variant) {

@@ -92,25 +92,25 @@ __global__ void __launch_bounds__(SMFV_TPB, MINB)
   static_assert(ORDER == 1 || ORDER == 2, "J and H rows only");
   using B = SmfvBox<BW>;
   constexpr int NJB = (9 + B::CH - 1) / B::CH, NHB = (54 + B::CH - 1) / B::CH;  // boxes of a J and an H row
-  // two boxes per warp, aligned to the swizzle's period after at most ALIGN - 128 bytes of padding
-  __shared__ __align__(128) unsigned char raw[B::ALIGN - 128 + SMFV_TPB / 32 * 2 * B::BYTES];
-  __shared__ float sX[SMFV_TPB * 6];
+  // two boxes per warp, at the swizzle's period.  The CTA holds nothing else in shared memory (8 KB of 64-byte boxes),
+  // so that 14 CTAs leave the SM's smaller shared-memory carve-outs, and more L1 for the spilled registers, in reach.
+  __shared__ __align__(B::ALIGN) unsigned char raw[SMFV_TPB / 32 * 2 * B::BYTES];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t base = (int64_t)blockIdx.x * SMFV_TPB;
   const int cnt = (int)min((int64_t)SMFV_TPB, n - base);
-  for (int e = tid; e < cnt * 6; e += SMFV_TPB) sX[e] = x[base * 6 + e];
-  __syncthreads();
   const int64_t row0 = base + warp * 32;
-  if (row0 >= n) return;
+  // (a box off the swizzle's period would be written in the wrong order: such a CTA writes nothing)
+  if (row0 >= n || (smem_u32(raw) & (B::ALIGN - 1)) != 0) return;
   const bool live = tid < cnt;
   unsigned char *bufs[2];
-  bufs[0] = raw + ((B::ALIGN - (smem_u32(raw) & (B::ALIGN - 1))) & (B::ALIGN - 1)) + warp * 2 * B::BYTES;
+  bufs[0] = raw + warp * 2 * B::BYTES;
   bufs[1] = bufs[0] + B::BYTES;
 
-  // lanes past the end evaluate the identity (rows the TMA unit clips), so that the warp stays converged
+  // each lane reads its own matrix (the warp's 32 rows are 768 contiguous bytes); lanes past the end evaluate the
+  // identity (rows the TMA unit clips), so that the warp stays converged
   float xin[6];
 #pragma unroll
-  for (int k = 0; k < 6; k++) xin[k] = live ? sX[tid * 6 + k] : (k < 3 ? 1.f : 0.f);
+  for (int k = 0; k < 6; k++) xin[k] = live ? x[(base + tid) * 6 + k] : (k < 3 ? 1.f : 0.f);
   SmfInF in;
   voigt_in_f(xin, in);
   SmfSpecF Sp;
