@@ -20,8 +20,10 @@ __global__ void __launch_bounds__(SMFX_TPB) smf_mixed_kernel(int64_t n, const fl
 }
 
 
-// ---- Voigt layout, orders 1 and 2: J and H rows written by the TMA unit.  Each warp takes 32 consecutive matrices,
-// one per lane; a lane keeps its matrix's distinct J (21) and H (56) values in registers and writes its own row
+// ---- Voigt layout: J and H rows written by the TMA unit (orders 1 and 2), F by each lane (every order).  Each warp
+// takes 32 consecutive matrices, one per lane, and each lane reads its own input row: no staging, no CTA barrier, so
+// a warp starts when its own loads arrive and the warps of a CTA drift apart (boxes drain while other warps
+// compute).  A lane keeps its matrix's distinct J (21) and H (56) values in registers and writes its own row
 // chunks, weighted, as 16-byte shared-memory stores into a swizzled box of 32 rows x BW floats; one lane hands each
 // box to the TMA unit (columns and rows past the array are clipped by the unit), two boxes per warp in flight.  This
 // replaces the CTA-wide expansion through per-entry gathers and 4-byte stores.  Variants (the box width and the CTAs
@@ -89,18 +91,17 @@ __global__ void __launch_bounds__(SMFV_TPB, MINB)
     smf_mixed_voigt_kernel(int64_t n, const float *__restrict__ x, float *__restrict__ F,
                            const __grid_constant__ CUtensorMap mJ, const __grid_constant__ CUtensorMap mH,
                            const SmfCoefF C) {
-  static_assert(ORDER == 1 || ORDER == 2, "J and H rows only");
+  static_assert(ORDER >= 0 && ORDER <= 2, "F, J and H");
   using B = SmfvBox<BW>;
   constexpr int NJB = (9 + B::CH - 1) / B::CH, NHB = (54 + B::CH - 1) / B::CH;  // boxes of a J and an H row
-  // two boxes per warp, at the swizzle's period.  The CTA holds nothing else in shared memory (8 KB of 64-byte boxes),
-  // so that 14 CTAs leave the SM's smaller shared-memory carve-outs, and more L1 for the spilled registers, in reach.
-  __shared__ __align__(B::ALIGN) unsigned char raw[SMFV_TPB / 32 * 2 * B::BYTES];
+  // two boxes per warp, at the swizzle's period (none at order 0): the CTA's only shared memory
+  __shared__ __align__(B::ALIGN) unsigned char raw[ORDER == 0 ? 16 : SMFV_TPB / 32 * 2 * B::BYTES];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t base = (int64_t)blockIdx.x * SMFV_TPB;
   const int cnt = (int)min((int64_t)SMFV_TPB, n - base);
   const int64_t row0 = base + warp * 32;
   // (a box off the swizzle's period would be written in the wrong order: such a CTA writes nothing)
-  if (row0 >= n || (smem_u32(raw) & (B::ALIGN - 1)) != 0) return;
+  if (row0 >= n || (ORDER > 0 && (smem_u32(raw) & (B::ALIGN - 1)) != 0)) return;
   const bool live = tid < cnt;
   unsigned char *bufs[2];
   bufs[0] = raw + warp * 2 * B::BYTES;
@@ -124,6 +125,7 @@ __global__ void __launch_bounds__(SMFV_TPB, MINB)
       o[s] = V[a][0] * Sp.fl[0] * V[b][0] + V[a][1] * Sp.fl[1] * V[b][1] + V[a][2] * Sp.fl[2] * V[b][2];
     }
   }
+  if (ORDER == 0) return;
   float Dm[3][3];
   smf_dm_f<KIND>(Sp, C, Dm);
   // the second divided differences before the J boxes: their 10 values stay live across them instead of the spectrum
@@ -186,6 +188,12 @@ cudaError_t smf_mixed_launch_t(double al, int64_t n, const float *x, bool mat, f
   smf_coef_f(KIND, al, C);
   const int order = H ? 2 : (J ? 1 : 0);
   const int variant = order >= 1 ? smf_voigt_variant[order - 1].load() : 0;
+  if (!mat && order == 0) {  // F only: the per-lane kernel without boxes (no tensor maps; its map arguments unused)
+    CUtensorMap none{};
+    smf_mixed_voigt_kernel<KIND, 0, 16, 16>
+        <<<(unsigned)((n + SMFV_TPB - 1) / SMFV_TPB), SMFV_TPB, 0, st>>>(n, x, F, none, none, C);
+    return cudaGetLastError();
+  }
   if (!mat && variant != 0) {
     const cudaError_t e = order == 2 ? smfv_launch<KIND, 2>(variant, n, x, F, J, H, C, st)
                                      : smfv_launch<KIND, 1>(variant, n, x, F, J, H, C, st);
@@ -198,8 +206,7 @@ cudaError_t smf_mixed_launch_t(double al, int64_t n, const float *x, bool mat, f
     else smf_mixed_kernel<KIND, 0, true><<<blocks, SMFX_TPB, 0, st>>>(n, x, F, J, H, C);
   } else {
     if (order == 2) smf_mixed_kernel<KIND, 2, false><<<blocks, SMFX_TPB, 0, st>>>(n, x, F, J, H, C);
-    else if (order == 1) smf_mixed_kernel<KIND, 1, false><<<blocks, SMFX_TPB, 0, st>>>(n, x, F, J, H, C);
-    else smf_mixed_kernel<KIND, 0, false><<<blocks, SMFX_TPB, 0, st>>>(n, x, F, J, H, C);
+    else smf_mixed_kernel<KIND, 1, false><<<blocks, SMFX_TPB, 0, st>>>(n, x, F, J, H, C);
   }
   return cudaGetLastError();
 }

@@ -244,6 +244,35 @@ def test_smf_mixed_voigt_store_paths(kind, alpha, order):
         lib.matfun_cuda_smf_f32_tune(order, 2 if order == 1 else 1)  # the library's defaults
 
 
+@pytest.mark.parametrize("kind,alpha", [(1, 0.0), (2, 0.7)])
+def test_smf_mixed_voigt_order0_tails(kind, alpha):
+    """Voigt order 0 runs the per-lane kernel (each lane reads its own row and writes its own F row): on batch tails
+    around the 32 matrices of a warp and the 64 of a CTA, F equals the F of the matrix layout (the CTA tile) on the
+    same matrices to rounding, with the same NaN rows, and nothing past row n is written"""
+    import torch
+
+    import matfun_gb300
+    from matfun_gb300 import workloads as w
+    lib = matfun_gb300.load()
+    for n in (1, 7, 31, 32, 33, 63, 64, 65, 97, 129, 1000):
+        A = w.c2_smf_spd(n, seed=60 + n, as_voigt=False)
+        if n > 5:
+            A[5, 0, 1] = A[5, 1, 0] = np.nan  # a NaN input row
+        X = np.ascontiguousarray(np.stack([A[:, 0, 0], A[:, 1, 1], A[:, 2, 2], A[:, 0, 1], A[:, 0, 2], A[:, 1, 2]], 1))
+        F = torch.full((n + 3, 6), 7.0, dtype=torch.float32, device="cuda")
+        Fm = torch.full((n, 9), 7.0, dtype=torch.float32, device="cuda")
+        dX, dA = torch.from_numpy(X).cuda(), torch.from_numpy(np.ascontiguousarray(A.reshape(n, 9))).cuda()
+        assert lib.smf_cuda_eval_f32(kind, alpha, n, dX.data_ptr(), F.data_ptr(), None, None, None) == 0
+        assert lib.smf_cuda_eval_matrix_f32(kind, alpha, n, dA.data_ptr(), Fm.data_ptr(), None, None, None) == 0
+        torch.cuda.synchronize()
+        assert bool((F[n:] == 7.0).all()), f"n={n}: rows past n written"
+        got = F[:n].double().cpu().numpy()
+        m = Fm.double().cpu().numpy()
+        ref = np.stack([m[:, 0], m[:, 4], m[:, 8], m[:, 1], m[:, 2], m[:, 5]], 1)
+        assert np.array_equal(np.isnan(got), np.isnan(ref)), f"n={n}"
+        assert maxrel(got, ref) <= 1e-6, f"n={n}"
+
+
 @pytest.mark.parametrize("scale,order", [(1e-30, 0), (1e30, 0), (2.0 ** -20, 2), (2.0 ** 40, 2)])
 def test_smf_mixed_extreme_scales(scale, order):
     """the float-float eigensystem scales by a power of two first: matrices of 1e-30 and 1e30 (FP32 range) keep the
