@@ -62,34 +62,34 @@ PIPE_FLOPS = {
     "gmf/pow0.3/2/f32": {"fp64": 4468, "fp32": 20323},
     "gmf/log/tangent/f64": {"fp64": 7661, "fp32": 7534},
     "smf/log/2/f64/c0": {"fp64": 2877, "fp32": 90},
-    "smf/exp/0/f32": {"fp64": None, "fp32": 1969},
+    "smf/exp/0/f32": {"fp64": None, "fp32": 1931},
     "smf/exp/0/f64": {"fp64": 701, "fp32": 14},
-    "smf/exp/1/f32": {"fp64": None, "fp32": 2378},
+    "smf/exp/1/f32": {"fp64": None, "fp32": 2330},
     "smf/exp/1/f64": {"fp64": 1104, "fp32": 20},
-    "smf/exp/2/f32": {"fp64": None, "fp32": 3680},
+    "smf/exp/2/f32": {"fp64": None, "fp32": 3463},
     "smf/exp/2/f64": {"fp64": 2348, "fp32": 214},
-    "smf/log/0/f32": {"fp64": None, "fp32": 2229},
+    "smf/log/0/f32": {"fp64": None, "fp32": 2189},
     "smf/log/0/f64": {"fp64": 882, "fp32": 22},
-    "smf/log/1/f32": {"fp64": None, "fp32": 2738},
+    "smf/log/1/f32": {"fp64": None, "fp32": 2629},
     "smf/log/1/f64": {"fp64": 1331, "fp32": 41},
-    "smf/log/2/f32": {"fp64": None, "fp32": 3968},
+    "smf/log/2/f32": {"fp64": None, "fp32": 3673},
     "smf/log/2/f64": {"fp64": 2956, "fp32": 263},
-    "smf/sqrt/0/f32": {"fp64": None, "fp32": 1957},
+    "smf/sqrt/0/f32": {"fp64": None, "fp32": 1919},
     "smf/sqrt/0/f64": {"fp64": 653, "fp32": 14},
-    "smf/sqrt/1/f32": {"fp64": None, "fp32": 2282},
+    "smf/sqrt/1/f32": {"fp64": None, "fp32": 2210},
     "smf/sqrt/1/f64": {"fp64": 999, "fp32": 14},
-    "smf/sqrt/2/f32": {"fp64": None, "fp32": 3759},
+    "smf/sqrt/2/f32": {"fp64": None, "fp32": 3284},
     "smf/sqrt/2/f64": {"fp64": 2726, "fp32": 256},
-    "smf/pow/0/f32": {"fp64": None, "fp32": 2116},
+    "smf/pow/0/f32": {"fp64": None, "fp32": 2078},
     "smf/pow/0/f64": {"fp64": 981, "fp32": 14},
-    "smf/pow/1/f32": {"fp64": None, "fp32": 2861},
+    "smf/pow/1/f32": {"fp64": None, "fp32": 2570},
     "smf/pow/1/f64": {"fp64": 1998, "fp32": 31},
-    "smf/pow/2/f32": {"fp64": None, "fp32": 4274},
+    "smf/pow/2/f32": {"fp64": None, "fp32": 3702},
     "smf/pow/2/f64": {"fp64": 3726, "fp32": 273},
     "smf/log/vjp/f64": {"fp64": 1381, "fp32": 49},
     "smf/log/hvp/f64": {"fp64": 2170, "fp32": 90},
-    "smf/log/vjp/f32": {"fp64": None, "fp32": 2726},
-    "smf/log/hvp/f32": {"fp64": None, "fp32": 3254},
+    "smf/log/vjp/f32": {"fp64": None, "fp32": 2636},
+    "smf/log/hvp/f32": {"fp64": None, "fp32": 2992},
     "gmf/pow0.3/vjp/f64": {"fp64": 4288, "fp32": 10652},
     "gmf/pow0.3/hvp/f64": {"fp64": 9067, "fp32": 24339},
     "gmf/pow0.3/vjp/f32": {"fp64": 3263, "fp32": 11624},
@@ -473,10 +473,12 @@ def mixed_sweep(lib, args, dev, pk):
             ms32, ms64, err, ns = pair_f32_f64(lib.smf_cuda_eval_f32, lib.smf_cuda_eval, x32, 6, kind, alpha, order,
                                                args.mixed_steps, dev)
             call = CpuCall("smf_eval", kind, alpha, xh[:16384].astype(np.float64), order)
+            rf32 = roofline(n, ms32, io_bytes("smf_voigt", order, 4), f"smf/{name}/{order}/f32", pk)
             rows.append({"kind": name, "alpha": alpha, "order": order, "mixed_ms": ms32, "fp64_ms": ms64,
                          "mixed_matrices_per_s": n / (ms32 * 1e-3), "fp64_matrices_per_s": n / (ms64 * 1e-3),
                          "speedup_vs_fp64": ms64 / ms32, "err_vs_fp64": err,
-                         "roofline": roofline(n, ms32, io_bytes("smf_voigt", order, 4), f"smf/{name}/{order}/f32", pk),
+                         "mixed_hbm_frac": rf32["hbm"]["frac"] if "hbm" in rf32 else rf32["frac"],
+                         "roofline": rf32,
                          "fp64_roofline": roofline(n, ms64, io_bytes("smf_voigt", order), f"smf/{name}/{order}/f64",
                                                    pk),
                          "cpu_baseline": cpu_baseline(call, args.cpu_budget_row,
@@ -486,6 +488,7 @@ def mixed_sweep(lib, args, dev, pk):
                         "[1e-12,1], FP32 storage; every kind and order; errors of the FP32 results against the FP64 "
                         "path on the same values (per batch, and per matrix where its outputs fit FP32's range)",
             "err_sample": ns, "rows": rows,
+            "log_o2_mixed_hbm_frac": next(r["mixed_hbm_frac"] for r in rows if r["kind"] == "log" and r["order"] == 2),
             "store_path": {"chosen": {str(o): autotune.SMF_F32_PATHS[p] for o, p in path.items()},
                            "log_ms": {str(o): {autotune.SMF_F32_PATHS[p]: round(t, 4) for p, t in d.items()}
                                       for o, d in path_ms.items()}}}
