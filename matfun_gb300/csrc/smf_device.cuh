@@ -236,9 +236,9 @@ MF_D void smf_eigen(const double *v, double al, double lam[3], double fl[3], dou
 
 // ---- first divided differences f[a, b] (f[a, a] = f'(a)) in forms stable for close arguments
 // exp: e^max(a, b) (1 - e^-d) / d, d = |a - b| (no overflow, no cancellation)
-// log: with s = (a + b) / 2, z = (a - b) / (a + b): log a - log b = 2 atanh z, so f[a, b] = atanh(z) / (z s) for
-//      |z| < 0.5 (1 / s at z = 0; near 0 the ratio atanh(z) / z = 1 + z^2 / 3 + ... hardly depends on z, so the
-//      rounding of z does not reach it and no separate series is needed), and the plain quotient (fa - fb) / (a - b)
+// log: with s = (a + b) / 2, z = (a - b) / (a + b): log a - log b = 2 atanh z, so f[a, b] = 2 atanh(z) / (a - b)
+//      = atanh(z) / (z s) for |z| < 0.5 (1 / s at z = 0; z's rounding reaches the result at about an ulp, and no
+//      separate series is needed near z = 0), and the plain quotient (fa - fb) / (a - b)
 //      of the logarithms already at hand for |z| >= 0.5 (a / b >= 3: their difference is >= log 3, so it is as
 //      accurate as log a - log b evaluated anew).  Two forms instead of three: the lanes of a warp split between them,
 //      and the warp pays for every form one of its lanes takes.
@@ -254,18 +254,21 @@ MF_D double smf_dd1(double a, double b, double fa, double fb, const SmfCoef &C) 
     return d > 0 ? fmax * (-expm1(-d) / d) : fmax;
   }
   if (KIND == LOG) {
-    const double s = 0.5 * (a + b), z = (a - b) / (a + b), az = fabs(z);
-    if (az >= 0.5) return (fa - fb) / (a - b);
-    const double zs = z != 0.0 ? z : 0.5;
-    return (z != 0.0 ? atanh(zs) / zs : 1.0) / s;
+    // (atanh(z) / z) / s = 2 atanh(z) / (a - b): both forms are products with 1 / (a - b), the quotient's only
+    // division (an FP64 division costs several FP64 instructions; z = 0: 1 / s)
+    const double r = 1.0 / (a + b), z = (a - b) * r, az = fabs(z);
+    const double dab = a - b, rd = 1.0 / (dab != 0.0 ? dab : 1.0);
+    if (az >= 0.5) return (fa - fb) * rd;
+    return z != 0.0 ? 2.0 * atanh(z) * rd : 2.0 * r;
   }
   a = a > 0 ? a : 0.0;
   b = b > 0 ? b : 0.0;
   if (KIND == SQRT) return 1.0 / (sqrt(a) + sqrt(b));
   const double s = 0.5 * (a + b), sp = s > 0 ? s : 1.0;
-  const double z = (a - b) / (2.0 * sp), az = fabs(z);
-  if (az >= 0.5) return (fa - fb) / (a - b);
-  const double g = az == 0 ? C.al : (expm1(C.al * log1p(z)) - expm1(C.al * log1p(-z))) / (2.0 * z);
+  const double dab = a - b, rd = 1.0 / (dab != 0.0 ? dab : 1.0);  // (1 / (2 z) = sp / (a - b))
+  const double z = dab * (s > 0 ? 1.0 / (a + b) : 0.5), az = fabs(z);
+  if (az >= 0.5) return (fa - fb) * rd;
+  const double g = az == 0 ? C.al : (expm1(C.al * log1p(z)) - expm1(C.al * log1p(-z))) * (sp * rd);
   return (s > 0 ? pow_split(sp, C.bh1, C.bl1) : C.zp1) * g;
 }
 
@@ -304,8 +307,9 @@ MF_D double smf_dd2(double li, double lj, double lk, double fi, double fj, doubl
     u = lo - md; w = hi - md; scale = f1;
   } else {
     cluster = (md > 0) & (md - lo <= C.tau * md) & (hi - md <= C.tau * md);
-    u = (lo - md) / md; w = (hi - md) / md;
-    scale = (KIND == LOG ? 1.0 : f1) / (md * md);
+    const double im = 1.0 / md;  // (one division for the offsets and the scale)
+    u = (lo - md) * im; w = (hi - md) * im;
+    scale = (KIND == LOG ? im : f1 * im) * im;
   }
   double out;
   if (cluster) {
