@@ -61,7 +61,7 @@ PIPE_FLOPS = {
     "gmf/sqrt/2/f32": {"fp64": 3804, "fp32": 20265},
     "gmf/pow0.3/2/f32": {"fp64": 4468, "fp32": 20323},
     "gmf/log/tangent/f64": {"fp64": 7661, "fp32": 7534},
-    "smf/log/2/f64/c0": {"fp64": 2877, "fp32": 90},
+    "smf/log/2/f64/c0": {"fp64": 2577, "fp32": 45},
     "smf/exp/0/f32": {"fp64": None, "fp32": 1931},
     "smf/exp/0/f64": {"fp64": 701, "fp32": 14},
     "smf/exp/1/f32": {"fp64": None, "fp32": 2330},
@@ -71,23 +71,23 @@ PIPE_FLOPS = {
     "smf/log/0/f32": {"fp64": None, "fp32": 2189},
     "smf/log/0/f64": {"fp64": 882, "fp32": 22},
     "smf/log/1/f32": {"fp64": None, "fp32": 2629},
-    "smf/log/1/f64": {"fp64": 1331, "fp32": 41},
+    "smf/log/1/f64": {"fp64": 1290, "fp32": 26},
     "smf/log/2/f32": {"fp64": None, "fp32": 3673},
-    "smf/log/2/f64": {"fp64": 2956, "fp32": 263},
+    "smf/log/2/f64": {"fp64": 2664, "fp32": 221},
     "smf/sqrt/0/f32": {"fp64": None, "fp32": 1919},
     "smf/sqrt/0/f64": {"fp64": 653, "fp32": 14},
     "smf/sqrt/1/f32": {"fp64": None, "fp32": 2210},
     "smf/sqrt/1/f64": {"fp64": 999, "fp32": 14},
     "smf/sqrt/2/f32": {"fp64": None, "fp32": 3284},
-    "smf/sqrt/2/f64": {"fp64": 2726, "fp32": 256},
+    "smf/sqrt/2/f64": {"fp64": 2400, "fp32": 214},
     "smf/pow/0/f32": {"fp64": None, "fp32": 2078},
     "smf/pow/0/f64": {"fp64": 981, "fp32": 14},
     "smf/pow/1/f32": {"fp64": None, "fp32": 2570},
-    "smf/pow/1/f64": {"fp64": 1998, "fp32": 31},
+    "smf/pow/1/f64": {"fp64": 1971, "fp32": 19},
     "smf/pow/2/f32": {"fp64": None, "fp32": 3702},
-    "smf/pow/2/f64": {"fp64": 3726, "fp32": 273},
-    "smf/log/vjp/f64": {"fp64": 1381, "fp32": 49},
-    "smf/log/hvp/f64": {"fp64": 2170, "fp32": 90},
+    "smf/pow/2/f64": {"fp64": 3373, "fp32": 219},
+    "smf/log/vjp/f64": {"fp64": 1320, "fp32": 32},
+    "smf/log/hvp/f64": {"fp64": 1870, "fp32": 45},
     "smf/log/vjp/f32": {"fp64": None, "fp32": 2636},
     "smf/log/hvp/f32": {"fp64": None, "fp32": 2992},
     "gmf/pow0.3/vjp/f64": {"fp64": 4288, "fp32": 10652},
